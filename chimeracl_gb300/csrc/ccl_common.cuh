@@ -1,0 +1,82 @@
+// Shared definitions for the chimeracl_gb300 CUDA kernels (sm_103a).
+//
+// Layout conventions (identical to the reference's device containers):
+//  * particles: structure of arrays, one array per component (x, y, z, px,
+//    py, pz, w, g_inv), index = particle number;
+//  * real-space fields: row-major (Nr, Nx), node (ir, ix) at ix + ir*Nx, row 0
+//    the ghost row at r = -dr/2; mode m=0 real, m>=1 complex interleaved;
+//  * spectral fields: row-major complex (Nr-1, Nx), row = radial mode index,
+//    column = longitudinal wavenumber index (numpy fftfreq order).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/chimeracl_gb300.h"
+
+namespace ccl {
+
+typedef uint32_t u32;
+
+// Number of SMs on the GB300 (2 dies x 76); grid-stride kernels size their
+// grids in multiples of it.
+constexpr int kNumSM = 152;
+constexpr int kMaxModes = 4;  // azimuthal modes m = 0..3 (M <= 3)
+
+void set_error(const char *fmt, ...);
+
+#define CCL_REQUIRE(cond, code, ...)                                           \
+  do {                                                                         \
+    if (!(cond)) {                                                             \
+      ::ccl::set_error(__VA_ARGS__);                                           \
+      return (code);                                                           \
+    }                                                                          \
+  } while (0)
+
+#define CCL_LAUNCH_CHECK(what)                                                 \
+  do {                                                                         \
+    cudaError_t e_ = cudaGetLastError();                                       \
+    if (e_ != cudaSuccess) {                                                   \
+      ::ccl::set_error("%s: %s", what, cudaGetErrorString(e_));                \
+      return CCL_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+static inline int grid_for(long n, int threads, int per_sm = 8) {
+  long b = (n + threads - 1) / threads;
+  long cap = (long)kNumSM * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+static inline cudaStream_t S(void *stream) { return (cudaStream_t)stream; }
+
+// Complex number of real type T, laid out as (re, im).
+template <typename T> struct cplx {
+  T re, im;
+};
+
+template <typename T> struct vec2;
+template <> struct vec2<double> { typedef double2 type; };
+template <> struct vec2<float> { typedef float2 type; };
+
+template <typename T> __device__ __forceinline__ cplx<T> ld_c(const T *p, long i) {
+  typename vec2<T>::type v = reinterpret_cast<const typename vec2<T>::type *>(p)[i];
+  cplx<T> r;
+  r.re = v.x;
+  r.im = v.y;
+  return r;
+}
+template <typename T> __device__ __forceinline__ void st_c(T *p, long i, cplx<T> c) {
+  typename vec2<T>::type v;
+  v.x = c.re;
+  v.y = c.im;
+  reinterpret_cast<typename vec2<T>::type *>(p)[i] = v;
+}
+
+// Pointer bundles passed by value to kernels (kernel parameter space).
+template <int N> struct ptrs {
+  void *p[N];
+};
+
+}  // namespace ccl

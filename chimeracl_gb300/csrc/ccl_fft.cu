@@ -1,0 +1,427 @@
+// Batched longitudinal FFT (along x, contiguous rows) for the spectral
+// transforms: mixed-radix Stockham autosort in shared memory, one CTA per
+// row, radices 8/4/2 for powers of two and a table-driven DFT for odd prime
+// factors (3, 5, 7, 11, 13).  The row's phase factor, smoothing filter,
+// real-part cast and absorbing-edge profile are applied on the way in/out
+// so that every transform stage of the step reads and writes HBM once.
+//
+// Forward: X_k = sum_n x_n e^{-2 pi i nk/N} (unnormalised); inverse with
+// e^{+2 pi i nk/N} and 1/N -- the conventions of the reference's Reikna FFT
+// (transformer_methods_cl.py:507-509).
+#include <math.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "ccl_common.cuh"
+#include "ccl_launch.h"
+
+namespace ccl {
+
+constexpr int FFT_THREADS = 256;
+constexpr int FFT_MAXST = 16;
+
+struct FftPlan {
+  int n, nst;
+  int rad[FFT_MAXST];
+};
+
+static bool make_plan(int n, FftPlan *p) {
+  p->n = n;
+  p->nst = 0;
+  int m = n;
+  while (m % 8 == 0) { p->rad[p->nst++] = 8; m /= 8; }
+  while (m % 4 == 0) { p->rad[p->nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { p->rad[p->nst++] = 2; m /= 2; }
+  const int odd[] = {3, 5, 7, 11, 13};
+  for (int q : odd)
+    while (m % q == 0) {
+      if (p->nst >= FFT_MAXST) return false;
+      p->rad[p->nst++] = q;
+      m /= q;
+    }
+  return m == 1 && p->nst <= FFT_MAXST;
+}
+
+template <typename T> __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  cplx<T> r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+  return r;
+}
+template <typename T> __device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) {
+  cplx<T> r = {a.re + b.re, a.im + b.im};
+  return r;
+}
+template <typename T> __device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) {
+  cplx<T> r = {a.re - b.re, a.im - b.im};
+  return r;
+}
+// multiply by -i (forward) or +i (inverse)
+template <typename T, bool INV> __device__ __forceinline__ cplx<T> mul_mi(cplx<T> a) {
+  cplx<T> r;
+  if (INV) { r.re = -a.im; r.im = a.re; }
+  else { r.re = a.im; r.im = -a.re; }
+  return r;
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft4(cplx<T> &a, cplx<T> &b, cplx<T> &c, cplx<T> &d) {
+  cplx<T> t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(b, d), t3 = mul_mi<T, INV>(csub(b, d));
+  a = cadd(t0, t2);
+  c = csub(t0, t2);
+  b = cadd(t1, t3);
+  d = csub(t1, t3);
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft8(cplx<T> *v) {
+  cplx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  cplx<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<T, INV>(e0, e1, e2, e3);
+  dft4<T, INV>(o0, o1, o2, o3);
+  const T h = (T)0.70710678118654752440084436210485;
+  // o_q *= W8^q, W8 = e^{-i pi/4} (forward) / e^{+i pi/4} (inverse)
+  cplx<T> w1 = {h, INV ? h : -h}, w3 = {-h, INV ? h : -h};
+  o1 = cmul(o1, w1);
+  o2 = mul_mi<T, INV>(o2);
+  o3 = cmul(o3, w3);
+  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+
+template <typename T> __device__ __forceinline__ cplx<T> twid(const cplx<T> *tw, long t, bool inv) {
+  cplx<T> w = tw[t];
+  if (inv) w.im = -w.im;
+  return w;
+}
+
+// One Stockham stage of a power-of-two radix R (unrolled, in registers).
+template <typename T, bool INV, int R>
+__device__ __forceinline__ void stage_pow2(const cplx<T> *__restrict__ src,
+                                           cplx<T> *__restrict__ dst, int N,
+                                           int Ns,
+                                           const cplx<T> *__restrict__ tw) {
+  const int NR = N / R, tstride = N / (Ns * R);
+  for (int j = threadIdx.x; j < NR; j += blockDim.x) {
+    const int k = j % Ns;
+    cplx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = src[j + r * NR];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++)
+        v[r] = cmul(v[r], twid(tw, (long)(r * k) * tstride, INV));
+    }
+    if (R == 8) {
+      dft8<T, INV>(v);
+    } else if (R == 4) {
+      dft4<T, INV>(v[0], v[1], v[2], v[3]);
+    } else {
+      cplx<T> a = cadd(v[0], v[1]), b = csub(v[0], v[1]);
+      v[0] = a;
+      v[1] = b;
+    }
+    const int ob = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) dst[ob + r * Ns] = v[r];
+  }
+}
+
+// One Stockham stage of an odd prime radix R <= 13 (table-driven DFT).
+template <typename T, bool INV>
+__device__ void stage_odd(const cplx<T> *__restrict__ src,
+                          cplx<T> *__restrict__ dst, int N, int Ns, int R,
+                          const cplx<T> *__restrict__ tw) {
+  const int NR = N / R, tstride = N / (Ns * R);
+  for (int j = threadIdx.x; j < NR; j += blockDim.x) {
+    const int k = j % Ns;
+    cplx<T> v[13], y[13];
+    for (int r = 0; r < R; r++) v[r] = src[j + r * NR];
+    if (Ns > 1)
+      for (int r = 1; r < R; r++)
+        v[r] = cmul(v[r], twid(tw, (long)(r * k) * tstride, INV));
+    // y_q = sum_r v_r W_R^{rq}, with W_R^t = W_N^{t N/R}
+    for (int q = 0; q < R; q++) {
+      cplx<T> acc = v[0];
+      for (int r = 1; r < R; r++)
+        acc = cadd(acc, cmul(v[r], twid(tw, (long)((r * q) % R) * NR, INV)));
+      y[q] = acc;
+    }
+    const int ob = (j / Ns) * Ns * R + k;
+    for (int r = 0; r < R; r++) dst[ob + r * Ns] = y[r];
+  }
+}
+
+// One full transform of the row held in sA (result returned: sA or sB).
+template <typename T, bool INV>
+__device__ cplx<T> *fft_row(cplx<T> *sA, cplx<T> *sB, const FftPlan &pl,
+                            const cplx<T> *__restrict__ tw) {
+  const int N = pl.n;
+  int Ns = 1;
+  cplx<T> *src = sA, *dst = sB;
+  for (int st = 0; st < pl.nst; st++) {
+    const int R = pl.rad[st];
+    if (R == 8) stage_pow2<T, INV, 8>(src, dst, N, Ns, tw);
+    else if (R == 4) stage_pow2<T, INV, 4>(src, dst, N, Ns, tw);
+    else if (R == 2) stage_pow2<T, INV, 2>(src, dst, N, Ns, tw);
+    else stage_odd<T, INV>(src, dst, N, Ns, R, tw);
+    __syncthreads();
+    cplx<T> *t = src;
+    src = dst;
+    dst = t;
+    Ns *= R;
+  }
+  return src;
+}
+
+// Forward stage: in -> FFT -> * phs (* filter) -> out
+template <typename T, bool IN_REAL, bool FILT>
+__global__ void __launch_bounds__(FFT_THREADS)
+    k_fft_fwd(FftPlan pl, const T *__restrict__ in, long in_ld,
+              T *__restrict__ out, const T *__restrict__ phs,
+              const T *__restrict__ filt, const cplx<T> *__restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
+  const int N = pl.n;
+  const long row = blockIdx.x;
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> v;
+    if (IN_REAL) {
+      v.re = in[row * in_ld + ix];
+      v.im = T(0);
+    } else {
+      v = ld_c(in, row * in_ld + ix);
+    }
+    sA[ix] = v;
+  }
+  __syncthreads();
+  cplx<T> *res = fft_row<T, false>(sA, sB, pl, tw);
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> v = res[ix], p = ld_c(phs, ix);
+    cplx<T> r = {(v.re * p.re - v.im * p.im), (v.re * p.im + v.im * p.re)};
+    if (FILT) {
+      T f = filt[row * N + ix];
+      r.re = f * r.re;
+      r.im = f * r.im;
+    }
+    st_c(out, row * N + ix, r);
+  }
+}
+
+// Backward stage: in * phs -> inverse FFT / N -> out (complex or real part)
+template <typename T, bool OUT_REAL>
+__global__ void __launch_bounds__(FFT_THREADS)
+    k_fft_bwd(FftPlan pl, const T *__restrict__ in, T *__restrict__ out,
+              long out_ld, const T *__restrict__ phs,
+              const cplx<T> *__restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
+  const int N = pl.n;
+  const long row = blockIdx.x;
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> a = ld_c(in, row * N + ix), p = ld_c(phs, ix);
+    cplx<T> v = {(a.re * p.re - a.im * p.im), (a.re * p.im + a.im * p.re)};
+    sA[ix] = v;
+  }
+  __syncthreads();
+  cplx<T> *res = fft_row<T, true>(sA, sB, pl, tw);
+  const T inv_n = (T)(1.0 / (double)N);
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> v = res[ix];
+    if (OUT_REAL) {
+      out[row * out_ld + ix] = v.re * inv_n;
+    } else {
+      cplx<T> r = {v.re * inv_n, v.im * inv_n};
+      st_c(out, row * out_ld + ix, r);
+    }
+  }
+}
+
+// Absorbing-edge round trip of one spectral component, in place.
+template <typename T, bool RS_REAL>
+__global__ void __launch_bounds__(FFT_THREADS)
+    k_damp(FftPlan pl, T *__restrict__ spec, T *__restrict__ rs,
+           const T *__restrict__ phs_p, const T *__restrict__ phs_m,
+           const T *__restrict__ prof, u32 nf, const cplx<T> *__restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
+  const int N = pl.n;
+  const u32 un = (u32)N;
+  const long row = blockIdx.x;
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> a = ld_c(spec, row * N + ix), p = ld_c(phs_p, ix);
+    cplx<T> v = {(a.re * p.re - a.im * p.im), (a.re * p.im + a.im * p.re)};
+    sA[ix] = v;
+  }
+  __syncthreads();
+  cplx<T> *res = fft_row<T, true>(sA, sB, pl, tw);
+  cplx<T> *other = (res == sA) ? sB : sA;
+  const T inv_n = (T)(1.0 / (double)N);
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> v = res[ix];
+    v.re = v.re * inv_n;
+    v.im = RS_REAL ? T(0) : v.im * inv_n;
+    const u32 ux = (u32)ix;
+    if (ux < nf) { v.re *= prof[ux]; v.im *= prof[ux]; }
+    if (ux > un - nf) { v.re *= prof[un - ux]; v.im *= prof[un - ux]; }
+    if (RS_REAL) rs[(row + 1) * N + ix] = v.re;
+    else st_c(rs, (row + 1) * N + ix, v);
+    other[ix] = v;
+    if (row == 0) {  // the ghost row is damped in place as well
+      if (RS_REAL) {
+        T g = rs[ix];
+        if (ux < nf) g *= prof[ux];
+        if (ux > un - nf) g *= prof[un - ux];
+        rs[ix] = g;
+      } else {
+        cplx<T> g = ld_c(rs, ix);
+        if (ux < nf) { g.re *= prof[ux]; g.im *= prof[ux]; }
+        if (ux > un - nf) { g.re *= prof[un - ux]; g.im *= prof[un - ux]; }
+        st_c(rs, ix, g);
+      }
+    }
+  }
+  __syncthreads();
+  cplx<T> *in2 = other, *tmp2 = (other == sA) ? sB : sA;
+  cplx<T> *res2 = fft_row<T, false>(in2, tmp2, pl, tw);
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+    cplx<T> v = res2[ix], p = ld_c(phs_m, ix);
+    cplx<T> r = {(v.re * p.re - v.im * p.im), (v.re * p.im + v.im * p.re)};
+    st_c(spec, row * N + ix, r);
+  }
+}
+
+// ---------------------------------------------------------------------
+// Twiddle tables W_N^t = e^{-2 pi i t/N}, built once per (device, N, type)
+// by a device kernel (sincospi) and kept for the life of the process.
+template <typename T> __global__ void k_twiddles(int n, cplx<T> *tw) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)t / (double)n, &s, &c);
+    cplx<T> w = {(T)c, (T)(-s)};
+    tw[t] = w;
+  }
+}
+
+template <typename T> static const cplx<T> *twiddles(int n, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, void *> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(dev, n);
+  auto it = cache.find(key);
+  if (it != cache.end()) return (const cplx<T> *)it->second;
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(cplx<T>) * (size_t)n) != cudaSuccess) return nullptr;
+  k_twiddles<T><<<(n + 255) / 256, 256, 0, s>>>(n, (cplx<T> *)p);
+  cache[key] = p;
+  return (const cplx<T> *)p;
+}
+
+template <typename T> static int fft_check(int nx, FftPlan *pl, size_t *smem) {
+  const int nmax = sizeof(T) == 8 ? 4096 : 8192;
+  CCL_REQUIRE(nx >= 2 && nx <= nmax, CCL_ERR_UNSUPPORTED,
+              "fft: nx=%d outside [2, %d]", nx, nmax);
+  CCL_REQUIRE(make_plan(nx, pl), CCL_ERR_UNSUPPORTED,
+              "fft: nx=%d has prime factors above 13", nx);
+  *smem = 2 * sizeof(cplx<T>) * (size_t)nx;
+  return CCL_OK;
+}
+
+template <typename K> static void allow_smem(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+}
+
+template <typename T>
+int fft_forward_rows(int nrows, int nx, const T *in, long in_ld, int in_real,
+                     T *out, const T *phs, const T *filt, cudaStream_t s) {
+  FftPlan pl;
+  size_t smem;
+  int rc = fft_check<T>(nx, &pl, &smem);
+  if (rc) return rc;
+  if (nrows == 0) return CCL_OK;
+  const cplx<T> *tw = twiddles<T>(nx, s);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+#define CCL_FWD(R, F)                                                          \
+  {                                                                            \
+    auto kern = k_fft_fwd<T, R, F>;                                            \
+    allow_smem(kern, smem);                                                    \
+    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, in_ld, out, phs, filt, tw);  \
+  }
+  if (in_real) {
+    if (filt) CCL_FWD(true, true) else CCL_FWD(true, false)
+  } else {
+    if (filt) CCL_FWD(false, true) else CCL_FWD(false, false)
+  }
+#undef CCL_FWD
+  CCL_LAUNCH_CHECK("fft_forward_rows");
+  return CCL_OK;
+}
+
+template <typename T>
+int fft_backward_rows(int nrows, int nx, const T *in, T *out, long out_ld,
+                      int out_real, const T *phs, cudaStream_t s) {
+  FftPlan pl;
+  size_t smem;
+  int rc = fft_check<T>(nx, &pl, &smem);
+  if (rc) return rc;
+  if (nrows == 0) return CCL_OK;
+  const cplx<T> *tw = twiddles<T>(nx, s);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  if (out_real) {
+    auto kern = k_fft_bwd<T, true>;
+    allow_smem(kern, smem);
+    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, out, out_ld, phs, tw);
+  } else {
+    auto kern = k_fft_bwd<T, false>;
+    allow_smem(kern, smem);
+    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, out, out_ld, phs, tw);
+  }
+  CCL_LAUNCH_CHECK("fft_backward_rows");
+  return CCL_OK;
+}
+
+template <typename T>
+int damp_rows(int nrows, int nx, T *spec, T *rs, int rs_real,
+              const T *phs_p, const T *phs_m, const T *prof, int nf,
+              cudaStream_t s) {
+  FftPlan pl;
+  size_t smem;
+  int rc = fft_check<T>(nx, &pl, &smem);
+  if (rc) return rc;
+  CCL_REQUIRE(nf >= 0, CCL_ERR_ARG, "damp: nf=%d", nf);
+  if (nrows == 0) return CCL_OK;
+  const cplx<T> *tw = twiddles<T>(nx, s);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  if (rs_real) {
+    auto kern = k_damp<T, true>;
+    allow_smem(kern, smem);
+    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, spec, rs, phs_p, phs_m, prof,
+                                          (u32)nf, tw);
+  } else {
+    auto kern = k_damp<T, false>;
+    allow_smem(kern, smem);
+    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, spec, rs, phs_p, phs_m, prof,
+                                          (u32)nf, tw);
+  }
+  CCL_LAUNCH_CHECK("damp_rows");
+  return CCL_OK;
+}
+
+#define CCL_INST_FFT(T)                                                        \
+  template int fft_forward_rows<T>(int, int, const T *, long, int, T *,       \
+                                   const T *, const T *, cudaStream_t);        \
+  template int fft_backward_rows<T>(int, int, const T *, T *, long, int,      \
+                                    const T *, cudaStream_t);                  \
+  template int damp_rows<T>(int, int, T *, T *, int, const T *, const T *,    \
+                            const T *, int, cudaStream_t);
+CCL_INST_FFT(double)
+CCL_INST_FFT(float)
+
+}  // namespace ccl

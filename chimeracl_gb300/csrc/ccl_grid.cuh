@@ -1,0 +1,391 @@
+// Grid kernels: charge/current deposit, deposit post-processing, ghost-row
+// fill, field gather + Boris push.  Templated on the real type T and the
+// highest azimuthal mode M.
+//
+// Deposit design.  One CTA owns a tile of (DEP_TR-1) x (DEP_TX-1) grid nodes
+// and runs one thread per cell of the DEP_TR x DEP_TX cells that touch them
+// (cells on the tile border are also computed by the neighbouring CTA, so no
+// node is written by two CTAs and no atomics are needed).  Each thread sums
+// its cell's cell-sorted particles into 2x2 corner accumulators in registers,
+// in the order of sort_indx, exactly as the reference's per-cell loop does
+// (grid_deposit_m1.cl:105-138).  The corner sums are then added to the node
+// tile in shared memory in four phases, one per cell colour
+// (ix&1) + 2(ir&1): the order in which the reference's four colour launches
+// add them (grid_methods_cl.py:261-264).  The result is the reference's sum,
+// term by term and in the same order, without its four launches.
+#pragma once
+#include "ccl_common.cuh"
+#include "ccl_particles.cuh"
+
+namespace ccl {
+
+constexpr int DEP_TX = 32, DEP_TR = 8, DEP_THREADS = DEP_TX * DEP_TR;
+constexpr int DEP_NTX = DEP_TX - 1, DEP_NTR = DEP_TR - 1;
+
+struct DepGrid {
+  int Nx, Nr;
+  double xmin, dx_inv, rmin, dr_inv;
+};
+
+// Field pointer bundle: for a scalar deposit f[m] (m = 0..M); for a vector
+// deposit f[3m + k].  Mode 0 is real, modes >= 1 complex.
+template <typename T, int M, bool VEC>
+__global__ void __launch_bounds__(DEP_THREADS)
+    k_deposit(const u32 *__restrict__ sort_indx,
+              const u32 *__restrict__ cell_off, const T *__restrict__ x,
+              const T *__restrict__ y, const T *__restrict__ z,
+              const T *__restrict__ ux, const T *__restrict__ uy,
+              const T *__restrict__ uz, const T *__restrict__ g_inv,
+              const T *__restrict__ w, T q, DepGrid g, ptrs<12> f) {
+  constexpr int NK = VEC ? 3 : 1;       // vector components
+  constexpr int NQ = NK * (1 + 2 * M);  // reals per node
+  __shared__ T acc[NQ][DEP_NTR][DEP_NTX];
+  const int Nx = g.Nx, Nr = g.Nr;
+  const int nx0 = blockIdx.x * DEP_NTX, nr0 = blockIdx.y * DEP_NTR;
+  const int tx = threadIdx.x % DEP_TX, tr = threadIdx.x / DEP_TX;
+
+  // 1. node tile <- current field values
+  for (int t = threadIdx.x; t < DEP_NTR * DEP_NTX; t += DEP_THREADS) {
+    int r = t / DEP_NTX, c = t - r * DEP_NTX;
+    int nr = nr0 + r, nx = nx0 + c;
+    bool in = nr < Nr && nx < Nx;
+    long node = (long)nr * Nx + nx;
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+      acc[k * (1 + 2 * M)][r][c] = in ? ((const T *)f.p[k])[node] : T(0);
+#pragma unroll
+      for (int m = 1; m <= M; m++) {
+        const T *fm = (const T *)f.p[m * NK + k];
+        acc[k * (1 + 2 * M) + 2 * m - 1][r][c] = in ? fm[2 * node] : T(0);
+        acc[k * (1 + 2 * M) + 2 * m][r][c] = in ? fm[2 * node + 1] : T(0);
+      }
+    }
+  }
+
+  // 2. this thread's cell: per-corner sums over its particles
+  const int ix = nx0 - 1 + tx, ir = nr0 - 1 + tr;
+  const bool valid = ix > 0 && ix < Nx - 2 && ir >= 0 && ir < Nr - 2;
+  T s[4][NQ];
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+#pragma unroll
+    for (int qq = 0; qq < NQ; qq++) s[c][qq] = T(0);
+  if (valid) {
+    const long cg = (long)ix + (long)ir * (Nx - 1);
+    const u32 p0 = cell_off[cg], p1 = cell_off[cg + 1];
+    const T xmin = (T)g.xmin, dx_inv = (T)g.dx_inv, rmin = (T)g.rmin,
+            dr_inv = (T)g.dr_inv;
+    const T fix = (T)ix, fir = (T)ir;
+    for (u32 ip = p0; ip < p1; ip++) {
+      const u32 p = sort_indx[ip];
+      const T xp = x[p], yp = y[p], zp = z[p];
+      T wp;
+      if (VEC)
+        wp = w[p] * g_inv[p] * q;
+      else
+        wp = w[p] * q;
+      const T rp = sqrt(yp * yp + zp * zp);
+      T rinv;
+      if (VEC)
+        rinv = rp > T(0) ? T(1) / rp : T(0);  // grid_deposit_m1.cl:280-281
+      else
+        rinv = T(1) / rp;                     // grid_deposit_m1.cl:115
+      T e[M + 1][2];
+      if (M >= 1) {
+        e[1][0] = yp * rinv;
+        e[1][1] = zp * rinv;
+      }
+#pragma unroll
+      for (int m = 2; m <= M; m++) {  // e^{i m phi} by recurrence (m >= 2)
+        e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+        e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+      }
+      T sX1 = (xp - xmin) * dx_inv - fix;
+      T sX0 = T(1) - sX1;
+      T sR1 = (rp - rmin) * dr_inv - fir;
+      T sR0 = T(1) - sR1;
+      sX0 *= wp;
+      sX1 *= wp;
+      const T C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+      T jp[3] = {T(0), T(0), T(0)};
+      if (VEC) {
+        jp[0] = ux[p];
+        jp[1] = uy[p];
+        jp[2] = uz[p];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+#pragma unroll
+        for (int k = 0; k < NK; k++) {
+          constexpr int B = 1 + 2 * M;
+          if (VEC) {
+            T jproj = C[c] * jp[k];
+            s[c][k * B] += C[c] * jp[k];
+#pragma unroll
+            for (int m = 1; m <= M; m++) {
+              s[c][k * B + 2 * m - 1] += jproj * e[m][0];
+              s[c][k * B + 2 * m] += jproj * e[m][1];
+            }
+          } else {
+            s[c][0] += C[c];
+#pragma unroll
+            for (int m = 1; m <= M; m++) {
+              s[c][2 * m - 1] += C[c] * e[m][0];
+              s[c][2 * m] += C[c] * e[m][1];
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // 3. add to the node tile colour by colour (the reference's launch order)
+  const int colour = (ix & 1) + 2 * (ir & 1);
+#pragma unroll
+  for (int col = 0; col < 4; col++) {
+    __syncthreads();
+    if (valid && colour == col) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        int lr = ir + (c >> 1) - nr0, lc = ix + (c & 1) - nx0;
+        if (lr >= 0 && lr < DEP_NTR && lc >= 0 && lc < DEP_NTX) {
+#pragma unroll
+          for (int qq = 0; qq < NQ; qq++) acc[qq][lr][lc] += s[c][qq];
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // 4. node tile -> global
+  for (int t = threadIdx.x; t < DEP_NTR * DEP_NTX; t += DEP_THREADS) {
+    int r = t / DEP_NTX, c = t - r * DEP_NTX;
+    int nr = nr0 + r, nx = nx0 + c;
+    if (nr >= Nr || nx >= Nx) continue;
+    long node = (long)nr * Nx + nx;
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+      ((T *)f.p[k])[node] = acc[k * (1 + 2 * M)][r][c];
+#pragma unroll
+      for (int m = 1; m <= M; m++) {
+        T *fm = (T *)f.p[m * NK + k];
+        fm[2 * node] = acc[k * (1 + 2 * M) + 2 * m - 1][r][c];
+        fm[2 * node + 1] = acc[k * (1 + 2 * M) + 2 * m][r][c];
+      }
+    }
+  }
+}
+
+template <typename T, int M, bool VEC>
+int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
+              const T *y, const T *z, const T *ux, const T *uy, const T *uz,
+              const T *g_inv, const T *w, int charge, DepGrid g,
+              void *const *flds, cudaStream_t s) {
+  ptrs<12> f;
+  const int nptr = (VEC ? 3 : 1) * (M + 1);
+  for (int i = 0; i < nptr; i++) {
+    CCL_REQUIRE(flds[i], CCL_ERR_ARG, "deposit: null field pointer %d", i);
+    f.p[i] = flds[i];
+  }
+  dim3 grid((g.Nx + DEP_NTX - 1) / DEP_NTX, (g.Nr + DEP_NTR - 1) / DEP_NTR);
+  // the reference passes the charge as a signed char (grid_methods_cl.py:259)
+  T q = (T)(signed char)charge;
+  k_deposit<T, M, VEC><<<grid, DEP_THREADS, 0, s>>>(
+      sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w, q, g, f);
+  CCL_LAUNCH_CHECK("deposit");
+  return CCL_OK;
+}
+
+template <typename T, bool VEC>
+int deposit(int M, const u32 *sort_indx, const u32 *cell_off, const T *x,
+            const T *y, const T *z, const T *ux, const T *uy, const T *uz,
+            const T *g_inv, const T *w, int charge, DepGrid g,
+            void *const *flds, cudaStream_t s) {
+  switch (M) {
+    case 0:
+      return deposit_m<T, 0, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
+                                  g_inv, w, charge, g, flds, s);
+    case 1:
+      return deposit_m<T, 1, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
+                                  g_inv, w, charge, g, flds, s);
+    case 2:
+      return deposit_m<T, 2, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
+                                  g_inv, w, charge, g, flds, s);
+    case 3:
+      return deposit_m<T, 3, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
+                                  g_inv, w, charge, g, flds, s);
+  }
+  set_error("deposit: M=%d not supported (0..3)", M);
+  return CCL_ERR_UNSUPPORTED;
+}
+
+// ---------------------------------------------------------------------
+// treat_axis + divide_by_dv (grid_generic.cl:4-59) fused: the thread of row 1
+// also writes row 0 so that row 0 is read before it is scaled.
+template <typename T>
+__global__ void k_postproc(ptrs<32> f, int Mp1, int Nx, int Nr,
+                           const T *__restrict__ dv) {
+  const int pidx = blockIdx.z, m = pidx % Mp1;
+  const int ir = blockIdx.y + 1;
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix >= Nx) return;
+  T *a = (T *)f.p[pidx];
+  if (m == 0) {
+    long i = (long)ir * Nx + ix;
+    if (ir == 1) {
+      T r0 = a[ix];
+      a[i] = (a[i] - r0) * dv[1];
+      a[ix] = r0 * dv[0];
+    } else {
+      a[i] = a[i] * dv[ir];
+    }
+  } else {
+    long i = (long)ir * Nx + ix;
+    if (ir == 1) {
+      T r0 = a[2 * ix], i0 = a[2 * ix + 1];
+      a[2 * i] = (a[2 * i] - r0) * dv[1];
+      a[2 * i + 1] = (a[2 * i + 1] - i0) * dv[1];
+      a[2 * ix] = r0 * dv[0];
+      a[2 * ix + 1] = i0 * dv[0];
+    } else {
+      a[2 * i] = a[2 * i] * dv[ir];
+      a[2 * i + 1] = a[2 * i + 1] * dv[ir];
+    }
+  }
+}
+
+// warp_axis_m0_d / warp_axis_m1plus_c (grid_generic.cl:63-86)
+template <typename T>
+__global__ void k_warp_axis(ptrs<32> f, int Mp1, int Nx) {
+  const int pidx = blockIdx.y, m = pidx % Mp1;
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix >= Nx) return;
+  T *a = (T *)f.p[pidx];
+  if (m == 0) {
+    a[ix] = a[ix + Nx];
+  } else {
+    a[2 * ix] = -a[2 * (ix + Nx)];
+    a[2 * ix + 1] = -a[2 * (ix + Nx) + 1];
+  }
+}
+
+// ---------------------------------------------------------------------
+// gather_and_push (grid_deposit_m1.cl:330-511): bilinear gather of E, B over
+// modes 0..M (factor 2 for m >= 1, Hermitian symmetry) and Boris push.
+// f.p[6m + c], c = ex, ey, ez, bx, by, bz.
+template <typename T, int M>
+__global__ void __launch_bounds__(256)
+    k_gather_push(long np, const T *__restrict__ x, const T *__restrict__ y,
+                  const T *__restrict__ z, T *__restrict__ px,
+                  T *__restrict__ py, T *__restrict__ pz,
+                  T *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
+                  const u32 *__restrict__ np_stay_p, T dt, DepGrid g,
+                  ptrs<24> f) {
+  const u32 np_stay = *np_stay_p;
+  const int Nx = g.Nx, nxc = Nx - 1, nrc = g.Nr - 1;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x) {
+    const u32 p = sort_indx[i];
+    if (p >= np_stay) continue;  // grid_deposit_m1.cl:367-368
+    const T xp = x[p], yp = y[p], zp = z[p];
+    const T rp = sqrt(yp * yp + zp * zp);
+    const T xmin = (T)g.xmin, dx_inv = (T)g.dx_inv, rmin = (T)g.rmin,
+            dr_inv = (T)g.dr_inv;
+    const int ix = floor_to_int((double)floor((xp - xmin) * dx_inv), -1);
+    const int ir = floor_to_int((double)floor((rp - rmin) * dr_inv), 1 << 30);
+    if (!(ix > 0 && ix < nxc - 1 && ir < nrc - 1)) continue;
+    const long ig = (long)ix + (long)ir * Nx;
+    T u[3] = {px[p], py[p], pz[p]};
+    const T dt_2 = T(0.5) * dt;
+    const T rinv = T(1) / rp;
+    const T sX1 = (xp - xmin) * dx_inv - (T)ix, sX0 = T(1) - sX1;
+    const T sR1 = (rp - rmin) * dr_inv - (T)ir, sR0 = T(1) - sR1;
+    T e[M + 1][2];
+    if (M >= 1) {
+      e[1][0] = yp * rinv;
+      e[1][1] = -zp * rinv;
+    }
+#pragma unroll
+    for (int m = 2; m <= M; m++) {  // e^{-i m phi} by recurrence (m >= 2)
+      e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+      e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+    }
+    const T C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+    T ep[3] = {T(0), T(0), T(0)}, bp[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const long l = ig + (c & 1) + (long)Nx * (c >> 1);
+        const T cc = C[c];
+        ep[k] += cc * ((const T *)f.p[k])[l];
+        bp[k] += cc * ((const T *)f.p[3 + k])[l];
+#pragma unroll
+        for (int m = 1; m <= M; m++) {
+          cplx<T> fe = ld_c((const T *)f.p[6 * m + k], l);
+          cplx<T> fb = ld_c((const T *)f.p[6 * m + 3 + k], l);
+          T er = T(2) * fe.re, ei = T(2) * fe.im;
+          T br = T(2) * fb.re, bi = T(2) * fb.im;
+          ep[k] += cc * er * e[m][0];
+          ep[k] -= cc * ei * e[m][1];
+          bp[k] += cc * br * e[m][0];
+          bp[k] -= cc * bi * e[m][1];
+        }
+      }
+    }
+    T um[3], up[3], u0[3], t[3], sv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) um[k] = u[k] + dt_2 * ep[k];
+    T gi = T(1) / sqrt(T(1) + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) t[k] = dt_2 * bp[k] * gi;
+    const T f2 = T(2) / (T(1) + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
+    u0[0] = um[0] + um[1] * t[2] - um[2] * t[1];
+    u0[1] = um[1] - um[0] * t[2] + um[2] * t[0];
+    u0[2] = um[2] + um[0] * t[1] - um[1] * t[0];
+    up[0] = um[0] + u0[1] * sv[2] - u0[2] * sv[1];
+    up[1] = um[1] - u0[0] * sv[2] + u0[2] * sv[0];
+    up[2] = um[2] + u0[0] * sv[1] - u0[1] * sv[0];
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = up[k] + dt_2 * ep[k];
+    gi = T(1) / sqrt(T(1) + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    px[p] = u[0];
+    py[p] = u[1];
+    pz[p] = u[2];
+    g_inv[p] = gi;
+  }
+}
+
+template <typename T>
+int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
+                T *py, T *pz, T *g_inv, const u32 *sort_indx,
+                const u32 *np_stay, double factor_push, DepGrid g,
+                const void *const *flds, cudaStream_t s) {
+  if (np == 0) return CCL_OK;
+  ptrs<24> f;
+  for (int i = 0; i < 6 * (M + 1); i++) {
+    CCL_REQUIRE(flds[i], CCL_ERR_ARG, "gather: null field pointer %d", i);
+    f.p[i] = (void *)flds[i];
+  }
+  int nb = grid_for(np, 256, 16);
+  T dt = (T)factor_push;
+#define CCL_GP(MM)                                                             \
+  k_gather_push<T, MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv,     \
+                                          sort_indx, np_stay, dt, g, f)
+  switch (M) {
+    case 0: CCL_GP(0); break;
+    case 1: CCL_GP(1); break;
+    case 2: CCL_GP(2); break;
+    case 3: CCL_GP(3); break;
+    default:
+      set_error("gather: M=%d not supported (0..3)", M);
+      return CCL_ERR_UNSUPPORTED;
+  }
+#undef CCL_GP
+  CCL_LAUNCH_CHECK("gather_push");
+  return CCL_OK;
+}
+
+}  // namespace ccl

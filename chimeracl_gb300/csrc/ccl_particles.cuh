@@ -1,0 +1,453 @@
+// Particle kernels: coordinate push, cell index + stable cell sort, align,
+// plasma injector.  Templated on the real type T; the FP64 instantiation is
+// compiled with -fmad=false so that every expression rounds exactly as the
+// reference kernels written in strict IEEE arithmetic do.
+#pragma once
+#include "ccl_common.cuh"
+
+namespace ccl {
+
+// ---------------------------------------------------------------------
+// push_xyz (particles_generic.cl:129-153)
+template <typename T>
+__global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
+                         T *__restrict__ z, const T *__restrict__ px,
+                         const T *__restrict__ py, const T *__restrict__ pz,
+                         const T *__restrict__ g_inv, T dt) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x) {
+    T dt_g = dt * g_inv[i];
+    T ddx = px[i] * dt_g, ddy = py[i] * dt_g, ddz = pz[i] * dt_g;
+    x[i] = x[i] + ddx;
+    y[i] = y[i] + ddy;
+    z[i] = z[i] + ddz;
+  }
+}
+
+template <typename T>
+int push_x(long np, T *x, T *y, T *z, const T *px, const T *py, const T *pz,
+           const T *g_inv, double dt, cudaStream_t s) {
+  if (np == 0) return CCL_OK;
+  k_push_x<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv,
+                                                 (T)dt);
+  CCL_LAUNCH_CHECK("push_x");
+  return CCL_OK;
+}
+
+// ---------------------------------------------------------------------
+// Cell key of a particle (particles_generic.cl:106-125).  Coordinates are
+// converted to double so that the FP32 form sorts with the same key rule.
+struct KeyGrid {
+  int Nx, Nr;
+  double xmin, dx_inv, rmin, dr_inv;
+};
+
+__device__ __forceinline__ int floor_to_int(double f, int bad) {
+  // (int) of an out-of-range or NaN double: such particles are outside the
+  // window; give them an index that fails the window test.
+  return (f > -2147483648.0 && f < 2147483647.0) ? (int)f : bad;
+}
+
+__device__ __forceinline__ u32 cell_key(double xp, double yp, double zp,
+                                        const KeyGrid &g) {
+  int nxc = g.Nx - 1, nrc = g.Nr - 1;
+  double r = sqrt(yp * yp + zp * zp);
+  int ix = floor_to_int(floor((xp - g.xmin) * g.dx_inv), -1);
+  int ir = floor_to_int(floor((r - g.rmin) * g.dr_inv), -1);
+  if (ix > 0 && ix < nxc - 1 && ir < nrc - 1 && ir >= 0)
+    return (u32)(ix + ir * nxc);
+  return (u32)(nrc * nxc);
+}
+
+// keys + per-cell counts; counts aggregated per warp with match_any so that
+// a warp of cell-sorted particles issues one atomic per distinct cell.
+template <typename T>
+__global__ void k_keys(long np, const T *__restrict__ x,
+                       const T *__restrict__ y, const T *__restrict__ z,
+                       KeyGrid g, u32 *__restrict__ keys,
+                       u32 *__restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long base = (blockIdx.x * (long)blockDim.x + threadIdx.x) & ~31L; base < np;
+       base += stride) {
+    long i = base + lane;
+    bool valid = i < np;
+    u32 k = 0xffffffffu;
+    if (valid) {
+      k = cell_key((double)x[i], (double)y[i], (double)z[i], g);
+      keys[i] = k;
+    }
+    unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&counts[k], __popc(peers));
+  }
+}
+
+// ---------------------------------------------------------------------
+// Exclusive scan of u32 (device-wide, reduce-then-scan).
+constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8,
+              SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32 *sh,
+                                                    u32 *total) {
+  // sh: SCAN_THREADS/32 words
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    u32 t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) sh[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    u32 s = lane < nw ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      u32 t = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += t;
+    }
+    if (lane < nw) sh[lane] = s;
+  }
+  __syncthreads();
+  u32 wpre = warp ? sh[warp - 1] : 0;
+  if (total) *total = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return wpre + inc - v;
+}
+
+static __global__ void k_scan_reduce(const u32 *__restrict__ in, long L,
+                              u32 *__restrict__ part) {
+  __shared__ u32 sh[32];
+  long base = (long)blockIdx.x * SCAN_TILE;
+  u32 s = 0;
+#pragma unroll
+  for (int it = 0; it < SCAN_ITEMS; it++) {
+    long i = base + it * SCAN_THREADS + threadIdx.x;
+    if (i < L) s += in[i];
+  }
+  u32 tot;
+  block_exclusive_scan(s, sh, &tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// exclusive scan of one tile per block, plus part[blockIdx] (scanned)
+static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
+                            const u32 *__restrict__ part, u32 *__restrict__ out,
+                            u32 *__restrict__ total_out) {
+  __shared__ u32 sh[32];
+  long base = (long)blockIdx.x * SCAN_TILE + (long)threadIdx.x * SCAN_ITEMS;
+  u32 v[SCAN_ITEMS];
+  u32 s = 0;
+#pragma unroll
+  for (int it = 0; it < SCAN_ITEMS; it++) {
+    long i = base + it;
+    v[it] = i < L ? in[i] : 0;
+    s += v[it];
+  }
+  u32 tot;
+  u32 pre = block_exclusive_scan(s, sh, &tot) + (part ? part[blockIdx.x] : 0);
+#pragma unroll
+  for (int it = 0; it < SCAN_ITEMS; it++) {
+    long i = base + it;
+    if (i < L) out[i] = pre;
+    pre += v[it];
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+    *total_out = (part ? part[blockIdx.x] : 0) + tot;
+}
+
+static inline long scan_ws_words(long L) {
+  long w = 0;
+  while (L > SCAN_TILE) {
+    L = (L + SCAN_TILE - 1) / SCAN_TILE;
+    w += L;
+  }
+  return w + 1;
+}
+
+// out[0..L-1] = exclusive scan of in; *total_out = sum (if non-null).
+// Works in place (out == in).  ws: scan_ws_words(L) words.
+static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
+                          u32 *ws, cudaStream_t s) {
+  if (L <= 0) return CCL_OK;
+  long nb = (L + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb == 1) {
+    k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, L, nullptr, out, total_out);
+    CCL_LAUNCH_CHECK("scan_tile");
+    return CCL_OK;
+  }
+  u32 *part = ws;
+  k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part);
+  CCL_LAUNCH_CHECK("scan_reduce");
+  int rc = scan_exclusive(part, nb, part, nullptr, ws + nb, s);
+  if (rc) return rc;
+  k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part, out,
+                                                     total_out);
+  CCL_LAUNCH_CHECK("scan_tile");
+  return CCL_OK;
+}
+
+// ---------------------------------------------------------------------
+// Stable LSD radix sort of (key, particle number): per pass a tile
+// histogram, a device-wide scan of the (digit, tile) table, and a scatter
+// in which each warp ranks its 256 keys in order (match_any per round of 32)
+// so that the order of equal keys is the input order.
+constexpr int RS_THREADS = 256, RS_WARPS = RS_THREADS / 32, RS_ITEMS = 8,
+              RS_TILE = RS_THREADS * RS_ITEMS, RS_MAXBITS = 10;
+
+static __global__ void k_radix_hist(const u32 *__restrict__ keys, long n, int shift,
+                             int nbits, u32 *__restrict__ hist, int ntiles) {
+  extern __shared__ u32 shh[];
+  const int NB = 1 << nbits;
+  for (int d = threadIdx.x; d < NB; d += RS_THREADS) shh[d] = 0;
+  __syncthreads();
+  long base = (long)blockIdx.x * RS_TILE;
+#pragma unroll
+  for (int it = 0; it < RS_ITEMS; it++) {
+    long i = base + it * RS_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&shh[(keys[i] >> shift) & (NB - 1)], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < NB; d += RS_THREADS)
+    hist[(long)d * ntiles + blockIdx.x] = shh[d];
+}
+
+static __global__ void k_radix_scatter(const u32 *__restrict__ kin,
+                                const u32 *__restrict__ vin, long n, int shift,
+                                int nbits, const u32 *__restrict__ offs,
+                                int ntiles, u32 *__restrict__ kout,
+                                u32 *__restrict__ vout) {
+  extern __shared__ u32 wh[];  // RS_WARPS x NB
+  const int NB = 1 << nbits;
+  for (int i = threadIdx.x; i < RS_WARPS * NB; i += RS_THREADS) wh[i] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  long base = (long)blockIdx.x * RS_TILE + (long)warp * (RS_TILE / RS_WARPS);
+  u32 kk[RS_ITEMS], vv[RS_ITEMS], pos[RS_ITEMS];
+  int dg[RS_ITEMS];
+  u32 *myh = wh + warp * NB;
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    long i = base + r * 32 + lane;
+    bool valid = i < n;
+    u32 k = valid ? kin[i] : 0u;
+    u32 v = valid ? (vin ? vin[i] : (u32)i) : 0u;
+    int d = valid ? (int)((k >> shift) & (NB - 1)) : NB;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    u32 rank = __popc(peers & lt);
+    u32 before = valid ? myh[d] : 0u;
+    __syncwarp();
+    if (valid && rank == 0) myh[d] = before + __popc(peers);
+    __syncwarp();
+    kk[r] = k;
+    vv[r] = v;
+    pos[r] = before + rank;
+    dg[r] = d;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < NB; d += RS_THREADS) {
+    u32 run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+      u32 t = wh[w * NB + d];
+      wh[w * NB + d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    int d = dg[r];
+    if (d < NB) {
+      u32 p = offs[(long)d * ntiles + blockIdx.x] + wh[warp * NB + d] + pos[r];
+      if (kout) kout[p] = kk[r];
+      vout[p] = vv[r];
+    }
+  }
+}
+
+static inline int radix_passes(u32 maxkey, int *bits_per_pass) {
+  int bits = 32 - __builtin_clz(maxkey | 1u);
+  int np = (bits + RS_MAXBITS - 1) / RS_MAXBITS;
+  *bits_per_pass = (bits + np - 1) / np;
+  return np;
+}
+
+struct SortWs {
+  u32 *k[2], *v[2], *hist, *scan;
+};
+
+static inline size_t sort_ws_bytes(long np, long ncells) {
+  int bpp;
+  radix_passes((u32)ncells, &bpp);
+  long ntiles = (np + RS_TILE - 1) / RS_TILE;
+  long hist = (1L << bpp) * ntiles;
+  long scanw = scan_ws_words(hist > ncells + 1 ? hist : ncells + 1);
+  long words = 4 * np + hist + scanw + 64;
+  return (size_t)words * 4 + 256;
+}
+
+static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
+  int bpp;
+  radix_passes((u32)ncells, &bpp);
+  long ntiles = (np + RS_TILE - 1) / RS_TILE;
+  long hist = (1L << bpp) * ntiles;
+  uintptr_t p = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+  u32 *w = (u32 *)p;
+  SortWs s;
+  s.k[0] = w;
+  s.k[1] = w + np;
+  s.v[0] = w + 2 * np;
+  s.v[1] = w + 3 * np;
+  s.hist = w + 4 * np;
+  s.scan = s.hist + hist;
+  return s;
+}
+
+static __global__ void k_copy_u32(const u32 *src, u32 *dst) { *dst = *src; }
+
+template <typename T>
+int index_sort(long np, const T *x, const T *y, const T *z, KeyGrid g,
+               u32 *indx, u32 *counts, u32 *cell_offset, u32 *sort_indx,
+               u32 *np_stay, void *ws, size_t ws_bytes, cudaStream_t s) {
+  long C = (long)(g.Nx - 1) * (g.Nr - 1);
+  CCL_REQUIRE(ws_bytes >= sort_ws_bytes(np, C), CCL_ERR_WORKSPACE,
+              "index_sort: workspace %zu < %zu bytes", ws_bytes,
+              sort_ws_bytes(np, C));
+  SortWs w = carve_sort_ws(ws, np, C);
+  cudaMemsetAsync(counts, 0, (C + 1) * sizeof(u32), s);
+  if (np > 0) {
+    k_keys<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, g, indx, counts);
+    CCL_LAUNCH_CHECK("keys");
+  }
+  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1,
+                          w.scan, s);
+  if (rc) return rc;
+  k_copy_u32<<<1, 1, 0, s>>>(cell_offset + C, np_stay);
+  CCL_LAUNCH_CHECK("np_stay");
+  if (np == 0) return CCL_OK;
+  int bpp;
+  int npass = radix_passes((u32)C, &bpp);
+  long ntiles = (np + RS_TILE - 1) / RS_TILE;
+  size_t smem_h = (size_t)(1 << bpp) * 4, smem_s = RS_WARPS * smem_h;
+  const u32 *kin = indx, *vin = nullptr;
+  for (int p = 0; p < npass; p++) {
+    int shift = p * bpp;
+    k_radix_hist<<<(unsigned)ntiles, RS_THREADS, smem_h, s>>>(
+        kin, np, shift, bpp, w.hist, (int)ntiles);
+    CCL_LAUNCH_CHECK("radix_hist");
+    rc = scan_exclusive(w.hist, (1L << bpp) * ntiles, w.hist, nullptr, w.scan,
+                        s);
+    if (rc) return rc;
+    bool last = p == npass - 1;
+    u32 *kout = last ? nullptr : w.k[p & 1];
+    u32 *vout = last ? sort_indx : w.v[p & 1];
+    k_radix_scatter<<<(unsigned)ntiles, RS_THREADS, smem_s, s>>>(
+        kin, vin, np, shift, bpp, w.hist, (int)ntiles, kout, vout);
+    CCL_LAUNCH_CHECK("radix_scatter");
+    kin = kout;
+    vin = vout;
+  }
+  return CCL_OK;
+}
+
+// ---------------------------------------------------------------------
+// data_align_dbl (particles_generic.cl:156-169) over up to 16 components
+template <typename T>
+__global__ void k_align(long n, int ncomp, ptrs<16> src, ptrs<16> dst,
+                        const u32 *__restrict__ idx) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    u32 j = idx[i];
+    for (int c = 0; c < ncomp; c++)
+      ((T *)dst.p[c])[i] = ((const T *)src.p[c])[j];
+  }
+}
+
+template <typename T>
+int align(long n, int ncomp, void *const *src, void *const *dst,
+          const u32 *idx, cudaStream_t s) {
+  CCL_REQUIRE(ncomp >= 0 && ncomp <= 16, CCL_ERR_ARG, "align: ncomp %d", ncomp);
+  if (n == 0 || ncomp == 0) return CCL_OK;
+  ptrs<16> a, b;
+  for (int c = 0; c < ncomp; c++) {
+    CCL_REQUIRE(src[c] && dst[c], CCL_ERR_ARG, "align: null component %d", c);
+    a.p[c] = src[c];
+    b.p[c] = dst[c];
+  }
+  k_align<T><<<grid_for(n, 256), 256, 0, s>>>(n, ncomp, a, b, idx);
+  CCL_LAUNCH_CHECK("align");
+  return CCL_OK;
+}
+
+static __global__ void k_iota(u32 *a, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x)
+    a[i] = (u32)i;
+}
+
+// ---------------------------------------------------------------------
+// fill_grid (particles_generic.cl:33-84): one thread per cell
+template <typename T>
+__global__ void k_fill_grid(long ncells, T *x, T *y, T *z, T *w,
+                            const double *theta, const double *xgrid,
+                            const double *rgrid, u32 Nx, u32 npx, u32 npr,
+                            u32 npth) {
+  const u32 nxc = Nx - 1, nppc = npx * npr * npth;
+  for (long ic = blockIdx.x * (long)blockDim.x + threadIdx.x; ic < ncells;
+       ic += (long)gridDim.x * blockDim.x) {
+    u32 icell = (u32)ic, ir = icell / nxc, ix = icell - nxc * ir;
+    long ip = (long)icell * nppc;
+    double xmin = xgrid[ix], rmin = rgrid[ir], thmin = theta[icell];
+    double Lx = xgrid[ix + 1] - xgrid[ix], Lr = rgrid[ir + 1] - rgrid[ir];
+    double ddx = 1. / ((double)npx), ddr = 1. / ((double)npr);
+    double dth = 2 * M_PI / ((double)npth);
+    for (u32 ith = 0; ith < npth; ith++) {
+      double th = thmin + ith * dth;
+      double sn, cs;
+      sincos(th, &sn, &cs);
+      for (u32 irr = 0; irr < npr; irr++) {
+        double rp = rmin + (0.5 + (int)irr) * ddr * Lr;
+        double rps = rp * sn, rpc = rp * cs;
+        for (u32 ixx = 0; ixx < npx; ixx++) {
+          x[ip] = (T)(xmin + (0.5 + (int)ixx) * ddx * Lx);
+          y[ip] = (T)rps;
+          z[ip] = (T)rpc;
+          w[ip] = (T)rp;
+          ip++;
+        }
+      }
+    }
+  }
+}
+
+// profile_by_interpolant (particles_generic.cl:6-30); the knot search is
+// clamped to the last interval where the reference reads past its arrays.
+template <typename T>
+__global__ void k_dens_profile(long np, const T *x, T *w, const double *xx,
+                               const double *ff, const double *dxm1,
+                               u32 nloc) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x) {
+    double xp = (double)x[i];
+    u32 k;
+    for (k = 0; k < nloc - 1; k++)
+      if (xp > xx[k] && xp <= xx[k + 1]) break;
+    if (k > nloc - 2) k = nloc - 2;
+    double fm = ff[k] * dxm1[k], fp = ff[k + 1] * dxm1[k];
+    double f = fm * (xx[k + 1] - xp) + fp * (xp - xx[k]);
+    w[i] = (T)((double)w[i] * f);
+  }
+}
+
+template <typename T>
+__global__ void k_gamma_inv(long np, const T *px, const T *py, const T *pz,
+                            T *g) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x)
+    g[i] = (T)1 / sqrt((T)1 + px[i] * px[i] + py[i] * py[i] + pz[i] * pz[i]);
+}
+
+}  // namespace ccl

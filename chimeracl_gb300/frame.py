@@ -1,0 +1,52 @@
+"""Moving window (the reference's chimeraCL/frame.py): grid shift and
+plasma injection into the uncovered slab."""
+import numpy as np
+
+
+class Frame:
+    def __init__(self, configs_in, comm=None):
+        self._process_configs(configs_in)
+
+    def _process_configs(self, configs_in):
+        self.Args = configs_in
+        self.Args.setdefault("Steps", 1.0)
+        self.Args.setdefault("Velocity", 0.0)
+        self.Args.setdefault("dt", 1)
+        self.Args.setdefault("DensityProfiles", None)
+
+    def shift_grids(self, grids=(), steps=None):
+        """Xmin, Xmax, Xgrid += Steps*dt*V on host and device (frame.py:22-30);
+        the spectral transforms pick the shift up as the phase exp(i kx Xmin)."""
+        if steps is None:
+            steps = self.Args["Steps"]
+        x_shift = steps * self.Args["dt"] * self.Args["Velocity"]
+        for grid in grids:
+            for store in (grid.Args, grid.DataDev):
+                for arg in ("Xmax", "Xmin", "Xgrid"):
+                    store[arg] += x_shift
+
+    def inject_plasma(self, species, grid, steps=None):
+        """Fill the slab behind the right edge, then sort, align and find the
+        new right limit of each species (frame.py:32-64)."""
+        if steps is None:
+            steps = self.Args["Steps"]
+        x_shift = steps * self.Args["dt"] * self.Args["Velocity"]
+        for sp in species:
+            if sp.Args["Np"] == 0:
+                sp.Args["right_lim"] = grid.Args["Xmax"] - x_shift
+            dom = {"Xmin": sp.Args["right_lim"]}
+            dom["Xmax"] = dom["Xmin"] + x_shift
+            dom["Rmin"] = grid.Args["Rmin"] * (grid.Args["Rmin"] > 0)
+            dom["Rmax"] = grid.Args["Rmax"]
+            sp.make_new_domain(dom, density_profiles=self.Args["DensityProfiles"])
+            if "InjectorSource" in sp.Args:
+                sp.add_new_particles(sp.Args["InjectorSource"])
+            else:
+                sp.add_new_particles()
+        for sp in species:
+            sp.free_added()
+            sp.sort_parts(grid=grid)
+            sp.align_parts()
+            nppc = np.int32(np.prod(sp.Args["Nppc"]) + 1)
+            x_max = float(sp.DataDev["x"][-nppc:].max().item())
+            sp.Args["right_lim"] = x_max + 0.5 * sp.Args["ddx"]

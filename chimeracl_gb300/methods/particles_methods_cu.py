@@ -1,0 +1,203 @@
+"""Particle methods (the CUDA counterpart of
+chimeraCL/methods/particles_methods_cl.py): coordinate push, cell sort,
+align, plasma/beam injection."""
+import numpy as np
+import torch
+
+from .._lib import PP, call, sort_workspace_bytes, stream
+from .generic_methods_cu import GenericMethodsCU, LazyScalar
+
+
+class ParticleMethodsCU(GenericMethodsCU):
+    def init_particle_methods(self):
+        self.init_generic_methods()
+        # Host generator of the injector's random draws (the reference uses a
+        # device Threefry stream, particles_methods_cl.py:22): PCG64, seeded,
+        # so that runs are reproducible and comparable draw for draw.
+        seed = getattr(self, "_seed", None)
+        if seed is None:
+            seed = self.comm.seed
+        self._rng = np.random.Generator(np.random.PCG64(seed))
+
+    def _comps(self):
+        if "Immobile" in self.Args:
+            return ["x", "y", "z", "w"]
+        return ["x", "y", "z", "px", "py", "pz", "w", "g_inv"]
+
+    def add_new_particles(self, source=None):
+        """particles_methods_cl.py:40-64"""
+        src = self.DataDev if source is None else source.DataDev
+        for arg in self._comps():
+            self.DataDev[arg] = torch.cat([self.DataDev[arg], src[arg + "_new"]])
+        self.reset_num_parts()
+        self.flag_sorted = False
+
+    def make_new_domain(self, parts_in, density_profiles=None):
+        """particles_methods_cl.py:66-147"""
+        A, D = self.Args, self.DataDev
+        xmin, xmax, rmin, rmax = (parts_in[k] for k in ("Xmin", "Xmax", "Rmin", "Rmax"))
+        Nx_loc = int(np.ceil((xmax - xmin) / A["dx"]) + 1)
+        Nr_loc = int(np.round((rmax - rmin) / A["dr"]) + 1)
+        Xg = xmin + A["dx"] * np.arange(Nx_loc)
+        Rg = rmin + A["dr"] * np.arange(Nr_loc)
+        A["right_lim"] = Xg[-1]
+        ncells = (Nx_loc - 1) * (Nr_loc - 1)
+        Np = int(ncells * np.prod(A["Nppc"]))
+        real = self.comm.real
+        for arg in ("x", "y", "z", "w"):
+            D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+        theta = self.dev_arr(shape=ncells, dtype=np.double)
+        self._fill_arr_rand(theta, xmin=0, xmax=2 * np.pi)
+        Xg_d, Rg_d = self.dev_arr(val=Xg), self.dev_arr(val=Rg)
+        npx, npr, npth = (int(v) for v in A["Nppc"])
+        call("ccl_fill_grid", self._dt, ncells, D["x_new"].data_ptr(), D["y_new"].data_ptr(),
+             D["z_new"].data_ptr(), D["w_new"].data_ptr(), theta.data_ptr(), Xg_d.data_ptr(),
+             Rg_d.data_ptr(), Nx_loc, npx, npr, npth, stream())
+        D["w_new"] *= A["w0"]
+        if density_profiles is not None:
+            for prf in density_profiles:
+                if prf["coord"] != "x":
+                    print("Only longitudinal profiling is implemented")
+                    continue
+                self.dens_profile(prf["points"], prf["values"], parts_in["Xmin"],
+                                  parts_in["Xmax"], coord=prf["coord"] + "_new", weight="w_new")
+        if "Immobile" not in A:
+            for arg in ("px", "py", "pz"):
+                if "d" + arg not in parts_in and arg + "_c" not in parts_in:
+                    D[arg + "_new"] = torch.zeros(Np, dtype=real, device=self.comm.device)
+                    parts_in[arg + "_c"] = 0
+                    parts_in["d" + arg] = 0
+                else:
+                    D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+                    parts_in.setdefault(arg + "_c", 0)
+                    if "d" + arg in parts_in:
+                        self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"],
+                                             sigma=parts_in["d" + arg])
+                    else:
+                        parts_in["d" + arg] = 0
+                        D[arg + "_new"].fill_(parts_in[arg + "_c"])
+            mom = sum(parts_in[k] ** 2 for k in ("px_c", "py_c", "pz_c", "dpx", "dpy", "dpz"))
+            D["g_inv_new"] = torch.ones(Np, dtype=real, device=self.comm.device)
+            if mom != 0:
+                call("ccl_gamma_inv", self._dt, Np, D["px_new"].data_ptr(),
+                     D["py_new"].data_ptr(), D["pz_new"].data_ptr(), D["g_inv_new"].data_ptr(),
+                     stream())
+
+    def make_new_beam(self, parts_in):
+        """particles_methods_cl.py:149-177 (normal draws in the order
+        x, y, z, px, py, pz)."""
+        D, Np = self.DataDev, int(parts_in["Np"])
+        real = self.comm.real
+        for arg in ("x", "y", "z", "px", "py", "pz", "w"):
+            D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+        for arg in ("x", "y", "z"):
+            self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"], sigma=parts_in["L" + arg])
+        for arg in ("px", "py", "pz"):
+            parts_in.setdefault(arg + "_c", 0)
+            parts_in.setdefault("d" + arg, 0)
+            self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"], sigma=parts_in["d" + arg])
+        D["w_new"].fill_(parts_in["FullCharge"] / parts_in["Np"])
+        D["g_inv_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+        call("ccl_gamma_inv", self._dt, Np, D["px_new"].data_ptr(), D["py_new"].data_ptr(),
+             D["pz_new"].data_ptr(), D["g_inv_new"].data_ptr(), stream())
+
+    def dens_profile(self, x_prf, f_prf, xmin, xmax, coord="x", weight="w"):
+        """particles_methods_cl.py:179-204"""
+        x_prf = np.array(x_prf, dtype=np.double)
+        f_prf = np.array(f_prf, dtype=np.double)
+        i0 = (x_prf < xmin).sum() - 1
+        i1 = (x_prf < xmax).sum() + 1
+        x_loc = x_prf[i0:i1]
+        f_loc = f_prf[i0:i1]
+        if x_loc.size < 2:
+            raise ValueError("dens_profile: the profile knots must bracket the domain "
+                             f"[{xmin}, {xmax}]")
+        dxm1 = 1.0 / (x_loc[1:] - x_loc[:-1])
+        xl, fl, dl = self.dev_arr(val=x_loc), self.dev_arr(val=f_loc), self.dev_arr(val=dxm1)
+        D = self.DataDev
+        call("ccl_dens_profile", self._dt, D[coord].numel(), D[coord].data_ptr(),
+             D[weight].data_ptr(), xl.data_ptr(), fl.data_ptr(), dl.data_ptr(), x_loc.size,
+             stream())
+
+    def push_coords(self, mode="half"):
+        """particles_methods_cl.py:206-223"""
+        if self.Args["Np"] == 0 or "Immobile" in self.Args:
+            return
+        D = self.DataDev
+        dt = self.Args["dt_2"] if mode == "half" else self.Args["dt"]
+        call("ccl_push_x", self._dt, self.Args["Np"], D["x"].data_ptr(), D["y"].data_ptr(),
+             D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(), D["pz"].data_ptr(),
+             D["g_inv"].data_ptr(), float(dt), stream())
+        self.flag_sorted = False
+
+    def index_sort(self, grid):
+        """particles_methods_cl.py:225-261: keys, counts, exclusive prefix
+        (cell_offset), stable sort -- one C-ABI call.  Np_stay stays on the
+        device (read lazily through Args)."""
+        Np = self.Args["Np"]
+        C = grid.Args["Nxm1Nrm1"]
+        dev, D = self.comm.device, self.DataDev
+        i32 = torch.int32
+        D["indx_in_cell"] = torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np]
+        D["sum_in_cell"] = torch.empty(C + 1, dtype=i32, device=dev)
+        D["cell_offset"] = torch.empty(C + 2, dtype=i32, device=dev)
+        D["sort_indx"] = torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np]
+        ws_bytes = sort_workspace_bytes(Np, C)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        G = grid.Args
+        call("ccl_index_sort", self._dt, Np, D["x"].data_ptr(), D["y"].data_ptr(),
+             D["z"].data_ptr(), G["Nx"], float(G["Xmin"]), float(G["dx_inv"]), G["Nr"],
+             float(G["Rmin"]), float(G["dr_inv"]), D["indx_in_cell"].data_ptr(),
+             D["sum_in_cell"].data_ptr(), D["cell_offset"].data_ptr(),
+             D["sort_indx"].data_ptr(), D["Np_stay_dev"].data_ptr(), ws.data_ptr(), ws_bytes,
+             stream())
+        dict.__setitem__(self.Args, "Np_stay", LazyScalar(D["Np_stay_dev"]))
+
+    def align_and_damp(self, comps_align):
+        """particles_methods_cl.py:263-286"""
+        D = self.DataDev
+        ns = self.Args["Np_stay"]
+        if ns == 0:
+            for comp in comps_align + ["sort_indx"]:
+                D[comp] = D[comp][:0].clone()
+            self.reset_num_parts()
+            return
+        src = [D[c] for c in comps_align]
+        dst = [torch.empty(ns, dtype=D[c].dtype, device=self.comm.device) for c in comps_align]
+        call("ccl_align", self._dt, ns, len(src), PP(src), PP(dst), D["sort_indx"].data_ptr(),
+             stream())
+        for c, t in zip(comps_align, dst):
+            D[c] = t
+        D["sort_indx"] = torch.empty(ns, dtype=torch.int32, device=self.comm.device)
+        call("ccl_iota_u32", D["sort_indx"].data_ptr(), ns, stream())
+        self.reset_num_parts()
+
+    def reset_num_parts(self, Np=None):
+        """particles_methods_cl.py:288-293"""
+        if Np is None:
+            Np = self.DataDev["x"].numel()
+        self.DataDev["Np"].fill_(Np)
+        self.DataDev["Np_stay_dev"].fill_(Np)
+        self.Args["Np"] = Np
+        self.Args["Np_stay"] = Np
+
+    def _fill_arr_randn(self, arr, mu=0, sigma=1):
+        v = mu + sigma * self._rng.standard_normal(arr.numel())
+        arr.copy_(torch.from_numpy(v).to(arr.dtype))
+
+    def _fill_arr_rand(self, arr, xmin=0, xmax=1):
+        v = xmin + (xmax - xmin) * self._rng.random(arr.numel())
+        arr.copy_(torch.from_numpy(v).to(arr.dtype))
+
+    def _cumsum(self, arr_in, allocator=None, output_dtype=np.uint32):
+        """[0, cumsum(arr_in)...] (particles_methods_cl.py:303-311)."""
+        out = torch.zeros(arr_in.numel() + 1, dtype=torch.int64, device=arr_in.device)
+        out[1:] = torch.cumsum(arr_in.to(torch.int64), 0)
+        return out.to(torch.int32 if np.dtype(output_dtype) == np.uint32 else torch.int64)
+
+    def free_mp(self):
+        """Memory pools are torch's caching allocator: nothing to release."""
+
+    def free_added(self):
+        for arg in self._comps():
+            self.DataDev.pop(arg + "_new", None)

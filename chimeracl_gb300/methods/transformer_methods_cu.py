@@ -1,0 +1,254 @@
+"""Fourier-Bessel transform methods (the CUDA counterpart of
+chimeraCL/methods/transformer_methods_cl.py).
+
+A full transform is the batched radial Hankel GEMM (``ccl_dht_gemm``) and the
+batched longitudinal FFT (``ccl_fft_forward_rows`` / ``_backward_rows``) with
+the moving-window phase, real-part cast and (optionally) the smoothing filter
+applied inside the FFT kernel; the half transforms are the FFT kernel alone.
+"""
+import torch
+
+from .._lib import PP, P, call, stream
+from .generic_methods_cu import GenericMethodsCU
+
+
+class TransformerMethodsCU(GenericMethodsCU):
+    def init_transformer_methods(self):
+        self.init_generic_methods()
+        self._phs_cache = {}
+        self._prepare_fft()
+        self._prepare_dot()
+
+    # ------------------------------------------------------------------
+    def _phase(self, dir):
+        """exp(+i kx Xmin) for dir=1, exp(-i kx Xmin) for dir=0
+        (get_phase_plus/minus), recomputed only when Xmin moves."""
+        x0 = float(self.Args["Xmin"])
+        key = (dir, x0)
+        t = self._phs_cache.get(dir)
+        if t is None or t[0] != x0:
+            buf = self.DataDev.get("phs_shft_" + str(dir))
+            if buf is None:
+                buf = torch.empty(self.Args["Nx"], dtype=self.comm.cplx, device=self.comm.device)
+                self.DataDev["phs_shft_" + str(dir)] = buf
+            call("ccl_phase", self._dt, self.Args["Nx"], buf.data_ptr(),
+                 self.DataDev["kx"].data_ptr(), x0, 1 if dir == 1 else -1, stream())
+            self._phs_cache[dir] = (x0, buf)
+        self.DataDev["phs_shft"] = self._phs_cache[dir][1]
+        del key
+        return self._phs_cache[dir][1]
+
+    def _prepare_fft(self):
+        """Nothing to plan ahead: FFT plans and twiddle tables are built by
+        the library on first use of each length."""
+
+    def _prepare_dot(self):
+        """The Hankel GEMM needs no preparation; matrices are uploaded by
+        send_args_to_dev."""
+
+    def _dht(self, Y, A, X, ldx, ldy, ncols, cplx, alpha=1.0, beta=0.0, xoff=0, yoff=0):
+        """Y = beta*Y + alpha*(A X) on one matrix pair (offsets in elements of
+        the tensors' own dtype)."""
+        m = A.shape[0]
+        a = complex(alpha)
+        xp = X.data_ptr() + xoff * X.element_size()
+        yp = Y.data_ptr() + yoff * Y.element_size()
+        call("ccl_dht_gemm", self._dt, 1, m, A.shape[1], ncols, int(cplx), PP([A]), PP([xp]), ldx,
+             PP([yp]), ldy, a.real, a.imag, float(beta), stream())
+
+    def _cdot(self, out, A, X):
+        """out = A X for a complex (Nr-1, Nx) field (the reference's _cdot)."""
+        nx = X.shape[-1]
+        self._dht(out, A, X, 2 * nx, 2 * nx, 2 * nx, True)
+
+    def _ddot(self, out, A, X):
+        nx = X.shape[-1]
+        self._dht(out, A, X, nx, nx, nx, False)
+
+    # ------------------------------------------------------------------
+    def transform_field(self, arg_cmp, dir, mode, filt=None):
+        """transformer_methods_cl.py:38-64.  ``filt`` (optional, a list of
+        M+1 real filters) multiplies the forward result in the FFT epilogue,
+        which is fields_smooth fused into the transform."""
+        A = self.Args
+        phs = self._phase(dir)
+        M, Nx, Nr = A["M"], A["Nx"], A["Nr"]
+        nrows = Nr - 1
+        for m in range(M + 1):
+            s = str(m)
+            rs = self.DataDev[arg_cmp + "_m" + s]
+            sp = self.DataDev[arg_cmp + "_fb_m" + s]
+            if dir == 0:
+                f = None if filt is None else filt[m]
+                fptr = None if f is None else f.data_ptr()
+                if mode == "full":
+                    mat = self._real_dev("DHT_m" + s)
+                    if m == 0:
+                        buf = self.DataDev["fld_buff1_d"]
+                        self._dht(buf, mat, rs, Nx, Nx, Nx, False, xoff=Nx)
+                        call("ccl_fft_forward_rows", self._dt, nrows, Nx, buf.data_ptr(), Nx, 1,
+                             sp.data_ptr(), phs.data_ptr(), fptr, stream())
+                    else:
+                        self._dht(sp, mat, rs, 2 * Nx, 2 * Nx, 2 * Nx, True, xoff=Nx)
+                        call("ccl_fft_forward_rows", self._dt, nrows, Nx, sp.data_ptr(), Nx, 0,
+                             sp.data_ptr(), phs.data_ptr(), fptr, stream())
+                else:
+                    call("ccl_fft_forward_rows", self._dt, nrows, Nx, P(rs, Nx), Nx,
+                         int(m == 0), sp.data_ptr(), phs.data_ptr(), fptr, stream())
+            else:
+                if mode == "full":
+                    mat = self._real_dev("DHT_inv_m" + s)
+                    if m == 0:
+                        buf = self.DataDev["fld_buff0_d"]
+                        call("ccl_fft_backward_rows", self._dt, nrows, Nx, sp.data_ptr(),
+                             buf.data_ptr(), Nx, 1, phs.data_ptr(), stream())
+                        self._dht(rs, mat, buf, Nx, Nx, Nx, False, yoff=Nx)
+                    else:
+                        buf = self.DataDev["fld_buff0_c"]
+                        call("ccl_fft_backward_rows", self._dt, nrows, Nx, sp.data_ptr(),
+                             buf.data_ptr(), Nx, 0, phs.data_ptr(), stream())
+                        self._dht(rs, mat, buf, 2 * Nx, 2 * Nx, 2 * Nx, True, yoff=Nx)
+                else:
+                    call("ccl_fft_backward_rows", self._dt, nrows, Nx, sp.data_ptr(), P(rs, Nx),
+                         Nx, int(m == 0), phs.data_ptr(), stream())
+
+    def _transform_forward(self, dht_arg, arg_in, arg_out, phs_shft):
+        self.transform_field(arg_in[:-2], 0, "full")
+
+    def _transform_backward(self, dht_arg, arg_in, arg_out, phs_shft):
+        self.transform_field(arg_out[:-2], 1, "full")
+
+    def _half_transform_forward(self, dht_arg, arg_in, arg_out, phs_shft):
+        self.transform_field(arg_in[:-2], 0, "half")
+
+    def _half_transform_backward(self, dht_arg, arg_in, arg_out, phs_shft):
+        self.transform_field(arg_out[:-2], 1, "half")
+
+    # ------------------------------------------------------------------
+    def field_poiss_vec(self, fld):
+        """B_m *= 1/w^2 (transformer_methods_cl.py:66-71)"""
+        for m in range(self.Args["M"] + 1):
+            for c in self.Args["vec_comps"]:
+                self.mult_elementwise(self._real_dev("Poiss_m" + str(m)),
+                                      self.DataDev[fld + c + "_fb_m" + str(m)])
+
+    def field_poiss_scl(self, fld):
+        for m in range(self.Args["M"] + 1):
+            self.mult_elementwise(self._real_dev("Poiss_m" + str(m)),
+                                  self.DataDev[fld + "_fb_m" + str(m)])
+
+    def fields_smooth(self, flds):
+        """transformer_methods_cl.py:79-85"""
+        for m in range(self.Args["M"] + 1):
+            for fld in flds:
+                self.mult_elementwise(self._real_dev("SmoothingFilter_m" + str(m)),
+                                      self.DataDev[fld + "_fb_m" + str(m)])
+
+    def _get_mm1_vec(self, fld):
+        if self.Args["M"] == 0:
+            return
+        for c in self.Args["vec_comps"]:
+            self._get_mm1_one(fld + c, c)
+
+    def _get_mm1_scl(self, fld, comp="x"):
+        if self.Args["M"] == 0:
+            return
+        self._get_mm1_one(fld, comp)
+
+    def _get_mm1_one(self, fld, comp):
+        A = self.Args
+        call("ccl_get_m1", self._dt, A["Nr"] - 1, A["Nx"],
+             self.DataDev["buff_fb_m-1_" + comp].data_ptr(),
+             self.DataDev[fld + "_fb_m1"].data_ptr(), stream())
+
+    def field_grad(self, scl_in, vec_out):
+        """Spectral gradient (transformer_methods_cl.py:87-133)."""
+        A, D = self.Args, self.DataDev
+        M = A["M"]
+        kx = self._real_dev("kx")
+        b0 = D["fld_buff0_c"]
+        self._get_mm1_scl(scl_in)
+        for m in range(M + 1):
+            s = str(m)
+            ox, oy, oz = (D[vec_out + c + "_fb_m" + s] for c in A["vec_comps"])
+            for o in (ox, oy, oz):
+                self.set_to(o, 0.0)
+            self.ab_dot_x(1j, kx, D[scl_in + "_fb_m" + s], ox)
+            if m > 0:
+                f = D[scl_in + "_fb_m" + str(m - 1)]
+            elif M > 0:
+                f = D["buff_fb_m-1_x"]
+            else:
+                continue
+            self._cdot(b0, self._real_dev("dDHT_minus_m" + s), f)
+            self.zpaxz(oy, -1.0, b0)
+            self.zpaxz(oz, -1.0j, b0)
+            if m < M:
+                self._cdot(b0, self._real_dev("dDHT_plus_m" + s), D[scl_in + "_fb_m" + str(m + 1)])
+                self.append_c2c(oy, b0)
+                self.zpaxz(oz, -1.0j, b0)
+
+    def field_div(self, vec_in, scl_out):
+        """Spectral divergence (transformer_methods_cl.py:135-183)."""
+        A, D = self.Args, self.DataDev
+        M = A["M"]
+        kx = self._real_dev("kx")
+        b0, b1 = D["fld_buff0_c"], D["fld_buff1_c"]
+        for c in ("y", "z"):
+            self._get_mm1_scl(vec_in + c, c)
+        for m in range(M + 1):
+            s = str(m)
+            out = D[scl_out + "_fb_m" + s]
+            self.set_to(out, 0.0)
+            self.ab_dot_x(1j, kx, D[vec_in + "x_fb_m" + s], out)
+            if m > 0:
+                fy, fz = D[vec_in + "y_fb_m" + str(m - 1)], D[vec_in + "z_fb_m" + str(m - 1)]
+            elif M > 0:
+                fy, fz = D["buff_fb_m-1_y"], D["buff_fb_m-1_z"]
+            else:
+                continue
+            self.axpbyz(-1.0j, fz, -1.0, fy, b0)
+            self._cdot(b1, self._real_dev("dDHT_minus_m" + s), b0)
+            self.append_c2c(out, b1)
+            if m < M:
+                fy, fz = D[vec_in + "y_fb_m" + str(m + 1)], D[vec_in + "z_fb_m" + str(m + 1)]
+                self.axpbyz(-1.0j, fz, 1.0, fy, b0)
+                self._cdot(b1, self._real_dev("dDHT_plus_m" + s), b0)
+                self.append_c2c(out, b1)
+
+    def field_rot(self, fld_in, fld_out):
+        """Spectral curl (transformer_methods_cl.py:185-263)."""
+        A, D = self.Args, self.DataDev
+        M = A["M"]
+        kx = self._real_dev("kx")
+        b0, b1 = D["fld_buff0_c"], D["fld_buff1_c"]
+        self._get_mm1_vec(fld_in)
+        for m in range(M + 1):
+            s = str(m)
+            ox, oy, oz = (D[fld_out + c + "_fb_m" + s] for c in A["vec_comps"])
+            for o in (ox, oy, oz):
+                self.set_to(o, 0.0)
+            self.ab_dot_x(-1.0j, kx, D[fld_in + "z_fb_m" + s], oy)
+            self.ab_dot_x(1.0j, kx, D[fld_in + "y_fb_m" + s], oz)
+            if m > 0:
+                fx, fy, fz = (D[fld_in + c + "_fb_m" + str(m - 1)] for c in A["vec_comps"])
+            elif M > 0:
+                fx, fy, fz = (D["buff_fb_m-1_" + c] for c in A["vec_comps"])
+            else:
+                continue
+            dm = self._real_dev("dDHT_minus_m" + s)
+            self.axpbyz(-1.0, fz, 1.0j, fy, b0)
+            self._cdot(b1, dm, b0)
+            self.append_c2c(ox, b1)
+            self._cdot(b0, dm, fx)
+            self.zpaxz(oy, -1.0j, b0)
+            self.zpaxz(oz, 1.0, b0)
+            if m < M:
+                fx, fy, fz = (D[fld_in + c + "_fb_m" + str(m + 1)] for c in A["vec_comps"])
+                dp = self._real_dev("dDHT_plus_m" + s)
+                self.axpbyz(1.0, fz, 1.0j, fy, b0)
+                self._cdot(b1, dp, b0)
+                self.append_c2c(ox, b1)
+                self._cdot(b0, dp, fx)
+                self.zpaxz(oy, -1.0j, b0)
+                self.zpaxz(oz, -1.0, b0)

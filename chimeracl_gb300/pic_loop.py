@@ -1,0 +1,148 @@
+"""The particle-in-cell loop (the reference's chimeraCL/pic_loop.py).
+
+``PIC_loop.step()`` runs the reference's sequence (pic_loop.py:57-142):
+frame shift + injection every ``Steps``; half push + sort; current deposit;
+half push + sort; charge deposit; forward transforms of rho, J with the
+smoothing filter; dN0 <- dN1; spectral grad rho -> dN1; PSATD push; edge
+damping; B from G; backward transforms of E, B; gather + Boris push.
+
+With ``timit=True`` each phase is timed on the device with CUDA events under
+the reference's twelve phase names (device time, no host synchronisation
+inside the step; ``Timer`` is filled when read through ``timings()``)."""
+import numpy as np
+import torch
+
+loop_steps = ["frame", "push-x", "sort", "depose", "transform", "smooth", "data_copy",
+              "grad", "push-eb", "damp-eb", "restore_B", "gather + push-p"]
+
+
+def timer_plot(Timer):
+    import matplotlib.pyplot as plt
+    fig, ax = plt.subplots(figsize=(16, 5))
+    keys = list(Timer.keys())
+    ind = np.arange(1, len(keys) + 1)
+    plt.bar(ind, [Timer[k] for k in keys])
+    ax.set_xticks(ind)
+    ax.set_xticklabels(keys)
+    return fig
+
+
+class PIC_loop:
+    def __init__(self, solvers=(), species=(), frames=(), diags=(), timit=False,
+                 fuse_smooth=True):
+        self.solvers = list(solvers)
+        self.mainsolver = self.solvers[0]
+        self.species = list(species)
+        self.frames = list(frames)
+        self.diags = list(diags)
+        self.timit = timit
+        # fuse_smooth: apply the smoothing filter inside the forward FFT of
+        # rho and J (same arithmetic as fields_smooth after the transform)
+        self.fuse_smooth = fuse_smooth
+        self.it = 0
+        self.Timer = {k: 0.0 for k in loop_steps}
+        self._events = []
+
+    def timer_start(self):
+        if self.timit:
+            self._t0 = torch.cuda.Event(enable_timing=True)
+            self._t0.record()
+
+    def timer_record(self, name):
+        if self.timit:
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            self._events.append((name, self._t0, e))
+
+    def timings(self):
+        """Accumulated device time per phase in seconds."""
+        if self._events:
+            torch.cuda.synchronize()
+            for name, a, b in self._events:
+                self.Timer[name] += a.elapsed_time(b) * 1e-3
+            self._events = []
+        return self.Timer
+
+    def step(self):
+        for diag in self.diags:
+            diag.make_record(self.it)
+
+        self.timer_start()
+        for frame in self.frames:
+            if np.mod(self.it, frame.Args["Steps"]) == 0:
+                frame.shift_grids(grids=self.solvers)
+                frame.inject_plasma(species=self.species, grid=self.mainsolver)
+        self.timer_record("frame")
+
+        for parts in self.species:
+            self.timer_start()
+            parts.push_coords(mode="half")
+            self.timer_record("push-x")
+            self.timer_start()
+            parts.sort_parts(grid=self.mainsolver)
+            self.timer_record("sort")
+
+        self.timer_start()
+        for solver in self.solvers:
+            solver.depose_currents(species=self.species)
+        self.timer_record("depose")
+
+        for parts in self.species:
+            self.timer_start()
+            parts.push_coords(mode="half")
+            self.timer_record("push-x")
+            self.timer_start()
+            parts.sort_parts(grid=self.mainsolver)
+            self.timer_record("sort")
+
+        for solver in self.solvers:
+            self.timer_start()
+            solver.depose_charge(species=self.species)
+            self.timer_record("depose")
+
+            self.timer_start()
+            M = solver.Args["M"]
+            if self.fuse_smooth:
+                filt = [solver._real_dev("SmoothingFilter_m" + str(m)) for m in range(M + 1)]
+                solver.fb_transform(scals=["rho"], vects=["J"], dir=0, filt=filt)
+                self.timer_record("transform")
+            else:
+                solver.fb_transform(scals=["rho"], vects=["J"], dir=0)
+                self.timer_record("transform")
+                self.timer_start()
+                solver.fields_smooth(flds=["rho", "Jx", "Jy", "Jz"])
+                self.timer_record("smooth")
+
+            # dN0 <- dN1: the old gradient becomes N0 by exchanging buffers,
+            # and field_grad overwrites dN1 (pic_loop.py:106-111 copies)
+            self.timer_start()
+            D = solver.DataDev
+            for m in range(M + 1):
+                for c in solver.Args["vec_comps"]:
+                    s = c + "_fb_m" + str(m)
+                    D["dN0" + s], D["dN1" + s] = D["dN1" + s], D["dN0" + s]
+            self.timer_record("data_copy")
+
+            self.timer_start()
+            solver.field_grad("rho", "dN1")
+            self.timer_record("grad")
+            self.timer_start()
+            solver.push_fields()
+            self.timer_record("push-eb")
+            self.timer_start()
+            solver.damp_fields()
+            self.timer_record("damp-eb")
+            self.timer_start()
+            solver.restore_B_fb()
+            self.timer_record("restore_B")
+            self.timer_start()
+            solver.fb_transform(vects=["E", "B"], dir=1)
+            self.timer_record("transform")
+            self.timer_start()
+            solver.gather_and_push(species=self.species)
+            self.timer_record("gather + push-p")
+
+        for parts in self.species:
+            parts.free_mp()
+        self.it += 1
+        return self.it

@@ -1,0 +1,275 @@
+/*
+ * chimeracl_gb300 -- C ABI of the GB300 (sm_103a) kernels behind the
+ * quasi-cylindrical PSATD particle-in-cell step.
+ *
+ * Every entry point replaces one method (or one fused group of methods) of
+ * chimeraCL's methods layer (chimeraCL/methods/*_methods_cl.py) and the
+ * OpenCL kernels it launches; the reference file:line is given beside each.
+ *
+ * Conventions
+ *  - All pointers are device pointers unless stated; sizes are element counts.
+ *  - `dtype` selects the arithmetic: CCL_F64 (the plain FP64 drop-in: double
+ *    particles, double/complex128 fields) or CCL_F32 (float particles,
+ *    float/complex64 fields).  Complex arrays are interleaved (re, im).
+ *    "Real coefficient" arrays (filters, PSATD coefficients, 1/dV, damping
+ *    profile) are in the same real type as `dtype`; knot, grid and theta
+ *    arrays of the plasma injector are always double.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    asynchronous on that stream; none synchronises the host.
+ *  - Return value: CCL_OK (0) or an error code; ccl_last_error() gives a
+ *    message.  Arguments are validated before any launch.
+ */
+#ifndef CHIMERACL_GB300_H
+#define CHIMERACL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CCL_OK 0
+#define CCL_ERR_ARG 1         /* invalid argument (null pointer, bad size) */
+#define CCL_ERR_CUDA 2        /* a CUDA launch or runtime call failed */
+#define CCL_ERR_UNSUPPORTED 3 /* a size or mode this build does not handle */
+#define CCL_ERR_WORKSPACE 4   /* workspace smaller than required */
+
+#define CCL_F64 0
+#define CCL_F32 1
+
+/* Library version (major*10000 + minor*100 + patch). */
+int ccl_version(void);
+/* Message of the last error returned on the calling thread. */
+const char *ccl_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Particles  (chimeraCL/methods/particles_methods_cl.py)              */
+/* ------------------------------------------------------------------ */
+
+/* x += px*dt*g_inv (same for y, z) for np particles.
+ * Replaces push_coords -> push_xyz (particles_methods_cl.py:206-223,
+ * kernels/particles_generic.cl:129-153); dt is the species' dt_2 or dt. */
+int ccl_push_x(int dtype, long np, void *x, void *y, void *z, const void *px,
+               const void *py, const void *pz, const void *g_inv, double dt,
+               void *stream);
+
+/* Bytes of device workspace ccl_index_sort needs for np particles on a grid
+ * of ncells = (Nx-1)*(Nr-1) cells. */
+int ccl_index_sort_workspace(long np, long ncells, size_t *bytes);
+
+/* Cell index and cell sort of np particles.
+ * Replaces index_sort (particles_methods_cl.py:225-261): the kernels
+ * index_and_sum_in_cell (particles_generic.cl:88-126) and sort
+ * (particles_generic.cl:186-201) and the cumsum between them.
+ * Outputs, all exact integers:
+ *   indx_in_cell[np]        key = ix + ir*(Nx-1) for 0<ix<Nx-2, 0<=ir<Nr-2,
+ *                           else the overflow key (Nx-1)*(Nr-1);
+ *   sum_in_cell[C+1]        particles per key, C = (Nx-1)*(Nr-1);
+ *   cell_offset[C+2]        exclusive prefix sum, cell_offset[0] = 0;
+ *   sort_indx[np]           particle numbers in key order -- the sort is
+ *                           stable, so within a cell in ascending order;
+ *   np_stay[1] (device)     cell_offset[C], the in-window count.
+ * The host reads nothing; np_stay stays on the device. */
+int ccl_index_sort(int dtype, long np, const void *x, const void *y,
+                   const void *z, int Nx, double xmin, double dx_inv, int Nr,
+                   double rmin, double dr_inv, uint32_t *indx_in_cell,
+                   uint32_t *sum_in_cell, uint32_t *cell_offset,
+                   uint32_t *sort_indx, uint32_t *np_stay, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/* dst[c][i] = src[c][sort_indx[i]] for i < n, c < ncomp (ncomp <= 16).
+ * `src`, `dst` are host arrays of ncomp device pointers.
+ * Replaces align_and_damp -> data_align_dbl (particles_methods_cl.py:263-286,
+ * particles_generic.cl:156-169). */
+int ccl_align(int dtype, long n, int ncomp, void *const *src, void *const *dst,
+              const uint32_t *sort_indx, void *stream);
+
+/* a[i] = i for i < n (the sort_indx reset of align_and_damp,
+ * particles_methods_cl.py:283-285). */
+int ccl_iota_u32(uint32_t *a, long n, void *stream);
+
+/* Fill ncells = (Nx_loc-1)*(Nr_loc-1) cells with Nppc = npx*npr*npth
+ * particles each; w = r.  Replaces make_new_domain -> fill_grid
+ * (particles_methods_cl.py:66-98, particles_generic.cl:33-84). theta, xgrid,
+ * rgrid are double device arrays. */
+int ccl_fill_grid(int dtype, long ncells, void *x, void *y, void *z, void *w,
+                  const double *theta, const double *xgrid,
+                  const double *rgrid, uint32_t Nx_loc, uint32_t npx,
+                  uint32_t npr, uint32_t npth, void *stream);
+
+/* w[i] *= f(x[i]), f piecewise linear on nloc knots xx/ff (double),
+ * dxm1 = 1/(xx[k+1]-xx[k]).  Replaces dens_profile -> profile_by_interpolant
+ * (particles_methods_cl.py:179-204, particles_generic.cl:6-30). */
+int ccl_dens_profile(int dtype, long np, const void *x, void *w,
+                     const double *xx, const double *ff, const double *dxm1,
+                     uint32_t nloc, void *stream);
+
+/* g_inv = 1/sqrt(1 + px^2 + py^2 + pz^2)
+ * (particles_methods_cl.py:141-144, 174-177). */
+int ccl_gamma_inv(int dtype, long np, const void *px, const void *py,
+                  const void *pz, void *g_inv, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Grid  (chimeraCL/methods/grid_methods_cl.py)                        */
+/* ------------------------------------------------------------------ */
+
+/* rho_m += sum over sorted particles of q*w*S(x)S(r) e^{i m phi},
+ * m = 0..M; rho is a host array of M+1 device pointers (m=0 real (Nr,Nx),
+ * m>=1 complex (Nr,Nx)).  Replaces depose_scalar (grid_methods_cl.py:239-264,
+ * grid_deposit_m0.cl:20-129, grid_deposit_m1.cl:20-152). */
+int ccl_deposit_scalar(int dtype, int M, const uint32_t *sort_indx,
+                       const uint32_t *cell_offset, const void *x,
+                       const void *y, const void *z, const void *w, int charge,
+                       int Nx, double xmin, double dx_inv, int Nr, double rmin,
+                       double dr_inv, void *const *rho, void *stream);
+
+/* J_k,m += q*w*g_inv*u_k*S(x)S(r) e^{i m phi}; J is a host array of 3*(M+1)
+ * device pointers ordered m-major then x,y,z.  Replaces depose_vector
+ * (grid_methods_cl.py:266-290, grid_deposit_m0.cl:148-277,
+ * grid_deposit_m1.cl:171-327). */
+int ccl_deposit_vector(int dtype, int M, const uint32_t *sort_indx,
+                       const uint32_t *cell_offset, const void *x,
+                       const void *y, const void *z, const void *ux,
+                       const void *uy, const void *uz, const void *g_inv,
+                       const void *w, int charge, int Nx, double xmin,
+                       double dx_inv, int Nr, double rmin, double dr_inv,
+                       void *const *J, void *stream);
+
+/* Axis treatment (row 1 -= row 0) then multiplication by dV_inv[ir] for
+ * nfld fields of M+1 modes (flds: nfld*(M+1) pointers, field-major).
+ * Replaces postproc_depose_scalar / postproc_depose_vector
+ * (grid_methods_cl.py:293-346, grid_generic.cl:4-59). */
+int ccl_deposit_postproc(int dtype, int M, int nfld, void *const *flds,
+                         int Nx, int Nr, const void *dV_inv, void *stream);
+
+/* Ghost row 0 = +row 1 (m=0) or -row 1 (m>=1) for nfld fields.
+ * Replaces preproc_project_vec (grid_methods_cl.py:348-361,
+ * grid_generic.cl:63-86). */
+int ccl_warp_axis(int dtype, int M, int nfld, void *const *flds, int Nx,
+                  void *stream);
+
+/* Field gather from E, B (flds: 6*(M+1) pointers, m-major then
+ * Ex,Ey,Ez,Bx,By,Bz) and Boris push of u, g_inv, for the np particles of
+ * sort_indx; particles with number >= *np_stay are skipped as in the
+ * reference.  factor_push = 2 pi dt q/m.  Replaces _gather_and_push
+ * (grid_methods_cl.py:363-387, grid_deposit_m0.cl:280-427,
+ * grid_deposit_m1.cl:330-511). */
+int ccl_gather_push(int dtype, int M, long np, const void *x, const void *y,
+                    const void *z, void *px, void *py, void *pz, void *g_inv,
+                    const uint32_t *sort_indx, const uint32_t *np_stay,
+                    double factor_push, int Nx, double xmin, double dx_inv,
+                    int Nr, double rmin, double dr_inv,
+                    const void *const *flds, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Spectral transforms  (chimeraCL/methods/transformer_methods_cl.py)  */
+/* ------------------------------------------------------------------ */
+
+/* phs[ix] = exp(sign * i kx[ix] x0) (kx double).  Replaces get_phase_plus /
+ * get_phase_minus (transformer_generic.cl:28-55). */
+int ccl_phase(int dtype, int nx, void *phs, const double *kx, double x0,
+              int sign, void *stream);
+
+/* Batched longitudinal FFT, forward stage of a transform: row r of `in`
+ * (complex, or real when in_real, leading dimension in_ld elements) is
+ * Fourier transformed along x (unnormalised, e^{-i}), multiplied by phs[ix]
+ * and, if filter != NULL, by filter[r*nx+ix]; written to `out` (complex,
+ * (nrows, nx)).  Replaces the FFT + multiply_by_phase half of
+ * _transform_forward / _half_transform_forward
+ * (transformer_methods_cl.py:290-333, 427-455) and fields_smooth (:79-85).
+ * nx must factor into 2, 3, 5, 7 (nx <= 8192 f32, 4096 f64). */
+int ccl_fft_forward_rows(int dtype, int nrows, int nx, const void *in,
+                         long in_ld, int in_real, void *out, const void *phs,
+                         const void *filter, void *stream);
+
+/* Backward stage: row r of the complex spectral `in` (nrows, nx) is
+ * multiplied by phs[ix], inverse transformed (normalised 1/nx, e^{+i}) and
+ * written to `out` (complex, or its real part when out_real; leading
+ * dimension out_ld).  Replaces the multiply_by_phase + FFT + cast half of
+ * _transform_backward / _half_transform_backward
+ * (transformer_methods_cl.py:334-425). */
+int ccl_fft_backward_rows(int dtype, int nrows, int nx, const void *in,
+                          void *out, long out_ld, int out_real,
+                          const void *phs, void *stream);
+
+/* Absorbing-edge round trip of one spectral field in place: half backward
+ * transform (phase phs_plus, inverse FFT; real part for a real mode) into the
+ * real-space field rows 1..nrows of `rs` ((nrows+1, nx), complex or real per
+ * rs_real), edge profile (x[ix] *= f[ix] for ix < nf, x[ix] *= f[nx-ix] for
+ * ix > nx-nf, also applied to rs row 0), then half forward transform (FFT,
+ * phase phs_minus) back into `spec`.  Replaces damp_fields for one component
+ * (solver.py:32-35, transformer_methods_cl.py:385-455,
+ * solver_methods_cl.py:389-408, solver_ms_pic.cl:5-55). */
+int ccl_damp_rows(int dtype, int nrows, int nx, void *spec, void *rs,
+                  int rs_real, const void *phs_plus, const void *phs_minus,
+                  const void *profile, int nf, void *stream);
+
+/* Discrete Hankel transform / spectral radial derivative as a batched GEMM:
+ * Y[b] = beta*Y[b] + alpha * (A[b] X[b]) for b < batch, A[b] real (m x k,
+ * row-major, lda = k), X[b] (k x ncols) with leading dimension ldx, Y[b]
+ * (m x ncols), leading dimension ldy.  ncols counts real columns; when
+ * cplx != 0 the columns are interleaved (re, im) pairs and alpha is the
+ * complex (alpha_re, alpha_im), else alpha_re alone.  beta is 0 or 1.
+ * A, X, Y are host arrays of `batch` device pointers (batch <= 32).
+ * Replaces _ddot / _cdot (Reikna MatrixMul, transformer_methods_cl.py:458-480)
+ * in the forward/backward transforms, field_grad and field_rot. */
+int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
+                 const void *const *A, const void *const *X, long ldx,
+                 void *const *Y, long ldy, double alpha_re, double alpha_im,
+                 double beta, void *stream);
+
+/* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
+ * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,
+ * dN0_x..z, dN1_x..z; c1 = cos(w dt), c2 = sin(w dt) w, c3 = 1/w^2 (real).
+ * Replaces advance_fields -> advance_e_g_m (solver_methods_cl.py:368-387,
+ * solver_ms_pic.cl:57-143). */
+int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
+                      const void *c2, const void *c3, void *const *flds,
+                      void *stream);
+
+/* out[ir, ix] = (-Re, +Im) of in[ir, (nx-ix) mod nx]: the m=-1 mirror.
+ * Replaces _get_mm1_vec/_scl -> get_m1 (transformer_methods_cl.py:265-288,
+ * transformer_generic.cl:3-24). */
+int ccl_get_m1(int dtype, int nrows, int nx, void *out, const void *in,
+               void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Elementwise  (chimeraCL/methods/generic_methods_cl.py, generic.cl)  */
+/* ------------------------------------------------------------------ */
+
+/* a[i] = val for n elements (complex when cplx: (re, im)).
+ * Replaces set_to (generic_methods_cl.py:96-105). */
+int ccl_set(int dtype, int cplx, long n, void *a, double re, double im,
+            void *stream);
+/* base += add (complex n).  append_c2c, generic.cl:18-29. */
+int ccl_append_c2c(int dtype, long n, void *base, const void *add,
+                   void *stream);
+/* z += a x (complex n).  zpaxz_c2c, generic.cl:32-44. */
+int ccl_zpaxz(int dtype, long n, void *z, double are, double aim,
+              const void *x, void *stream);
+/* z = a x + b y (complex n).  axpbyz_c2c, generic.cl:61-77. */
+int ccl_axpbyz(int dtype, long n, double are, double aim, const void *x,
+               double bre, double bim, const void *y, void *z, void *stream);
+/* z *= x, x real, z complex (n).  mult_elementwise_d2c, generic.cl:47-58. */
+int ccl_mult_elementwise(int dtype, long n, const void *x, void *z,
+                         void *stream);
+/* z[ir,ix] = b[ix] * (a x[ir,ix]) over (nrows, nx), b real.
+ * ab_dot_x, generic.cl:82-99. */
+int ccl_ab_dot_x(int dtype, int nrows, int nx, double are, double aim,
+                 const void *b, const void *x, void *z, void *stream);
+/* out = Re(in) (n).  cast_array_d2c, generic.cl:102-112. */
+int ccl_cast_c2d(int dtype, long n, const void *in, void *out, void *stream);
+/* Edge profile on a (nrows, nx) field, in place.  profile_edges_c/_d,
+ * solver_ms_pic.cl:5-55. */
+int ccl_profile_edges(int dtype, int cplx, int nrows, int nx, void *a,
+                      const void *f, int nf, void *stream);
+/* a *= phs[ix] over complex (nrows, nx).  multiply_by_phase,
+ * transformer_generic.cl:58-80. */
+int ccl_multiply_by_phase(int dtype, int nrows, int nx, void *a,
+                          const void *phs, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHIMERACL_GB300_H */

@@ -1,0 +1,28 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built library")
+
+
+@pytest.fixture(scope="session")
+def cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from chimeracl_gb300 import _lib
+    _lib.load()
+    return torch.device("cuda", 0)
+
+
+@pytest.fixture(scope="session")
+def port():
+    from oracle.kernels import PortKernels
+    return PortKernels()

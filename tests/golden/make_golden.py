@@ -1,0 +1,69 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own
+OpenCL kernels (compiled unchanged as C++ into oracle/_ref) driven by the
+oracle's host restatement of the reference step.
+
+    python -m tests.golden.make_golden        # needs oracle/_ref built
+
+Each case is a small moving-window LPA run (prefilled plasma, immobile ions,
+Gaussian laser, frame shift + injection every `steps` steps) stopped after
+`nsteps` steps; the fixture holds the sort arrays ("key:" entries, exact),
+the real-space and spectral fields and the electron arrays."""
+import copy
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES = {
+    "lpa_m1_64x16.npz": dict(Nx=64, Nr=16, M=1, steps=2, nsteps=3, seed=21),
+    "lpa_m0_64x16.npz": dict(Nx=64, Nr=16, M=0, steps=2, nsteps=3, seed=22),
+}
+
+FIELDS = ("rho", "Jx", "Jz", "Ex", "Ez", "By", "Bz")
+
+
+def case_cfg(case):
+    from tests.lpa_setup import small_lpa
+    return small_lpa(Nx=case["Nx"], Nr=case["Nr"], M=case["M"], steps=case["steps"],
+                     seed=case["seed"], damp=6)
+
+
+def collect(solver, eons):
+    st = {}
+    M = solver.Args["M"] if hasattr(solver, "Args") else 0
+    D = solver.D if hasattr(solver, "D") else solver.DataDev
+    for f in FIELDS:
+        for m in range(M + 1):
+            st[f"{f}_m{m}"] = np.asarray(D[f"{f}_m{m}"])
+            if f != "rho":
+                st[f"{f}_fb_m{m}"] = np.asarray(D[f"{f}_fb_m{m}"])
+    E = eons.D if hasattr(eons, "D") else eons.DataDev
+    for k in ("x", "y", "z", "px", "py", "pz", "g_inv", "w"):
+        st["p:" + k] = np.asarray(E[k])
+    for k in ("indx_in_cell", "sum_in_cell", "cell_offset", "sort_indx"):
+        st["key:" + k] = np.asarray(E[k]).astype(np.uint32)
+    return st
+
+
+def run_case(case, K):
+    from oracle import pic_oracle as po
+    cfg = case_cfg(case)
+    s, e, i, loop = po.build_lpa(copy.deepcopy(cfg["grid_in"]), cfg["eons_in"], cfg["frame_in"],
+                                 cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"])
+    for _ in range(case["nsteps"]):
+        loop.step()
+    return collect(s, e)
+
+
+def main():
+    from oracle.kernels import RefKernels
+    K = RefKernels()
+    for name, case in CASES.items():
+        st = run_case(case, K)
+        np.savez_compressed(os.path.join(HERE, name), **st)
+        print(name, sum(v.nbytes for v in st.values()) // 1024, "KiB raw")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,96 @@
+"""Shared set-up of laser-wakefield (LPA) test cases for the product and the
+oracle: same grid, laser, prefilled plasma window, immobile ions, moving
+window and seeded injector draws on both sides (the way the reference's
+examples/lpa_script_small.py builds its run)."""
+import copy
+
+import numpy as np
+
+
+def small_lpa(Nx=64, Nr=16, M=1, Xmin=-40.0, Xmax=0.0, Rmax=20.0, nppc=(2, 2, 4), dens=1e-3,
+              a0=2.0, R=6.0, Lx=3.0, x0=-10.0, x_foc=None, damp=None, steps=20, seed=3,
+              profiles=None, prefill=True):
+    grid_in = dict(Xmin=Xmin, Xmax=Xmax, Nx=Nx, Rmin=0.0, Rmax=Rmax, Nr=Nr, M=M,
+                   DampCells=damp if damp is not None else max(2, min(50, Nx // 8)))
+    return dict(
+        grid_in=grid_in,
+        eons_in=dict(Nppc=tuple(nppc), dens=dens, charge=-1),
+        frame_in=dict(Velocity=1.0, Steps=steps),
+        laser_in=dict(k0=1.0, a0=a0, x0=x0, Lx=Lx, R=R, x_foc=x0 if x_foc is None else x_foc),
+        prefill=dict(Xmin=Xmin, Xmax=Xmax, Rmin=0.0, Rmax=Rmax) if prefill else None,
+        profiles=profiles, seed=seed)
+
+
+def build_product(cfg, precision="fp64"):
+    from chimeracl_gb300 import Communicator
+    from chimeracl_gb300.frame import Frame
+    from chimeracl_gb300.laser import add_gausian_pulse
+    from chimeracl_gb300.particles import Particles
+    from chimeracl_gb300.pic_loop import PIC_loop
+    from chimeracl_gb300.solver import Solver
+
+    seed = cfg["seed"]
+    comm = Communicator(precision=precision, seed=seed)
+    solver = Solver(copy.deepcopy(cfg["grid_in"]), comm)
+    if cfg["laser_in"] is not None:
+        add_gausian_pulse(solver, dict(cfg["laser_in"]))
+    e_in = copy.deepcopy(cfg["eons_in"])
+    e_in.update(dx=solver.Args["dx"], dr=solver.Args["dr"], dt=solver.Args["dt"])
+    i_in = copy.deepcopy(e_in)
+    i_in["charge"] = 1
+    i_in["Immobile"] = True
+    eons = Particles(e_in, comm, seed=seed)
+    ions = Particles(i_in, comm, seed=seed + 1)
+    ions.Args["InjectorSource"] = eons
+    if cfg["prefill"] is not None:
+        eons.make_new_domain(dict(cfg["prefill"]), density_profiles=cfg["profiles"])
+        eons.add_new_particles()
+        ions.add_new_particles(source=eons)
+        eons.free_added()
+    frames = []
+    if cfg["frame_in"] is not None:
+        f_in = dict(cfg["frame_in"])
+        f_in["dt"] = solver.Args["dt"]
+        f_in["DensityProfiles"] = cfg["profiles"]
+        frames.append(Frame(f_in))
+    loop = PIC_loop([solver], [eons, ions], frames)
+    return solver, eons, ions, loop
+
+
+def build_oracle(cfg, kind="port"):
+    from oracle import pic_oracle as po
+    from oracle.kernels import get_kernels
+
+    K = get_kernels(kind)
+    return po.build_lpa(cfg["grid_in"], cfg["eons_in"], cfg["frame_in"], cfg["laser_in"],
+                        prefill=cfg["prefill"], K=K, seed=cfg["seed"],
+                        density_profiles=cfg["profiles"])
+
+
+def to_np(t):
+    a = t.detach().cpu().numpy()
+    return a
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    scale = np.abs(b).max() if b.size else 0.0
+    d = np.abs(a.astype(np.complex128) - b.astype(np.complex128)).max() if b.size else 0.0
+    if scale == 0.0:
+        return 0.0 if d == 0.0 else np.inf
+    return float(d / scale)
+
+
+def compare_fields(solver, osolver, keys=None, verbose=False):
+    """Worst relative error (max |a-b| / max |b|) over the oracle's field
+    arrays."""
+    worst = 0.0
+    for k in (keys or osolver.D.keys()):
+        if k not in solver.DataDev:
+            continue
+        e = rel_err(to_np(solver.DataDev[k]), osolver.D[k])
+        if verbose and e > 0:
+            print(f"{k:>16s} {e:.3e}")
+        worst = max(worst, e)
+    return worst

