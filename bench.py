@@ -1,0 +1,502 @@
+"""Benchmark: electron particle-steps/s of the quasi-cylindrical PSATD PIC
+step on one GB300, on the mixed-precision single-run workload -- window
+z in [-80, 0], r in [0, 40] (lambda0), Nz=2048, Nr=256, modes m=0,1, 2x1x4
+macro-electrons per cell (about 4.2M) in n_e = 2e-3 n_c with a linear
+up-ramp over the first 20 lambda0, immobile ions, Gaussian laser a0=3,
+w0=10, tau=8 (field FWHM), moving window with injection every 20 steps.
+Synthetic seeded plasma (no dataset exists for this workload).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm times the FP32 step (the headline `value`) and the plain FP64 step
+on the same seed through the public API (Solver / Particles / Frame /
+PIC_loop), reports their ratio and the relative deviation of the FP32 run's
+integrated diagnostics from the FP64 run's, a roofline line for the
+dominant kernel, and a CPU baseline (the oracle on the host cores).  The
+reference arm times the oracle (the reference's step restated on the CPU,
+OpenMP kernels + numpy FFT/GEMM) on all host threads.  N>1 runs independent
+replicas, one per GPU (the step does not shard: every transform couples the
+whole grid), with the time taken as the maximum over ranks.
+"""
+import argparse
+import copy
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+WORKLOAD = "lpa_mixed_single_run_2048x256_m1"
+
+
+def workload(seed=0):
+    """The mixed-precision single-run LPA configuration."""
+    tau = 8.0
+    return dict(
+        grid_in=dict(Xmin=-80.0, Xmax=0.0, Nx=2048, Rmin=0.0, Rmax=40.0, Nr=256, M=1,
+                     DampCells=50),
+        eons_in=dict(Nppc=(2, 1, 4), dens=2e-3, charge=-1),
+        frame_in=dict(Velocity=1.0, Steps=20),
+        laser_in=dict(k0=1.0, a0=3.0, x0=-10.0, Lx=tau / (2 * np.sqrt(np.log(2))), R=10.0,
+                      x_foc=-10.0),
+        prefill=dict(Xmin=-80.0, Xmax=0.0, Rmin=0.0, Rmax=40.0),
+        profiles=[{"coord": "x", "points": [-1e4, -80.0, -60.0, 1e6],
+                   "values": [0.0, 0.0, 1.0, 1.0]}],
+        seed=seed)
+
+
+def config_line(cfg):
+    g = cfg["grid_in"]
+    return {"workload": WORKLOAD, "Nz": g["Nx"], "Nr": g["Nr"], "modes": g["M"] + 1,
+            "ppc": list(cfg["eons_in"]["Nppc"]), "dens": cfg["eons_in"]["dens"],
+            "a0": cfg["laser_in"]["a0"], "w0": cfg["laser_in"]["R"], "tau": 8.0,
+            "window": [g["Xmin"], g["Xmax"], 0.0, g["Rmax"]], "frame_steps": 20,
+            "l2": "working set (particles + fields) larger than L2; no flush",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+def build_run(cfg, precision, device_index=0):
+    """Set the run up through the public API, as the reference's example
+    scripts do (examples/lpa_script_small.py:51-95)."""
+    from chimeracl_gb300 import Communicator
+    from chimeracl_gb300.frame import Frame
+    from chimeracl_gb300.laser import add_gausian_pulse
+    from chimeracl_gb300.particles import Particles
+    from chimeracl_gb300.pic_loop import PIC_loop
+    from chimeracl_gb300.solver import Solver
+
+    comm = Communicator(precision=precision, device=device_index, seed=cfg["seed"])
+    solver = Solver(copy.deepcopy(cfg["grid_in"]), comm)
+    add_gausian_pulse(solver, dict(cfg["laser_in"]))
+    e_in = copy.deepcopy(cfg["eons_in"])
+    e_in.update(dx=solver.Args["dx"], dr=solver.Args["dr"], dt=solver.Args["dt"])
+    i_in = copy.deepcopy(e_in)
+    i_in["charge"] = 1
+    i_in["Immobile"] = True
+    eons = Particles(e_in, comm, seed=cfg["seed"])
+    ions = Particles(i_in, comm, seed=cfg["seed"] + 1)
+    ions.Args["InjectorSource"] = eons
+    eons.make_new_domain(dict(cfg["prefill"]), density_profiles=cfg["profiles"])
+    eons.add_new_particles()
+    ions.add_new_particles(source=eons)
+    eons.free_added()
+    f_in = dict(cfg["frame_in"], dt=solver.Args["dt"], DensityProfiles=cfg["profiles"])
+    loop = PIC_loop([solver], [eons, ions], [Frame(f_in)])
+    return solver, eons, ions, loop
+
+
+def diagnostics_dev(solver, eons):
+    """Integrated diagnostics on the device (float64 reductions): field
+    energy sum_m w_m sum (|E|^2 + |B|^2) 2 pi r dr dx over rows r > 0
+    (w_0 = 1, w_m = 2), on-axis Ez wake amplitude max |Ez_m0[1, ix]| behind
+    the laser (x < x_laser - 2 Lx), kinetic energy sum w (gamma - 1)."""
+    import torch
+    A, D = solver.Args, solver.DataDev
+    r = torch.as_tensor(A["Rgrid"][1:, None], device=D["Ez_m0"].device)
+    vol = 2 * np.pi * r * A["dr"] * A["dx"]
+    We = torch.zeros((), dtype=torch.float64, device=r.device)
+    for m in range(A["M"] + 1):
+        wm = 1.0 if m == 0 else 2.0
+        for f in ("E", "B"):
+            for c in "xyz":
+                a = D[f + c + "_m" + str(m)][1:].to(torch.complex128 if m else torch.float64)
+                We = We + wm * ((a.abs() ** 2) * vol).sum()
+    ez = D["Ez_m0"][1].to(torch.float64).abs()
+    kin = (eons.DataDev["w"].to(torch.float64)
+           * (1.0 / eons.DataDev["g_inv"].to(torch.float64) - 1.0)).sum()
+    return We, ez, kin
+
+
+def wake_amplitude(ez_row, xgrid, x_laser, Lx):
+    sel = xgrid < (x_laser - 2 * Lx)
+    return float(np.abs(ez_row[sel]).max()) if sel.any() else float("nan")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+class Probe:
+    """CUDA-event timing of every launch of selected C-ABI calls, with each
+    call's algorithmic bytes and flops (counted from its arguments)."""
+
+    def __init__(self, names):
+        import torch
+        self.torch = torch
+        self.names = set(names)
+        self.rec = {n: [] for n in names}
+
+    def __call__(self, name, args, fn):
+        if name not in self.names:
+            return fn()
+        t = self.torch
+        a, b = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        a.record()
+        r = fn()
+        b.record()
+        self.rec[name].append((a, b, algorithmic(name, args)))
+        return r
+
+    def summary(self):
+        self.torch.cuda.synchronize()
+        out = {}
+        for n, lst in self.rec.items():
+            if not lst:
+                continue
+            ms = [a.elapsed_time(b) for a, b, _ in lst]
+            byts = sum(x[2][0] for x in lst)
+            flops = sum(x[2][1] for x in lst)
+            out[n] = {"launches": len(lst), "ms_total": sum(ms), "bytes": byts, "flops": flops}
+        return out
+
+
+def algorithmic(name, args):
+    """(bytes, flops) a call must move/compute at minimum."""
+    if name == "ccl_dht_gemm":
+        dtype, batch, m, k, ncols, cplx = args[:6]
+        beta = args[13]
+        b = 8 if dtype == 0 else 4
+        byts = batch * b * (m * k + k * ncols + m * ncols * (2 if beta else 1))
+        return byts, batch * 2.0 * m * k * ncols
+    if name in ("ccl_fft_forward_rows", "ccl_fft_backward_rows", "ccl_damp_rows"):
+        dtype, nrows, nx = args[:3]
+        b = 8 if dtype == 0 else 4
+        passes = 2 if name == "ccl_damp_rows" else 1
+        return nrows * nx * 2 * b * 2 * (1.5 if name == "ccl_damp_rows" else 1), \
+            passes * nrows * 5.0 * nx * np.log2(nx)
+    return 0, 0.0
+
+
+def install_probe(probe):
+    from chimeracl_gb300 import _lib
+    orig = _lib.call
+
+    def call(name, *args):
+        return probe(name, args, lambda: orig(name, *args))
+    _lib.call = call
+    for mod in list(sys.modules.values()):
+        if getattr(mod, "__name__", "").startswith("chimeracl_gb300") and hasattr(mod, "call") \
+                and getattr(mod, "call") is orig:
+            mod.call = call
+    return orig
+
+
+def remove_probe(orig):
+    from chimeracl_gb300 import _lib
+    for mod in list(sys.modules.values()):
+        if getattr(mod, "__name__", "").startswith("chimeracl_gb300") and hasattr(mod, "call"):
+            mod.call = orig
+    _lib.call = orig
+
+
+# ---------------------------------------------------------------------------
+def time_arm(cfg, precision, steps, warmup, device_index, dist):
+    """Warm up, then time exactly `steps` steps (barrier + synchronize on both
+    sides, CUDA events on the step stream)."""
+    import torch
+    from chimeracl_gb300 import _lib
+    solver, eons, ions, loop = build_run(cfg, precision, device_index)
+    for _ in range(warmup):
+        loop.step()
+    torch.cuda.synchronize()
+    np_sum = 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(device_index) as clk:
+        e0.record()
+        for _ in range(steps):
+            np_sum += eons.Args["Np"]
+            loop.step()
+        e1.record()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = _lib.launch_count() - n0
+    return dict(solver=solver, eons=eons, ions=ions, loop=loop, ms=ms, np_sum=np_sum,
+                launches=launches, clocks=clk.summary())
+
+
+def e2e_arm(run, steps):
+    """The same steps through PIC_loop.step() timed on the host clock, with
+    each step's injector draws generated on the host and uploaded (the H2D
+    traffic of make_new_domain at window shifts) and each step's result -- the
+    on-axis Ez line and the integrated diagnostics -- read back to the host."""
+    import torch
+    solver, eons, loop = run["solver"], run["eons"], run["loop"]
+    comm = solver.comm
+    h0, d0 = comm.h2d_bytes, comm.d2h_bytes
+    np_sum = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        np_sum += eons.Args["Np"]
+        loop.step()
+        We, ez, kin = diagnostics_dev(solver, eons)
+        res = torch.cat([ez, We.reshape(1), kin.reshape(1)]).cpu().numpy()
+        comm.d2h_bytes += res.nbytes
+    t = time.perf_counter() - t0
+    return dict(s=t, np_sum=np_sum, h2d=(comm.h2d_bytes - h0) / steps,
+                d2h=(comm.d2h_bytes - d0) / steps)
+
+
+def cpu_oracle_rate(cfg, steps, warmup=1):
+    """The oracle (reference step restated; C kernels with OpenMP over the
+    host cores, numpy FFT and GEMM) on the same workload: electron
+    particle-steps/s over `steps` steps after `warmup`."""
+    from oracle import pic_oracle as po
+    from oracle.kernels import PortKernels
+    K = PortKernels()
+    s, e, i, loop = po.build_lpa(copy.deepcopy(cfg["grid_in"]), cfg["eons_in"], cfg["frame_in"],
+                                 cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"],
+                                 density_profiles=cfg["profiles"])
+    for _ in range(warmup):
+        loop.step()
+    n = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        n += e.Args["Np"]
+        loop.step()
+    t = time.perf_counter() - t0
+    return n / t, K.num_threads(), t
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return dict(FALLBACK_PEAKS), "fallback"
+
+
+def roofline(probe_summary, peaks, src):
+    if not probe_summary:
+        return None
+    name, s = max(probe_summary.items(), key=lambda kv: kv[1]["ms_total"])
+    per_ms = s["ms_total"] / s["launches"]
+    if name == "ccl_dht_gemm":
+        # SIMT GEMM: report against HBM for its operand traffic
+        achieved = s["bytes"] / s["launches"] / (per_ms * 1e-3) / 1e9
+        peak = peaks["hbm_gbs"]
+        return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "launches": s["launches"], "ms_per_launch": round(per_ms, 5),
+                "flops_per_launch": s["flops"] / s["launches"], "peak_source": src}
+    achieved = s["bytes"] / s["launches"] / (per_ms * 1e-3) / 1e9
+    peak = peaks["hbm_gbs"]
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "launches": s["launches"], "ms_per_launch": round(per_ms, 5), "peak_source": src}
+
+
+# ---------------------------------------------------------------------------
+def init_dist(ngpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None, 0, 0, 1
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return dist, rank, local, world
+
+
+def reduce_max(dist, value, device):
+    """Maximum of a float over ranks."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, value, device):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args):
+    dist, rank, local, world = init_dist(args.gpus)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    cfg = workload(seed=1000)
+    rate, cores, t = cpu_oracle_rate(cfg, steps=args.steps, warmup=min(args.warmup, 1))
+    line = {"metric": "electron particle-steps/s", "value": rate, "unit": "particle-steps/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded plasma, laser)",
+            "config": config_line(cfg),
+            "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{args.steps} steps of the workload after "
+                                       f"{min(args.warmup, 1)} warm-up"},
+            "e2e": {"value": rate, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_ours(args):
+    import torch
+    dist, rank, local, world = init_dist(args.gpus)
+    dev = torch.device("cuda", local)
+    cfg = workload(seed=1000 + rank)
+    # FP32 form (headline) and the plain FP64 form on the same seed
+    r32 = time_arm(cfg, "fp32", args.steps, args.warmup, local, dist)
+    e2e = e2e_arm(r32, args.steps)
+    probe = Probe(["ccl_dht_gemm", "ccl_fft_forward_rows", "ccl_fft_backward_rows",
+                   "ccl_damp_rows"])
+    orig = install_probe(probe)
+    for _ in range(min(args.steps, 5)):
+        r32["loop"].step()
+    remove_probe(orig)
+    prof = probe.summary()
+    r64 = time_arm(cfg, "fp64", args.steps, args.warmup, local, dist)
+    # accuracy of the FP32 run vs the FP64 run at the same step
+    n_extra = args.steps + min(args.steps, 5)
+    for _ in range(n_extra - args.steps):
+        r64["loop"].step()
+    for _ in range(args.steps):  # e2e advanced the FP32 run by `steps`
+        r64["loop"].step()
+    torch.cuda.synchronize()
+    acc = {}
+    vals = {}
+    for tag, r in (("fp32", r32), ("fp64", r64)):
+        We, ez, kin = diagnostics_dev(r["solver"], r["eons"])
+        A = r["solver"].Args
+        x_las = cfg["laser_in"]["x0"] + r["loop"].it * A["dt"]
+        vals[tag] = (float(We), wake_amplitude(ez.cpu().numpy(), A["Xgrid"], x_las,
+                                               cfg["laser_in"]["Lx"]), float(kin),
+                     r["loop"].it)
+    if vals["fp32"][3] == vals["fp64"][3]:
+        acc = {"field_energy_rel_err": abs(vals["fp32"][0] / vals["fp64"][0] - 1),
+               "ez_wake_rel_err": abs(vals["fp32"][1] / vals["fp64"][1] - 1),
+               "kinetic_rel_err": abs(vals["fp32"][2] / vals["fp64"][2] - 1),
+               "at_step": vals["fp32"][3]}
+    ms32 = reduce_max(dist, r32["ms"], dev)
+    ms64 = reduce_max(dist, r64["ms"], dev)
+    np32 = reduce_sum(dist, r32["np_sum"], dev)
+    np64 = reduce_sum(dist, r64["np_sum"], dev)
+    e2e_s = reduce_max(dist, e2e["s"], dev)
+    e2e_np = reduce_sum(dist, e2e["np_sum"], dev)
+    value = np32 / (ms32 * 1e-3)
+    v64 = np64 / (ms64 * 1e-3)
+    if rank == 0:
+        peaks, src = load_peaks()
+        line = {
+            "metric": "electron particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded plasma, laser)",
+            "config": config_line(cfg),
+            "fp64": {"value": v64, "ms_per_step": ms64 / args.steps, "dtype": "f64",
+                     "gpu_launches": r64["launches"]},
+            "fp32_over_fp64": value / v64,
+            "fp32_vs_fp64_error": acc,
+            "e2e": {"value": e2e_np / e2e_s, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
+            "gpu_launches": r32["launches"],
+            "clocks": r32["clocks"],
+            "roofline": roofline(prof, peaks, src),
+            "kernel_probe": {k: {"launches": v["launches"], "ms_total": round(v["ms_total"], 4)}
+                             for k, v in prof.items()},
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            rate, cores, t = cpu_oracle_rate(cfg, steps=args.cpu_steps, warmup=1)
+            line["cpu_baseline"] = {"value": rate, "unit": "particle-steps/s", "cores": cores,
+                                    "kind": "port",
+                                    "sample": f"{args.cpu_steps} FP64 steps of the workload "
+                                              "after 1 warm-up step (oracle, OpenMP + numpy)"}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -78,6 +78,7 @@ def load(path=LIB_PATH):
         f.restype = C.c_int
     lib.ccl_version.restype = C.c_int
     lib.ccl_last_error.restype = C.c_char_p
+    lib.ccl_launch_count.restype = C.c_ulonglong
     _lib = lib
     return lib
 
@@ -118,6 +119,11 @@ def PP(tensors):
                 raise ValueError("chimeracl_gb300 expects contiguous CUDA tensors")
             arr[i] = t.data_ptr()
     return C.cast(arr, _pp)
+
+
+def launch_count():
+    """Kernels launched by the library so far (all threads)."""
+    return int(load().ccl_launch_count())
 
 
 def stream():

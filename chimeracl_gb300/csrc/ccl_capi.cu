@@ -3,12 +3,17 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "ccl_common.cuh"
 #include "ccl_launch.h"
 
 namespace ccl {
 
 static thread_local char g_err[512] = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -45,6 +50,8 @@ extern "C" {
 int ccl_version(void) { return 100; }
 
 const char *ccl_last_error(void) { return g_err; }
+
+unsigned long long ccl_launch_count(void) { return g_launches.load(); }
 
 // ---------------------------------------------------------------- particles
 int ccl_push_x(int dtype, long np, void *x, void *y, void *z, const void *px,

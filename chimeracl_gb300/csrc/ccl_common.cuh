@@ -23,6 +23,7 @@ constexpr int kNumSM = 152;
 constexpr int kMaxModes = 4;  // azimuthal modes m = 0..3 (M <= 3)
 
 void set_error(const char *fmt, ...);
+void count_launch();
 
 #define CCL_REQUIRE(cond, code, ...)                                           \
   do {                                                                         \
@@ -34,6 +35,7 @@ void set_error(const char *fmt, ...);
 
 #define CCL_LAUNCH_CHECK(what)                                                 \
   do {                                                                         \
+    ::ccl::count_launch();                                                     \
     cudaError_t e_ = cudaGetLastError();                                       \
     if (e_ != cudaSuccess) {                                                   \
       ::ccl::set_error("%s: %s", what, cudaGetErrorString(e_));                \

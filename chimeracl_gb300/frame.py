@@ -49,4 +49,5 @@ class Frame:
             sp.align_parts()
             nppc = np.int32(np.prod(sp.Args["Nppc"]) + 1)
             x_max = float(sp.DataDev["x"][-nppc:].max().item())
+            sp.comm.d2h_bytes += sp.DataDev["x"].element_size()
             sp.Args["right_lim"] = x_max + 0.5 * sp.Args["ddx"]

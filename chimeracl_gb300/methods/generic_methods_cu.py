@@ -37,10 +37,13 @@ def torch_dtype(dtype):
 class LazyScalar:
     """A device scalar read back only when the host asks for its value."""
 
-    def __init__(self, tensor):
+    def __init__(self, tensor, comm=None):
         self.tensor = tensor
+        self.comm = comm
 
     def resolve(self):
+        if self.comm is not None:
+            self.comm.d2h_bytes += self.tensor.element_size()
         return int(self.tensor.item())
 
 
@@ -91,6 +94,10 @@ class Communicator:
         self.real = torch.float64 if precision == "fp64" else torch.float32
         self.cplx = torch.complex128 if precision == "fp64" else torch.complex64
         self.ccl = CCL_F64 if precision == "fp64" else CCL_F32
+        # host<->device traffic issued by the methods (injector draws,
+        # profile knots, lazy scalar reads), for end-to-end accounting
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
         if verbose:
             print(f"chimeracl_gb300: {self.dev_name} ({precision})")
 
@@ -152,6 +159,7 @@ class GenericMethodsCU:
             a = np.ascontiguousarray(val)
             if a.dtype == np.uint32:
                 a = a.astype(np.int32)
+            self.comm.h2d_bytes += a.nbytes
             return torch.from_numpy(a).to(dev)
         td = torch_dtype(dtype)
         if isinstance(shape, int):

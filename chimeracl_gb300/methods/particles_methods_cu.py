@@ -151,7 +151,7 @@ class ParticleMethodsCU(GenericMethodsCU):
              D["sum_in_cell"].data_ptr(), D["cell_offset"].data_ptr(),
              D["sort_indx"].data_ptr(), D["Np_stay_dev"].data_ptr(), ws.data_ptr(), ws_bytes,
              stream())
-        dict.__setitem__(self.Args, "Np_stay", LazyScalar(D["Np_stay_dev"]))
+        dict.__setitem__(self.Args, "Np_stay", LazyScalar(D["Np_stay_dev"], self.comm))
 
     def align_and_damp(self, comps_align):
         """particles_methods_cl.py:263-286"""
@@ -183,11 +183,16 @@ class ParticleMethodsCU(GenericMethodsCU):
 
     def _fill_arr_randn(self, arr, mu=0, sigma=1):
         v = mu + sigma * self._rng.standard_normal(arr.numel())
-        arr.copy_(torch.from_numpy(v).to(arr.dtype))
+        self._upload(arr, v)
 
     def _fill_arr_rand(self, arr, xmin=0, xmax=1):
         v = xmin + (xmax - xmin) * self._rng.random(arr.numel())
-        arr.copy_(torch.from_numpy(v).to(arr.dtype))
+        self._upload(arr, v)
+
+    def _upload(self, arr, v):
+        h = torch.from_numpy(v).to(arr.dtype)
+        self.comm.h2d_bytes += h.numel() * h.element_size()
+        arr.copy_(h)
 
     def _cumsum(self, arr_in, allocator=None, output_dtype=np.uint32):
         """[0, cumsum(arr_in)...] (particles_methods_cl.py:303-311)."""

@@ -42,6 +42,8 @@ extern "C" {
 int ccl_version(void);
 /* Message of the last error returned on the calling thread. */
 const char *ccl_last_error(void);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long long ccl_launch_count(void);
 
 /* ------------------------------------------------------------------ */
 /* Particles  (chimeraCL/methods/particles_methods_cl.py)              */

@@ -82,14 +82,51 @@ def rel_err(a, b):
     return float(d / scale)
 
 
-def compare_fields(solver, osolver, keys=None, verbose=False):
-    """Worst relative error (max |a-b| / max |b|) over the oracle's field
-    arrays."""
+def field_floor(osolver, key, dens):
+    """Physical magnitude a field array is measured against.
+
+    Several arrays of a quasi-neutral plasma are pure rounding residue at
+    some steps -- rho_m0 while the ions still sit on the electrons, and the
+    fields it drives -- so a ratio to their own maximum compares noise with
+    noise.  They are measured against the scale of the quantity instead:
+    E, B, G against the largest E/B/G value of the same (real or spectral)
+    kind; rho, J against the plasma density (|rho_e| = dens in units of n_c);
+    their spectral images against dens times the transform's gain
+    (Nx * max row sum of the forward Hankel matrices); the gradients dN
+    against that times the largest wavenumber.  The m=-1 buffers hold G's
+    mirror at the end of a step."""
+    A, D = osolver.Args, osolver.D
+    spectral = "_fb" in key
+    base = key.split("_")[0]
+    if (base[0] in "EBG") or base == "buff":
+        grp = [k for k in D if (k[0] in "EBG") and (("_fb" in k) == spectral)]
+        return max(float(np.abs(D[k]).max()) for k in grp)
+    s = dens
+    if spectral:
+        M = A["M"]
+        s *= A["Nx"] * max(float(np.abs(A["DHT_m%d" % m]).sum(1).max()) for m in range(M + 1))
+        if base.startswith("dN"):
+            kmax = max([float(np.abs(A["kx"]).max())] +
+                       [float(A["kr_m%d" % m].max()) for m in range(M + 2)])
+            s *= kmax
+    return s
+
+
+def compare_fields(solver, osolver, keys=None, verbose=False, dens=None):
+    """Worst error over the oracle's field arrays: max |a-b| divided by the
+    larger of max |b| and the array's physical floor (``field_floor``, used
+    when ``dens`` is given; otherwise each array is measured against its own
+    maximum)."""
     worst = 0.0
     for k in (keys or osolver.D.keys()):
         if k not in solver.DataDev:
             continue
-        e = rel_err(to_np(solver.DataDev[k]), osolver.D[k])
+        a, b = to_np(solver.DataDev[k]), osolver.D[k]
+        d = float(np.abs(a.astype(np.complex128) - b.astype(np.complex128)).max()) if b.size else 0
+        scale = float(np.abs(b).max()) if b.size else 0.0
+        if dens is not None:
+            scale = max(scale, field_floor(osolver, k, dens))
+        e = d / scale if scale > 0 else (0.0 if d == 0 else np.inf)
         if verbose and e > 0:
             print(f"{k:>16s} {e:.3e}")
         worst = max(worst, e)

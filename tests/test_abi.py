@@ -13,7 +13,8 @@ HEADER = os.path.join(ROOT, "include", "chimeracl_gb300.h")
 def declared():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(?:int|const char \*)\s*(ccl_\w+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(?:int|const char \*|unsigned long long)\s*(ccl_\w+)\s*\(",
+                                 src)))
 
 
 def test_header_declares_entry_points():
@@ -34,7 +35,8 @@ def test_library_exports_every_declared_symbol():
 
 def test_binding_covers_every_compute_entry_point():
     from chimeracl_gb300 import _lib
-    compute = [n for n in declared() if n not in ("ccl_version", "ccl_last_error")]
+    compute = [n for n in declared()
+               if n not in ("ccl_version", "ccl_last_error", "ccl_launch_count")]
     assert sorted(set(compute) - set(_lib.SIGNATURES)) == []
 
 

@@ -3,7 +3,9 @@ PIC_loop on the CUDA library) against the oracle running the reference's
 step on the same seeded inputs.
 
 Bars (plain FP64 form): sort keys, counts and order identical; fields after
-one step within 1e-12 of each array's largest magnitude; after 25 steps
+one step within 1e-12 of their physical scale (tests.lpa_setup.field_floor:
+arrays that are rounding residue of a neutral plasma are measured against
+the magnitude of the quantity, not against their own noise); after 25 steps
 (one window shift + injection, then a second at step 20) within 1e-10."""
 import numpy as np
 import pytest
@@ -33,7 +35,8 @@ def test_one_step_fp64(cuda, M):
     sol, e, i, loop = build_product(cfg)
     osol, oe, oi, oloop = build_oracle(cfg)
     # identical starting state (the laser's spectral init runs through FFTs)
-    assert compare_fields(sol, osol) < 1e-12
+    dens = cfg["eons_in"]["dens"]
+    assert compare_fields(sol, osol, dens=dens) < 1e-12
     # y, z of the injector come from CUDA's sin/cos vs the host libm: ulps
     _particles_equal(e, oe, tol=1e-15)
     loop.step()
@@ -42,7 +45,7 @@ def test_one_step_fp64(cuda, M):
     _sort_equal(e, oe)
     _sort_equal(i, oi)
     assert e.Args["Np"] == oe.Args["Np"] and e.Args["Np_stay"] == oe.Args["Np_stay"]
-    worst = compare_fields(sol, osol)
+    worst = compare_fields(sol, osol, dens=dens)
     assert worst < 1e-12, worst
     _particles_equal(e, oe, tol=1e-12)
 
@@ -57,7 +60,7 @@ def test_25_steps_fp64_window(cuda):
     torch.cuda.synchronize()
     assert e.Args["Np"] == oe.Args["Np"]
     _sort_equal(e, oe)
-    worst = compare_fields(sol, osol)
+    worst = compare_fields(sol, osol, dens=cfg["eons_in"]["dens"])
     assert worst < 1e-10, worst
     _particles_equal(e, oe, tol=1e-10)
     assert sol.Args["Xmin"] == osol.Args["Xmin"]
@@ -73,5 +76,5 @@ def test_density_profile_injection(cuda):
         oloop.step()
     torch.cuda.synchronize()
     _sort_equal(e, oe)
-    assert compare_fields(sol, osol) < 1e-11
+    assert compare_fields(sol, osol, dens=cfg["eons_in"]["dens"]) < 1e-11
     _particles_equal(e, oe, tol=1e-11)
