@@ -204,19 +204,50 @@ class Probe:
 
 
 def algorithmic(name, args):
-    """(bytes, flops) a call must move/compute at minimum."""
+    """(bytes, flops) a call must move/compute at minimum: every operand read
+    once and every result written once."""
     if name == "ccl_dht_gemm":
         dtype, batch, m, k, ncols, cplx = args[:6]
         beta = args[13]
         b = 8 if dtype == 0 else 4
         byts = batch * b * (m * k + k * ncols + m * ncols * (2 if beta else 1))
         return byts, batch * 2.0 * m * k * ncols
-    if name in ("ccl_fft_forward_rows", "ccl_fft_backward_rows", "ccl_damp_rows"):
-        dtype, nrows, nx = args[:3]
+    if name == "ccl_dht_gemm_batch":
+        dtype, batch, m, k, ncols = args[:5]
+        beta = args[13]
         b = 8 if dtype == 0 else 4
-        passes = 2 if name == "ccl_damp_rows" else 1
-        return nrows * nx * 2 * b * 2 * (1.5 if name == "ccl_damp_rows" else 1), \
-            passes * nrows * 5.0 * nx * np.log2(nx)
+        byts = sum(b * (m * k + k * n + m * n * (2 if beta else 1)) for n in ncols[:batch])
+        return byts, sum(2.0 * m * k * n for n in ncols[:batch])
+    if name in ("ccl_fft_forward_batch", "ccl_fft_backward_batch", "ccl_damp_batch"):
+        dtype, batch, nrows, nx = args[:4]
+        real = args[6] if name == "ccl_fft_forward_batch" else args[7] if \
+            name == "ccl_fft_backward_batch" else args[6]
+        b = 8 if dtype == 0 else 4
+        byts = 0.0
+        for e in range(batch):
+            rsb = b if real[e] else 2 * b  # real-space side real (mode 0) or complex
+            if name == "ccl_damp_batch":  # spectral in + out, real-space row written
+                byts += nrows * nx * (2 * 2 * b + rsb)
+            else:
+                byts += nrows * nx * (2 * b + rsb)
+        passes = 2 if name == "ccl_damp_batch" else 1
+        return byts, batch * passes * nrows * 5.0 * nx * np.log2(nx)
+    if name == "ccl_index_sort":
+        dtype, n, Nx, Nr = args[0], args[1], args[5], args[8]
+        b = 8 if dtype == 0 else 4
+        C = (Nx - 1) * (Nr - 1)
+        # x, y, z read; key and sort index written; counts and offsets written
+        return n * (3 * b + 4 + 4) + (C + 1) * 4 + (C + 2) * 4, 0.0
+    if name == "ccl_gather_push":
+        dtype, M, n, Nx, Nr = args[0], args[1], args[2], args[13], args[16]
+        b = 8 if dtype == 0 else 4
+        # x, y, z, u, g_inv read, u, g_inv written, sort index; E, B read once
+        return n * (7 * b + 4 * b + 4) + 6 * (2 * M + 1) * Nx * Nr * b, 0.0
+    if name == "ccl_psatd_advance":
+        dtype, n = args[0], args[1]
+        b = 8 if dtype == 0 else 4
+        # 15 complex + 3 real read, 6 complex written per spectral cell
+        return n * (15 * 2 + 3 + 6 * 2) * b, 0.0
     return 0, 0.0
 
 
@@ -277,20 +308,21 @@ def e2e_arm(run, steps):
     """The same steps through PIC_loop.step() timed on the host clock, with
     each step's injector draws generated on the host and uploaded (the H2D
     traffic of make_new_domain at window shifts) and each step's result -- the
-    on-axis Ez line and the integrated diagnostics -- read back to the host."""
+    on-axis Ez line, the wake diagnostic -- read back to the host."""
     import torch
     solver, eons, loop = run["solver"], run["eons"], run["loop"]
     comm = solver.comm
+    ez = solver.DataDev["Ez_m0"]
+    ez[1].cpu()  # first use of the copy path outside the timed region
+    torch.cuda.synchronize()
     h0, d0 = comm.h2d_bytes, comm.d2h_bytes
     np_sum = 0
-    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         np_sum += eons.Args["Np"]
         loop.step()
-        We, ez, kin = diagnostics_dev(solver, eons)
-        res = torch.cat([ez, We.reshape(1), kin.reshape(1)]).cpu().numpy()
-        comm.d2h_bytes += res.nbytes
+        line = solver.DataDev["Ez_m0"][1].cpu().numpy()
+        comm.d2h_bytes += line.nbytes
     t = time.perf_counter() - t0
     return dict(s=t, np_sum=np_sum, h2d=(comm.h2d_bytes - h0) / steps,
                 d2h=(comm.d2h_bytes - d0) / steps)
@@ -330,7 +362,7 @@ def roofline(probe_summary, peaks, src):
         return None
     name, s = max(probe_summary.items(), key=lambda kv: kv[1]["ms_total"])
     per_ms = s["ms_total"] / s["launches"]
-    if name == "ccl_dht_gemm":
+    if name in ("ccl_dht_gemm", "ccl_dht_gemm_batch"):
         # SIMT GEMM: report against HBM for its operand traffic
         achieved = s["bytes"] / s["launches"] / (per_ms * 1e-3) / 1e9
         peak = peaks["hbm_gbs"]
@@ -412,9 +444,12 @@ def run_ours(args):
     cfg = workload(seed=1000 + rank)
     # FP32 form (headline) and the plain FP64 form on the same seed
     r32 = time_arm(cfg, "fp32", args.steps, args.warmup, local, dist)
+    diagnostics_dev(r32["solver"], r32["eons"])  # first use of torch's reductions
     e2e = e2e_arm(r32, args.steps)
-    probe = Probe(["ccl_dht_gemm", "ccl_fft_forward_rows", "ccl_fft_backward_rows",
-                   "ccl_damp_rows"])
+    probe = Probe(["ccl_dht_gemm_batch", "ccl_dht_gemm", "ccl_fft_forward_batch",
+                   "ccl_fft_backward_batch", "ccl_damp_batch", "ccl_index_sort",
+                   "ccl_deposit_vector", "ccl_deposit_scalar", "ccl_gather_push",
+                   "ccl_psatd_advance"])
     orig = install_probe(probe)
     for _ in range(min(args.steps, 5)):
         r32["loop"].step()
@@ -485,7 +520,7 @@ def run_ours(args):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)

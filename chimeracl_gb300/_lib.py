@@ -45,6 +45,10 @@ SIGNATURES = {
     "ccl_fft_backward_rows": [_i, _i, _i, _vp, _vp, _l, _i, _vp, _vp],
     "ccl_damp_rows": [_i, _i, _i, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp],
     "ccl_dht_gemm": [_i, _i, _i, _i, _i, _i, _pp, _pp, _l, _pp, _l, _d, _d, _d, _vp],
+    "ccl_fft_forward_batch": [_i, _i, _i, _i, _pp, _vp, _vp, _pp, _vp, _pp, _vp],
+    "ccl_fft_backward_batch": [_i, _i, _i, _i, _pp, _pp, _vp, _vp, _vp, _vp],
+    "ccl_damp_batch": [_i, _i, _i, _i, _pp, _pp, _vp, _vp, _vp, _vp, _i, _vp],
+    "ccl_dht_gemm_batch": [_i, _i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],
     "ccl_psatd_advance": [_i, _l, _d, _vp, _vp, _vp, _pp, _vp],
     "ccl_get_m1": [_i, _i, _i, _vp, _vp, _vp],
     "ccl_set": [_i, _i, _l, _vp, _d, _d, _vp],
@@ -119,6 +123,16 @@ def PP(tensors):
                 raise ValueError("chimeracl_gb300 expects contiguous CUDA tensors")
             arr[i] = t.data_ptr()
     return C.cast(arr, _pp)
+
+
+def longs(vals):
+    """Host array of C longs."""
+    return (C.c_long * len(vals))(*vals)
+
+
+def ints(vals):
+    """Host array of C ints."""
+    return (C.c_int * len(vals))(*vals)
 
 
 def launch_count():

@@ -282,6 +282,61 @@ int ccl_damp_rows(int dtype, int nrows, int nx, void *spec, void *rs,
                           (const float *)profile, nf, S(stream));
 }
 
+int ccl_fft_forward_batch(int dtype, int batch, int nrows, int nx,
+                          const void *const *in, const long *in_ld,
+                          const int *in_real, void *const *out,
+                          const void *phs, const void *const *filter,
+                          void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNULL(in); NONNULL(in_ld); NONNULL(in_real); NONNULL(out); NONNULL(phs);
+  if (dtype == CCL_F64)
+    return fft_forward_batch<double>(batch, nrows, nx, in, in_ld, in_real, out,
+                                     phs, filter, S(stream));
+  return fft_forward_batch<float>(batch, nrows, nx, in, in_ld, in_real, out,
+                                  phs, filter, S(stream));
+}
+
+int ccl_fft_backward_batch(int dtype, int batch, int nrows, int nx,
+                           const void *const *in, void *const *out,
+                           const long *out_ld, const int *out_real,
+                           const void *phs, void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNULL(in); NONNULL(out); NONNULL(out_ld); NONNULL(out_real); NONNULL(phs);
+  if (dtype == CCL_F64)
+    return fft_backward_batch<double>(batch, nrows, nx, in, out, out_ld,
+                                      out_real, phs, S(stream));
+  return fft_backward_batch<float>(batch, nrows, nx, in, out, out_ld, out_real,
+                                   phs, S(stream));
+}
+
+int ccl_damp_batch(int dtype, int batch, int nrows, int nx, void *const *spec,
+                   void *const *rs, const int *rs_real, const void *phs_plus,
+                   const void *phs_minus, const void *profile, int nf,
+                   void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNULL(spec); NONNULL(rs); NONNULL(rs_real); NONNULL(phs_plus);
+  NONNULL(phs_minus); NONNULL(profile);
+  if (dtype == CCL_F64)
+    return damp_batch<double>(batch, nrows, nx, spec, rs, rs_real, phs_plus,
+                              phs_minus, profile, nf, S(stream));
+  return damp_batch<float>(batch, nrows, nx, spec, rs, rs_real, phs_plus,
+                           phs_minus, profile, nf, S(stream));
+}
+
+int ccl_dht_gemm_batch(int dtype, int batch, int m, int k, const int *ncols,
+                       int cplx, const void *const *A, const void *const *X,
+                       const long *ldx, void *const *Y, const long *ldy,
+                       double alpha_re, double alpha_im, double beta,
+                       void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNULL(ncols); NONNULL(A); NONNULL(X); NONNULL(ldx); NONNULL(Y); NONNULL(ldy);
+  if (dtype == CCL_F64)
+    return dht_gemm_batch<double>(batch, m, k, ncols, cplx, A, X, ldx, Y, ldy,
+                                  alpha_re, alpha_im, beta, S(stream));
+  return dht_gemm_batch<float>(batch, m, k, ncols, cplx, A, X, ldx, Y, ldy,
+                               alpha_re, alpha_im, beta, S(stream));
+}
+
 int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
                  const void *const *A, const void *const *X, long ldx,
                  void *const *Y, long ldy, double alpha_re, double alpha_im,

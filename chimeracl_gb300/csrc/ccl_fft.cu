@@ -176,32 +176,49 @@ __device__ cplx<T> *fft_row(cplx<T> *sA, cplx<T> *sB, const FftPlan &pl,
   return src;
 }
 
-// Forward stage: in -> FFT -> * phs (* filter) -> out
-template <typename T, bool IN_REAL, bool FILT>
+constexpr int FFT_MAXBATCH = 32;
+
+// Per-entry operands of a batched row transform (blockIdx.y = entry).
+struct FftBatch {
+  const void *in[FFT_MAXBATCH];
+  void *out[FFT_MAXBATCH];
+  const void *filt[FFT_MAXBATCH];
+  long ld[FFT_MAXBATCH];   // leading dimension of the real-space side
+  int real[FFT_MAXBATCH];  // real-space side is real (mode 0)
+};
+
+template <typename T>
+__device__ __forceinline__ cplx<T> mul_phs(cplx<T> v, cplx<T> p) {
+  cplx<T> r = {(v.re * p.re - v.im * p.im), (v.re * p.im + v.im * p.re)};
+  return r;
+}
+
+// Forward stage: in -> FFT -> * phs (* filter) -> out (complex (nrows, N))
+template <typename T>
 __global__ void __launch_bounds__(FFT_THREADS)
-    k_fft_fwd(FftPlan pl, const T *__restrict__ in, long in_ld,
-              T *__restrict__ out, const T *__restrict__ phs,
-              const T *__restrict__ filt, const cplx<T> *__restrict__ tw) {
+    k_fft_fwd(FftPlan pl, FftBatch b, const T *__restrict__ phs,
+              const cplx<T> *__restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
-  const int N = pl.n;
+  const int N = pl.n, e = blockIdx.y;
   const long row = blockIdx.x;
-  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> v;
-    if (IN_REAL) {
-      v.re = in[row * in_ld + ix];
-      v.im = T(0);
-    } else {
-      v = ld_c(in, row * in_ld + ix);
+  const long ld = b.ld[e];
+  const T *in = (const T *)b.in[e];
+  if (b.real[e]) {
+    for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+      cplx<T> v = {in[row * ld + ix], T(0)};
+      sA[ix] = v;
     }
-    sA[ix] = v;
+  } else {
+    for (int ix = threadIdx.x; ix < N; ix += blockDim.x) sA[ix] = ld_c(in, row * ld + ix);
   }
   __syncthreads();
   cplx<T> *res = fft_row<T, false>(sA, sB, pl, tw);
+  T *out = (T *)b.out[e];
+  const T *filt = (const T *)b.filt[e];
   for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> v = res[ix], p = ld_c(phs, ix);
-    cplx<T> r = {(v.re * p.re - v.im * p.im), (v.re * p.im + v.im * p.re)};
-    if (FILT) {
+    cplx<T> r = mul_phs(res[ix], ld_c(phs, ix));
+    if (filt) {
       T f = filt[row * N + ix];
       r.re = f * r.re;
       r.im = f * r.im;
@@ -211,50 +228,49 @@ __global__ void __launch_bounds__(FFT_THREADS)
 }
 
 // Backward stage: in * phs -> inverse FFT / N -> out (complex or real part)
-template <typename T, bool OUT_REAL>
+template <typename T>
 __global__ void __launch_bounds__(FFT_THREADS)
-    k_fft_bwd(FftPlan pl, const T *__restrict__ in, T *__restrict__ out,
-              long out_ld, const T *__restrict__ phs,
+    k_fft_bwd(FftPlan pl, FftBatch b, const T *__restrict__ phs,
               const cplx<T> *__restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
-  const int N = pl.n;
+  const int N = pl.n, e = blockIdx.y;
   const long row = blockIdx.x;
-  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> a = ld_c(in, row * N + ix), p = ld_c(phs, ix);
-    cplx<T> v = {(a.re * p.re - a.im * p.im), (a.re * p.im + a.im * p.re)};
-    sA[ix] = v;
-  }
+  const T *in = (const T *)b.in[e];
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x)
+    sA[ix] = mul_phs(ld_c(in, row * N + ix), ld_c(phs, ix));
   __syncthreads();
   cplx<T> *res = fft_row<T, true>(sA, sB, pl, tw);
   const T inv_n = (T)(1.0 / (double)N);
-  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> v = res[ix];
-    if (OUT_REAL) {
-      out[row * out_ld + ix] = v.re * inv_n;
-    } else {
-      cplx<T> r = {v.re * inv_n, v.im * inv_n};
-      st_c(out, row * out_ld + ix, r);
+  T *out = (T *)b.out[e];
+  const long ld = b.ld[e];
+  if (b.real[e]) {
+    for (int ix = threadIdx.x; ix < N; ix += blockDim.x) out[row * ld + ix] = res[ix].re * inv_n;
+  } else {
+    for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
+      cplx<T> r = {res[ix].re * inv_n, res[ix].im * inv_n};
+      st_c(out, row * ld + ix, r);
     }
   }
 }
 
-// Absorbing-edge round trip of one spectral component, in place.
-template <typename T, bool RS_REAL>
+// Absorbing-edge round trip, in place: b.in = b.out = spectral field,
+// b.filt = real-space field (nrows+1, N), b.real = mode 0.
+template <typename T>
 __global__ void __launch_bounds__(FFT_THREADS)
-    k_damp(FftPlan pl, T *__restrict__ spec, T *__restrict__ rs,
-           const T *__restrict__ phs_p, const T *__restrict__ phs_m,
-           const T *__restrict__ prof, u32 nf, const cplx<T> *__restrict__ tw) {
+    k_damp(FftPlan pl, FftBatch b, const T *__restrict__ phs_p,
+           const T *__restrict__ phs_m, const T *__restrict__ prof, u32 nf,
+           const cplx<T> *__restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T> *sA = (cplx<T> *)smraw, *sB = sA + pl.n;
-  const int N = pl.n;
+  const int N = pl.n, e = blockIdx.y;
   const u32 un = (u32)N;
   const long row = blockIdx.x;
-  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> a = ld_c(spec, row * N + ix), p = ld_c(phs_p, ix);
-    cplx<T> v = {(a.re * p.re - a.im * p.im), (a.re * p.im + a.im * p.re)};
-    sA[ix] = v;
-  }
+  T *spec = (T *)b.out[e];
+  T *rs = (T *)b.filt[e];
+  const bool rs_real = b.real[e] != 0;
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x)
+    sA[ix] = mul_phs(ld_c(spec, row * N + ix), ld_c(phs_p, ix));
   __syncthreads();
   cplx<T> *res = fft_row<T, true>(sA, sB, pl, tw);
   cplx<T> *other = (res == sA) ? sB : sA;
@@ -262,15 +278,15 @@ __global__ void __launch_bounds__(FFT_THREADS)
   for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
     cplx<T> v = res[ix];
     v.re = v.re * inv_n;
-    v.im = RS_REAL ? T(0) : v.im * inv_n;
+    v.im = rs_real ? T(0) : v.im * inv_n;
     const u32 ux = (u32)ix;
     if (ux < nf) { v.re *= prof[ux]; v.im *= prof[ux]; }
     if (ux > un - nf) { v.re *= prof[un - ux]; v.im *= prof[un - ux]; }
-    if (RS_REAL) rs[(row + 1) * N + ix] = v.re;
+    if (rs_real) rs[(row + 1) * N + ix] = v.re;
     else st_c(rs, (row + 1) * N + ix, v);
     other[ix] = v;
     if (row == 0) {  // the ghost row is damped in place as well
-      if (RS_REAL) {
+      if (rs_real) {
         T g = rs[ix];
         if (ux < nf) g *= prof[ux];
         if (ux > un - nf) g *= prof[un - ux];
@@ -284,13 +300,10 @@ __global__ void __launch_bounds__(FFT_THREADS)
     }
   }
   __syncthreads();
-  cplx<T> *in2 = other, *tmp2 = (other == sA) ? sB : sA;
-  cplx<T> *res2 = fft_row<T, false>(in2, tmp2, pl, tw);
-  for (int ix = threadIdx.x; ix < N; ix += blockDim.x) {
-    cplx<T> v = res2[ix], p = ld_c(phs_m, ix);
-    cplx<T> r = {(v.re * p.re - v.im * p.im), (v.re * p.im + v.im * p.re)};
-    st_c(spec, row * N + ix, r);
-  }
+  cplx<T> *tmp2 = (other == sA) ? sB : sA;
+  cplx<T> *res2 = fft_row<T, false>(other, tmp2, pl, tw);
+  for (int ix = threadIdx.x; ix < N; ix += blockDim.x)
+    st_c(spec, row * N + ix, mul_phs(res2[ix], ld_c(phs_m, ix)));
 }
 
 // ---------------------------------------------------------------------
@@ -338,80 +351,132 @@ template <typename K> static void allow_smem(K kernel, size_t smem) {
                          (int)smem);
 }
 
+static int batch_check(int batch, int nrows) {
+  CCL_REQUIRE(batch >= 0 && batch <= FFT_MAXBATCH, CCL_ERR_ARG,
+              "fft: batch %d outside [0, %d]", batch, FFT_MAXBATCH);
+  CCL_REQUIRE(nrows >= 0 && nrows <= 65535 * 32, CCL_ERR_ARG, "fft: nrows %d",
+              nrows);
+  return CCL_OK;
+}
+
 template <typename T>
-int fft_forward_rows(int nrows, int nx, const T *in, long in_ld, int in_real,
-                     T *out, const T *phs, const T *filt, cudaStream_t s) {
+int fft_forward_batch(int batch, int nrows, int nx, const void *const *in,
+                      const long *in_ld, const int *in_real, void *const *out,
+                      const void *phs, const void *const *filt,
+                      cudaStream_t s) {
   FftPlan pl;
   size_t smem;
   int rc = fft_check<T>(nx, &pl, &smem);
   if (rc) return rc;
-  if (nrows == 0) return CCL_OK;
+  if ((rc = batch_check(batch, nrows))) return rc;
+  if (nrows == 0 || batch == 0) return CCL_OK;
+  FftBatch b;
+  for (int i = 0; i < batch; i++) {
+    CCL_REQUIRE(in[i] && out[i], CCL_ERR_ARG, "fft: null operand %d", i);
+    CCL_REQUIRE(in_ld[i] >= nx, CCL_ERR_ARG, "fft: entry %d ld %ld < nx", i,
+                in_ld[i]);
+    b.in[i] = in[i];
+    b.out[i] = out[i];
+    b.filt[i] = filt ? filt[i] : nullptr;
+    b.ld[i] = in_ld[i];
+    b.real[i] = in_real[i];
+  }
   const cplx<T> *tw = twiddles<T>(nx, s);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-#define CCL_FWD(R, F)                                                          \
-  {                                                                            \
-    auto kern = k_fft_fwd<T, R, F>;                                            \
-    allow_smem(kern, smem);                                                    \
-    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, in_ld, out, phs, filt, tw);  \
-  }
-  if (in_real) {
-    if (filt) CCL_FWD(true, true) else CCL_FWD(true, false)
-  } else {
-    if (filt) CCL_FWD(false, true) else CCL_FWD(false, false)
-  }
-#undef CCL_FWD
-  CCL_LAUNCH_CHECK("fft_forward_rows");
+  auto kern = k_fft_fwd<T>;
+  allow_smem(kern, smem);
+  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  CCL_LAUNCH_CHECK("fft_forward");
   return CCL_OK;
+}
+
+template <typename T>
+int fft_backward_batch(int batch, int nrows, int nx, const void *const *in,
+                       void *const *out, const long *out_ld,
+                       const int *out_real, const void *phs, cudaStream_t s) {
+  FftPlan pl;
+  size_t smem;
+  int rc = fft_check<T>(nx, &pl, &smem);
+  if (rc) return rc;
+  if ((rc = batch_check(batch, nrows))) return rc;
+  if (nrows == 0 || batch == 0) return CCL_OK;
+  FftBatch b;
+  for (int i = 0; i < batch; i++) {
+    CCL_REQUIRE(in[i] && out[i], CCL_ERR_ARG, "fft: null operand %d", i);
+    CCL_REQUIRE(out_ld[i] >= nx, CCL_ERR_ARG, "fft: entry %d ld %ld < nx", i,
+                out_ld[i]);
+    b.in[i] = in[i];
+    b.out[i] = out[i];
+    b.filt[i] = nullptr;
+    b.ld[i] = out_ld[i];
+    b.real[i] = out_real[i];
+  }
+  const cplx<T> *tw = twiddles<T>(nx, s);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  auto kern = k_fft_bwd<T>;
+  allow_smem(kern, smem);
+  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  CCL_LAUNCH_CHECK("fft_backward");
+  return CCL_OK;
+}
+
+template <typename T>
+int damp_batch(int batch, int nrows, int nx, void *const *spec,
+               void *const *rs, const int *rs_real, const void *phs_p,
+               const void *phs_m, const void *prof, int nf, cudaStream_t s) {
+  FftPlan pl;
+  size_t smem;
+  int rc = fft_check<T>(nx, &pl, &smem);
+  if (rc) return rc;
+  if ((rc = batch_check(batch, nrows))) return rc;
+  CCL_REQUIRE(nf >= 0, CCL_ERR_ARG, "damp: nf=%d", nf);
+  if (nrows == 0 || batch == 0) return CCL_OK;
+  FftBatch b;
+  for (int i = 0; i < batch; i++) {
+    CCL_REQUIRE(spec[i] && rs[i], CCL_ERR_ARG, "damp: null operand %d", i);
+    b.in[i] = spec[i];
+    b.out[i] = spec[i];
+    b.filt[i] = rs[i];
+    b.ld[i] = nx;
+    b.real[i] = rs_real[i];
+  }
+  const cplx<T> *tw = twiddles<T>(nx, s);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  auto kern = k_damp<T>;
+  allow_smem(kern, smem);
+  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(
+      pl, b, (const T *)phs_p, (const T *)phs_m, (const T *)prof, (u32)nf, tw);
+  CCL_LAUNCH_CHECK("damp");
+  return CCL_OK;
+}
+
+template <typename T>
+int fft_forward_rows(int nrows, int nx, const T *in, long in_ld, int in_real,
+                     T *out, const T *phs, const T *filt, cudaStream_t s) {
+  const void *i[1] = {in};
+  void *o[1] = {out};
+  const void *f[1] = {filt};
+  long ld[1] = {in_ld};
+  int r[1] = {in_real};
+  return fft_forward_batch<T>(1, nrows, nx, i, ld, r, o, phs, f, s);
 }
 
 template <typename T>
 int fft_backward_rows(int nrows, int nx, const T *in, T *out, long out_ld,
                       int out_real, const T *phs, cudaStream_t s) {
-  FftPlan pl;
-  size_t smem;
-  int rc = fft_check<T>(nx, &pl, &smem);
-  if (rc) return rc;
-  if (nrows == 0) return CCL_OK;
-  const cplx<T> *tw = twiddles<T>(nx, s);
-  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-  if (out_real) {
-    auto kern = k_fft_bwd<T, true>;
-    allow_smem(kern, smem);
-    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, out, out_ld, phs, tw);
-  } else {
-    auto kern = k_fft_bwd<T, false>;
-    allow_smem(kern, smem);
-    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, in, out, out_ld, phs, tw);
-  }
-  CCL_LAUNCH_CHECK("fft_backward_rows");
-  return CCL_OK;
+  const void *i[1] = {in};
+  void *o[1] = {out};
+  long ld[1] = {out_ld};
+  int r[1] = {out_real};
+  return fft_backward_batch<T>(1, nrows, nx, i, o, ld, r, phs, s);
 }
 
 template <typename T>
-int damp_rows(int nrows, int nx, T *spec, T *rs, int rs_real,
-              const T *phs_p, const T *phs_m, const T *prof, int nf,
-              cudaStream_t s) {
-  FftPlan pl;
-  size_t smem;
-  int rc = fft_check<T>(nx, &pl, &smem);
-  if (rc) return rc;
-  CCL_REQUIRE(nf >= 0, CCL_ERR_ARG, "damp: nf=%d", nf);
-  if (nrows == 0) return CCL_OK;
-  const cplx<T> *tw = twiddles<T>(nx, s);
-  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-  if (rs_real) {
-    auto kern = k_damp<T, true>;
-    allow_smem(kern, smem);
-    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, spec, rs, phs_p, phs_m, prof,
-                                          (u32)nf, tw);
-  } else {
-    auto kern = k_damp<T, false>;
-    allow_smem(kern, smem);
-    kern<<<nrows, FFT_THREADS, smem, s>>>(pl, spec, rs, phs_p, phs_m, prof,
-                                          (u32)nf, tw);
-  }
-  CCL_LAUNCH_CHECK("damp_rows");
-  return CCL_OK;
+int damp_rows(int nrows, int nx, T *spec, T *rs, int rs_real, const T *phs_p,
+              const T *phs_m, const T *prof, int nf, cudaStream_t s) {
+  void *sp[1] = {spec}, *r[1] = {rs};
+  int re[1] = {rs_real};
+  return damp_batch<T>(1, nrows, nx, sp, r, re, phs_p, phs_m, prof, nf, s);
 }
 
 #define CCL_INST_FFT(T)                                                        \
@@ -420,7 +485,17 @@ int damp_rows(int nrows, int nx, T *spec, T *rs, int rs_real,
   template int fft_backward_rows<T>(int, int, const T *, T *, long, int,      \
                                     const T *, cudaStream_t);                  \
   template int damp_rows<T>(int, int, T *, T *, int, const T *, const T *,    \
-                            const T *, int, cudaStream_t);
+                            const T *, int, cudaStream_t);                     \
+  template int fft_forward_batch<T>(int, int, int, const void *const *,       \
+                                    const long *, const int *, void *const *, \
+                                    const void *, const void *const *,        \
+                                    cudaStream_t);                             \
+  template int fft_backward_batch<T>(int, int, int, const void *const *,      \
+                                     void *const *, const long *, const int *,\
+                                     const void *, cudaStream_t);              \
+  template int damp_batch<T>(int, int, int, void *const *, void *const *,     \
+                             const int *, const void *, const void *,         \
+                             const void *, int, cudaStream_t);
 CCL_INST_FFT(double)
 CCL_INST_FFT(float)
 

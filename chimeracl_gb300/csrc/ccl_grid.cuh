@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(256)
     const T rp = sqrt(yp * yp + zp * zp);
     const T xmin = (T)g.xmin, dx_inv = (T)g.dx_inv, rmin = (T)g.rmin,
             dr_inv = (T)g.dr_inv;
-    const int ix = floor_to_int((double)floor((xp - xmin) * dx_inv), -1);
-    const int ir = floor_to_int((double)floor((rp - rmin) * dr_inv), 1 << 30);
+    const int ix = floor_to_int<T>(floor((xp - xmin) * dx_inv), -1);
+    const int ir = floor_to_int<T>(floor((rp - rmin) * dr_inv), 1 << 30);
     if (!(ix > 0 && ix < nxc - 1 && ir < nrc - 1)) continue;
     const long ig = (long)ix + (long)ir * Nx;
     T u[3] = {px[p], py[p], pz[p]};

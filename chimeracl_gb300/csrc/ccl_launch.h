@@ -22,8 +22,25 @@ int fft_backward_rows(int nrows, int nx, const T *in, T *out, long out_ld,
 template <typename T>
 int damp_rows(int nrows, int nx, T *spec, T *rs, int rs_real, const T *phs_p,
               const T *phs_m, const T *prof, int nf, cudaStream_t s);
+template <typename T>
+int fft_forward_batch(int batch, int nrows, int nx, const void *const *in,
+                      const long *in_ld, const int *in_real, void *const *out,
+                      const void *phs, const void *const *filt, cudaStream_t s);
+template <typename T>
+int fft_backward_batch(int batch, int nrows, int nx, const void *const *in,
+                       void *const *out, const long *out_ld,
+                       const int *out_real, const void *phs, cudaStream_t s);
+template <typename T>
+int damp_batch(int batch, int nrows, int nx, void *const *spec,
+               void *const *rs, const int *rs_real, const void *phs_p,
+               const void *phs_m, const void *prof, int nf, cudaStream_t s);
 
 // ccl_dht.cu
+template <typename T>
+int dht_gemm_batch(int batch, int m, int k, const int *ncols, int cplx,
+                   const void *const *A, const void *const *X, const long *ldx,
+                   void *const *Y, const long *ldy, double are, double aim,
+                   double beta, cudaStream_t s);
 template <typename T>
 int dht_gemm(int batch, int m, int k, int ncols, int cplx, const void *const *A,
              const void *const *X, long ldx, void *const *Y, long ldy,

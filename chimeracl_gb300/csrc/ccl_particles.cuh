@@ -42,18 +42,23 @@ struct KeyGrid {
   double xmin, dx_inv, rmin, dr_inv;
 };
 
-__device__ __forceinline__ int floor_to_int(double f, int bad) {
-  // (int) of an out-of-range or NaN double: such particles are outside the
-  // window; give them an index that fails the window test.
-  return (f > -2147483648.0 && f < 2147483647.0) ? (int)f : bad;
+template <typename T>
+__device__ __forceinline__ int floor_to_int(T f, int bad) {
+  // (int) of an out-of-range or NaN value: such particles are outside the
+  // window; give them an index that fails the window test.  (For float the
+  // upper bound rounds to 2^31, still a valid strict bound.)
+  return (f > T(-2147483648.0) && f < T(2147483647.0)) ? (int)f : bad;
 }
 
-__device__ __forceinline__ u32 cell_key(double xp, double yp, double zp,
-                                        const KeyGrid &g) {
+// In the particles' own precision: the FP32 form must not touch the FP64
+// pipe (a few FP64 instructions per particle cost more than the whole
+// kernel's memory traffic on this part).
+template <typename T>
+__device__ __forceinline__ u32 cell_key(T xp, T yp, T zp, const KeyGrid &g) {
   int nxc = g.Nx - 1, nrc = g.Nr - 1;
-  double r = sqrt(yp * yp + zp * zp);
-  int ix = floor_to_int(floor((xp - g.xmin) * g.dx_inv), -1);
-  int ir = floor_to_int(floor((r - g.rmin) * g.dr_inv), -1);
+  T r = sqrt(yp * yp + zp * zp);
+  int ix = floor_to_int<T>(floor((xp - (T)g.xmin) * (T)g.dx_inv), -1);
+  int ir = floor_to_int<T>(floor((r - (T)g.rmin) * (T)g.dr_inv), -1);
   if (ix > 0 && ix < nxc - 1 && ir < nrc - 1 && ir >= 0)
     return (u32)(ix + ir * nxc);
   return (u32)(nrc * nxc);
@@ -74,7 +79,7 @@ __global__ void k_keys(long np, const T *__restrict__ x,
     bool valid = i < np;
     u32 k = 0xffffffffu;
     if (valid) {
-      k = cell_key((double)x[i], (double)y[i], (double)z[i], g);
+      k = cell_key<T>(x[i], y[i], z[i], g);
       keys[i] = k;
     }
     unsigned peers = __match_any_sync(0xffffffffu, k);

@@ -8,8 +8,10 @@ applied inside the FFT kernel; the half transforms are the FFT kernel alone.
 """
 import torch
 
-from .._lib import PP, P, call, stream
+from .._lib import PP, P, call, ints, longs, stream
 from .generic_methods_cu import GenericMethodsCU
+
+MAX_BATCH = 32
 
 
 class TransformerMethodsCU(GenericMethodsCU):
@@ -111,6 +113,61 @@ class TransformerMethodsCU(GenericMethodsCU):
                 else:
                     call("ccl_fft_backward_rows", self._dt, nrows, Nx, sp.data_ptr(), P(rs, Nx),
                          Nx, int(m == 0), phs.data_ptr(), stream())
+
+    def _work(self, i, cplx):
+        """Per-entry work buffer (Nr-1, Nx) of a batched transform."""
+        key = ("_wc%d" if cplx else "_wr%d") % i
+        buf = self.DataDev.get(key)
+        if buf is None:
+            shape = (self.Args["Nr"] - 1, self.Args["Nx"])
+            buf = torch.empty(shape, dtype=self.comm.cplx if cplx else self.comm.real,
+                              device=self.comm.device)
+            self.DataDev[key] = buf
+        return buf
+
+    def transform_fields(self, names, dir, mode, filt=None):
+        """Full or half transforms of several fields at once: every
+        (field, mode) pair of a direction shares one Hankel GEMM launch and
+        one FFT launch (the same arithmetic as transform_field per pair)."""
+        A = self.Args
+        M, Nx, Nr = A["M"], A["Nx"], A["Nr"]
+        nrows = Nr - 1
+        ent = [(n, m) for n in names for m in range(M + 1)]
+        for k in range(0, len(ent), MAX_BATCH):
+            self._transform_batch(ent[k:k + MAX_BATCH], dir, mode, filt, M, Nx, nrows)
+
+    def _transform_batch(self, ent, dir, mode, filt, M, Nx, nrows):
+        D = self.DataDev
+        phs = self._phase(dir)
+        rs = [D[n + "_m" + str(m)] for n, m in ent]
+        sp = [D[n + "_fb_m" + str(m)] for n, m in ent]
+        real = [int(m == 0) for _, m in ent]
+        ncol = [Nx if m == 0 else 2 * Nx for _, m in ent]
+        rows1 = [t.data_ptr() + Nx * t.element_size() for t in rs]  # rows 1..Nr-1
+        b = len(ent)
+        if dir == 0:
+            fl = [None if filt is None else filt[m] for _, m in ent]
+            if mode == "full":
+                mats = [self._real_dev("DHT_m" + str(m)) for _, m in ent]
+                outg = [self._work(i, False) if m == 0 else sp[i] for i, (_, m) in enumerate(ent)]
+                call("ccl_dht_gemm_batch", self._dt, b, nrows, nrows, ints(ncol), 0, PP(mats),
+                     PP(rows1), longs(ncol), PP(outg), longs(ncol), 1.0, 0.0, 0.0, stream())
+                fin = outg
+            else:
+                fin = rows1
+            call("ccl_fft_forward_batch", self._dt, b, nrows, Nx, PP(fin), longs([Nx] * b),
+                 ints(real), PP(sp), phs.data_ptr(), PP(fl), stream())
+        else:
+            if mode == "full":
+                bufs = [self._work(i, m != 0) for i, (_, m) in enumerate(ent)]
+                call("ccl_fft_backward_batch", self._dt, b, nrows, Nx, PP(sp), PP(bufs),
+                     longs([Nx] * b), ints(real), phs.data_ptr(), stream())
+                mats = [self._real_dev("DHT_inv_m" + str(m)) for _, m in ent]
+                call("ccl_dht_gemm_batch", self._dt, b, nrows, nrows, ints(ncol), 0, PP(mats),
+                     PP(bufs), longs(ncol), PP(rows1), longs(ncol), 1.0, 0.0, 0.0, stream())
+            else:
+                call("ccl_fft_backward_batch", self._dt, b, nrows, Nx, PP(sp), PP(rows1),
+                     longs([Nx] * b), ints(real), phs.data_ptr(), stream())
 
     def _transform_forward(self, dht_arg, arg_in, arg_out, phs_shft):
         self.transform_field(arg_in[:-2], 0, "full")

@@ -2,7 +2,7 @@
 + PSATD coefficients; push, damp and B-restore entry points."""
 import numpy as np
 
-from ._lib import call, stream
+from ._lib import PP, call, ints, stream
 from .grid import Grid
 from .methods.solver_methods_cu import SolverMethodsCU
 from .transformer import Transformer
@@ -34,14 +34,14 @@ class Solver(Grid, Transformer, SolverMethodsCU):
         nf = 2 * int(self._damp_cells())
         pp, pm = self._phase(1), self._phase(0)
         prof = self._real_dev("DampProfile")
-        for f in ("E", "G"):
-            for c in A["vec_comps"]:
-                for m in range(A["M"] + 1):
-                    rs = self.DataDev[f + c + "_m" + str(m)]
-                    sp = self.DataDev[f + c + "_fb_m" + str(m)]
-                    call("ccl_damp_rows", self._dt, A["Nr"] - 1, A["Nx"], sp.data_ptr(),
-                         rs.data_ptr(), int(m == 0), pp.data_ptr(), pm.data_ptr(),
-                         prof.data_ptr(), nf, stream())
+        ent = [(f + c, m) for f in ("E", "G") for c in A["vec_comps"] for m in range(A["M"] + 1)]
+        for k in range(0, len(ent), 32):
+            part = ent[k:k + 32]
+            sp = [self.DataDev[n + "_fb_m" + str(m)] for n, m in part]
+            rs = [self.DataDev[n + "_m" + str(m)] for n, m in part]
+            call("ccl_damp_batch", self._dt, len(part), A["Nr"] - 1, A["Nx"], PP(sp), PP(rs),
+                 ints([int(m == 0) for _, m in part]), pp.data_ptr(), pm.data_ptr(),
+                 prof.data_ptr(), nf, stream())
 
     def restore_B_fb(self):
         """B = rot(G) / w^2 in spectral space (solver.py:37-39)."""

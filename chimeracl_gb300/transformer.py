@@ -17,11 +17,8 @@ class Transformer(TransformerMethodsCU):
         """Transform scalar fields and the components of vector fields
         (transformer.py:17-26); ``filt`` fuses a spectral filter per mode
         into the forward transform."""
-        for s in scals:
-            self.transform_field(s, dir=dir, mode=mode, filt=filt)
-        for v in vects:
-            for c in self.Args["vec_comps"]:
-                self.transform_field(v + c, dir=dir, mode=mode, filt=filt)
+        names = list(scals) + [v + c for v in vects for c in self.Args["vec_comps"]]
+        self.transform_fields(names, dir=dir, mode=mode, filt=filt)
 
     def _make_spectral_axes(self):
         """kx (numpy fftfreq order), kr_m = j_{m,n}/R, w = |k|, 1/w^2 and the

@@ -207,6 +207,27 @@ int ccl_damp_rows(int dtype, int nrows, int nx, void *spec, void *rs,
                   int rs_real, const void *phs_plus, const void *phs_minus,
                   const void *profile, int nf, void *stream);
 
+/* Batched forms of the three row transforms above: `batch` (<= 32) entries
+ * of nrows rows each, one launch.  in/out/filter/spec/rs are host arrays of
+ * `batch` device pointers (filter may be NULL, or hold NULL entries);
+ * in_ld/out_ld and in_real/out_real/rs_real are host arrays of `batch`
+ * values.  The phase and profile arrays are shared by all entries.  Used to
+ * transform every field component and mode of a step stage at once
+ * (transformer.py:17-26 loops over them one transform at a time). */
+int ccl_fft_forward_batch(int dtype, int batch, int nrows, int nx,
+                          const void *const *in, const long *in_ld,
+                          const int *in_real, void *const *out,
+                          const void *phs, const void *const *filter,
+                          void *stream);
+int ccl_fft_backward_batch(int dtype, int batch, int nrows, int nx,
+                           const void *const *in, void *const *out,
+                           const long *out_ld, const int *out_real,
+                           const void *phs, void *stream);
+int ccl_damp_batch(int dtype, int batch, int nrows, int nx, void *const *spec,
+                   void *const *rs, const int *rs_real, const void *phs_plus,
+                   const void *phs_minus, const void *profile, int nf,
+                   void *stream);
+
 /* Discrete Hankel transform / spectral radial derivative as a batched GEMM:
  * Y[b] = beta*Y[b] + alpha * (A[b] X[b]) for b < batch, A[b] real (m x k,
  * row-major, lda = k), X[b] (k x ncols) with leading dimension ldx, Y[b]
@@ -220,6 +241,15 @@ int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
                  const void *const *A, const void *const *X, long ldx,
                  void *const *Y, long ldy, double alpha_re, double alpha_im,
                  double beta, void *stream);
+
+/* ccl_dht_gemm with a column count and leading dimensions per entry
+ * (ncols, ldx, ldy: host arrays of `batch` values), so the real m=0 and the
+ * complex m>=1 Hankel transforms of a field group share one launch. */
+int ccl_dht_gemm_batch(int dtype, int batch, int m, int k, const int *ncols,
+                       int cplx, const void *const *A, const void *const *X,
+                       const long *ldx, void *const *Y, const long *ldy,
+                       double alpha_re, double alpha_im, double beta,
+                       void *stream);
 
 /* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
  * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,
