@@ -8,10 +8,12 @@ Synthetic seeded plasma (no dataset exists for this workload).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Our arm times the FP32 step (the headline `value`) and the plain FP64 step
-on the same seed through the public API (Solver / Particles / Frame /
-PIC_loop), reports their ratio and the relative deviation of the FP32 run's
-integrated diagnostics from the FP64 run's, a roofline line for the
+Our arm times the mixed-precision step (the headline `value`: FP32
+particles and fields, radial Hankel/derivative GEMMs as BF16x3 products on
+the tensor cores) and the plain FP64 step on the same seed through the
+public API (Solver / Particles / Frame / PIC_loop), reports their ratio and
+the relative deviation of the mixed run's integrated diagnostics from the
+FP64 run's, a roofline line for the
 dominant kernel, and a CPU baseline (the oracle on the host cores).  The
 reference arm times the oracle (the reference's step restated on the CPU,
 OpenMP kernels + numpy FFT/GEMM) on all host threads.  N>1 runs independent
@@ -92,7 +94,7 @@ def build_run(cfg, precision, device_index=0):
     ions.add_new_particles(source=eons)
     eons.free_added()
     f_in = dict(cfg["frame_in"], dt=solver.Args["dt"], DensityProfiles=cfg["profiles"])
-    loop = PIC_loop([solver], [eons, ions], [Frame(f_in)])
+    loop = PIC_loop([solver], [eons, ions], [Frame(f_in)], graphs=True)
     return solver, eons, ions, loop
 
 
@@ -128,7 +130,8 @@ class ClockSampler:
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+         "utilization.gpu")
 
     def __init__(self, index):
         self.index = index
@@ -138,7 +141,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
@@ -155,7 +158,9 @@ class ClockSampler:
                 self.out, _ = self.proc.communicate()
 
     def summary(self):
-        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 9]
+        busy = [r for r in rows if r[9].strip().isdigit() and int(r[9]) >= 50]
+        rows = busy or rows  # samples taken under load, when there are any
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
@@ -232,6 +237,17 @@ def algorithmic(name, args):
                 byts += nrows * nx * (2 * b + rsb)
         passes = 2 if name == "ccl_damp_batch" else 1
         return byts, batch * passes * nrows * 5.0 * nx * np.log2(nx)
+    if name == "ccl_dht_bf16x3_gemm_batch":
+        batch, m, k, ncols = args[:4]
+        beta = args[12]
+        # FP32 X read, FP32 Y written (read too when accumulating), bf16 hi+lo A
+        byts = sum(4 * (m * k + k * n + m * n * (2 if beta else 1)) for n in ncols[:batch])
+        return byts, sum(3 * 2.0 * m * k * n for n in ncols[:batch])  # 3 bf16 products
+    if name in ("ccl_grad_combine", "ccl_rot_combine"):
+        dtype, M, nrows, nx = args[:4]
+        b = 8 if dtype == 0 else 4
+        per = 5 if name == "ccl_grad_combine" else 9  # complex in + out per cell
+        return (M + 1) * nrows * nx * 2 * b * per, 0.0
     if name == "ccl_index_sort":
         dtype, n, Nx, Nr = args[0], args[1], args[5], args[8]
         b = 8 if dtype == 0 else 4
@@ -290,6 +306,7 @@ def time_arm(cfg, precision, steps, warmup, device_index, dist):
     n0 = _lib.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(device_index) as clk:
+        time.sleep(0.3)  # let the sampler start before the timed region
         e0.record()
         for _ in range(steps):
             np_sum += eons.Args["Np"]
@@ -358,23 +375,29 @@ def load_peaks():
 
 
 def roofline(probe_summary, peaks, src):
+    """Roofline line of the kernel with the largest share of the probed
+    time: achieved = algorithmic bytes (or flops) per launch / mean launch
+    time; the tensor-core GEMM is checked against both the HBM copy peak and
+    the bf16 tensor peak and reported against the one it is closer to."""
     if not probe_summary:
         return None
     name, s = max(probe_summary.items(), key=lambda kv: kv[1]["ms_total"])
-    per_ms = s["ms_total"] / s["launches"]
-    if name in ("ccl_dht_gemm", "ccl_dht_gemm_batch"):
-        # SIMT GEMM: report against HBM for its operand traffic
-        achieved = s["bytes"] / s["launches"] / (per_ms * 1e-3) / 1e9
-        peak = peaks["hbm_gbs"]
-        return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                "launches": s["launches"], "ms_per_launch": round(per_ms, 5),
-                "flops_per_launch": s["flops"] / s["launches"], "peak_source": src}
-    achieved = s["bytes"] / s["launches"] / (per_ms * 1e-3) / 1e9
-    peak = peaks["hbm_gbs"]
-    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-            "launches": s["launches"], "ms_per_launch": round(per_ms, 5), "peak_source": src}
+    per_s = s["ms_total"] / s["launches"] * 1e-3
+    gbs = s["bytes"] / s["launches"] / per_s / 1e9
+    line = {"kernel": name, "launches": s["launches"], "ms_per_launch": round(per_s * 1e3, 5),
+            "traffic": None, "peak_source": src}
+    hbm = {"bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": round(gbs / peaks["hbm_gbs"], 4)}
+    if name == "ccl_dht_bf16x3_gemm_batch":
+        tfs = s["flops"] / s["launches"] / per_s / 1e12
+        pk = peaks.get("bf16_tflops", FALLBACK_PEAKS["bf16_tflops"])
+        ten = {"bound": "tensor", "achieved": round(tfs, 2), "peak": pk, "unit": "TFLOP/s",
+               "frac": round(tfs / pk, 4)}
+        line.update(ten if ten["frac"] > hbm["frac"] else hbm)
+        line["hbm_frac"], line["tensor_frac"] = hbm["frac"], ten["frac"]
+    else:
+        line.update(hbm)
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -442,17 +465,20 @@ def run_ours(args):
     dist, rank, local, world = init_dist(args.gpus)
     dev = torch.device("cuda", local)
     cfg = workload(seed=1000 + rank)
-    # FP32 form (headline) and the plain FP64 form on the same seed
-    r32 = time_arm(cfg, "fp32", args.steps, args.warmup, local, dist)
+    # mixed form (headline) and the plain FP64 form on the same seed
+    r32 = time_arm(cfg, "mixed", args.steps, args.warmup, local, dist)
     diagnostics_dev(r32["solver"], r32["eons"])  # first use of torch's reductions
     e2e = e2e_arm(r32, args.steps)
-    probe = Probe(["ccl_dht_gemm_batch", "ccl_dht_gemm", "ccl_fft_forward_batch",
+    probe = Probe(["ccl_dht_bf16x3_gemm_batch", "ccl_grad_combine", "ccl_rot_combine",
+                   "ccl_dht_gemm_batch", "ccl_dht_gemm", "ccl_fft_forward_batch",
                    "ccl_fft_backward_batch", "ccl_damp_batch", "ccl_index_sort",
                    "ccl_deposit_vector", "ccl_deposit_scalar", "ccl_gather_push",
                    "ccl_psatd_advance"])
     orig = install_probe(probe)
+    r32["loop"].graphs = False  # the probe times each launch: run the steps eagerly
     for _ in range(min(args.steps, 5)):
         r32["loop"].step()
+    r32["loop"].graphs = True
     remove_probe(orig)
     prof = probe.summary()
     r64 = time_arm(cfg, "fp64", args.steps, args.warmup, local, dist)
@@ -465,18 +491,18 @@ def run_ours(args):
     torch.cuda.synchronize()
     acc = {}
     vals = {}
-    for tag, r in (("fp32", r32), ("fp64", r64)):
+    for tag, r in (("mixed", r32), ("fp64", r64)):
         We, ez, kin = diagnostics_dev(r["solver"], r["eons"])
         A = r["solver"].Args
         x_las = cfg["laser_in"]["x0"] + r["loop"].it * A["dt"]
         vals[tag] = (float(We), wake_amplitude(ez.cpu().numpy(), A["Xgrid"], x_las,
                                                cfg["laser_in"]["Lx"]), float(kin),
                      r["loop"].it)
-    if vals["fp32"][3] == vals["fp64"][3]:
-        acc = {"field_energy_rel_err": abs(vals["fp32"][0] / vals["fp64"][0] - 1),
-               "ez_wake_rel_err": abs(vals["fp32"][1] / vals["fp64"][1] - 1),
-               "kinetic_rel_err": abs(vals["fp32"][2] / vals["fp64"][2] - 1),
-               "at_step": vals["fp32"][3]}
+    if vals["mixed"][3] == vals["fp64"][3]:
+        acc = {"field_energy_rel_err": abs(vals["mixed"][0] / vals["fp64"][0] - 1),
+               "ez_wake_rel_err": abs(vals["mixed"][1] / vals["fp64"][1] - 1),
+               "kinetic_rel_err": abs(vals["mixed"][2] / vals["fp64"][2] - 1),
+               "at_step": vals["mixed"][3]}
     ms32 = reduce_max(dist, r32["ms"], dev)
     ms64 = reduce_max(dist, r64["ms"], dev)
     np32 = reduce_sum(dist, r32["np_sum"], dev)
@@ -491,15 +517,16 @@ def run_ours(args):
             "metric": "electron particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded plasma, laser)",
+            "vs_baseline": None, "dtype": "f32+bf16x3", "data": "synthetic (seeded plasma, laser)",
             "config": config_line(cfg),
             "fp64": {"value": v64, "ms_per_step": ms64 / args.steps, "dtype": "f64",
                      "gpu_launches": r64["launches"]},
-            "fp32_over_fp64": value / v64,
-            "fp32_vs_fp64_error": acc,
+            "mixed_over_fp64": value / v64,
+            "mixed_vs_fp64_error": acc,
             "e2e": {"value": e2e_np / e2e_s, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
             "gpu_launches": r32["launches"],
+            "graph_replays": r32["loop"].graph_replays,
             "clocks": r32["clocks"],
             "roofline": roofline(prof, peaks, src),
             "kernel_probe": {k: {"launches": v["launches"], "ms_total": round(v["ms_total"], 4)}
@@ -520,7 +547,7 @@ def run_ours(args):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)

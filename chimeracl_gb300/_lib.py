@@ -50,7 +50,13 @@ SIGNATURES = {
     "ccl_damp_batch": [_i, _i, _i, _i, _pp, _pp, _vp, _vp, _vp, _vp, _i, _vp],
     "ccl_dht_gemm_batch": [_i, _i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],
     "ccl_psatd_advance": [_i, _l, _d, _vp, _vp, _vp, _pp, _vp],
+    "ccl_dht_bf16x3_prepare_bytes": [_i, _i, C.POINTER(_sz)],
+    "ccl_dht_bf16x3_prepare": [_i, _vp, _i, _i, _vp, _sz, _vp],
+    "ccl_dht_bf16x3_gemm_batch": [_i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],
+    "ccl_dht_bf16x3_status": [_i],
     "ccl_get_m1": [_i, _i, _i, _vp, _vp, _vp],
+    "ccl_grad_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _vp],
+    "ccl_rot_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _pp, _vp],
     "ccl_set": [_i, _i, _l, _vp, _d, _d, _vp],
     "ccl_append_c2c": [_i, _l, _vp, _vp, _vp],
     "ccl_zpaxz": [_i, _l, _vp, _d, _d, _vp, _vp],

@@ -350,6 +350,36 @@ int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
                          alpha_im, beta, S(stream));
 }
 
+int ccl_dht_bf16x3_prepare_bytes(int m, int k, size_t *bytes) {
+  NONNULL(bytes);
+  CCL_REQUIRE(m > 0 && k > 0 && k <= 256, CCL_ERR_UNSUPPORTED,
+              "%s: m=%d k=%d (k <= 256)", __func__, m, k);
+  *bytes = umma_split_bytes(m, k);
+  return CCL_OK;
+}
+
+int ccl_dht_bf16x3_prepare(int dtype, const void *A, int m, int k, void *out,
+                           size_t bytes, void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNULL(A); NONNULL(out);
+  if (dtype == CCL_F64)
+    return umma_split_a<double>((const double *)A, m, k, out, bytes, S(stream));
+  return umma_split_a<float>((const float *)A, m, k, out, bytes, S(stream));
+}
+
+int ccl_dht_bf16x3_gemm_batch(int batch, int m, int k, const int *ncols,
+                              int cplx, const void *const *A_prepared,
+                              const void *const *X, const long *ldx,
+                              void *const *Y, const long *ldy, double alpha_re,
+                              double alpha_im, double beta, void *stream) {
+  NONNULL(ncols); NONNULL(A_prepared); NONNULL(X); NONNULL(ldx); NONNULL(Y);
+  NONNULL(ldy);
+  return umma_gemm_batch(batch, m, k, ncols, cplx, A_prepared, X, ldx, Y, ldy,
+                         alpha_re, alpha_im, beta, S(stream));
+}
+
+int ccl_dht_bf16x3_status(int reset) { return umma_status(reset); }
+
 int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
                       const void *c2, const void *c3, void *const *flds,
                       void *stream) {
@@ -365,6 +395,25 @@ int ccl_get_m1(int dtype, int nrows, int nx, void *out, const void *in,
   CCL_REQUIRE(nrows >= 0 && nx > 0, CCL_ERR_ARG, "%s: nrows=%d nx=%d", __func__, nrows, nx);
   NONNULL(out); NONNULL(in);
   return DISPATCH(dtype, get_m1(nrows, nx, out, in, S(stream)));
+}
+
+int ccl_grad_combine(int dtype, int M, int nrows, int nx, const void *kx,
+                     const void *const *rho, const void *const *Pm,
+                     const void *const *Pp, void *const *dN, void *stream) {
+  DTYPE_CHECK(dtype);
+  CCL_REQUIRE(nrows >= 0 && nx > 0, CCL_ERR_ARG, "%s: nrows=%d nx=%d", __func__, nrows, nx);
+  NONNULL(kx); NONNULL(rho); NONNULL(dN);
+  return DISPATCH(dtype, grad_combine(M, nrows, nx, kx, rho, Pm, Pp, dN, S(stream)));
+}
+
+int ccl_rot_combine(int dtype, int M, int nrows, int nx, const void *kx,
+                    const void *const *G, const void *const *Qm,
+                    const void *const *Qp, const void *const *poiss,
+                    void *const *B, void *stream) {
+  DTYPE_CHECK(dtype);
+  CCL_REQUIRE(nrows >= 0 && nx > 0, CCL_ERR_ARG, "%s: nrows=%d nx=%d", __func__, nrows, nx);
+  NONNULL(kx); NONNULL(G); NONNULL(B);
+  return DISPATCH(dtype, rot_combine(M, nrows, nx, kx, G, Qm, Qp, poiss, B, S(stream)));
 }
 
 // -------------------------------------------------------------- elementwise

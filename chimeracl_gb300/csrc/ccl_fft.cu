@@ -345,10 +345,18 @@ template <typename T> static int fft_check(int nx, FftPlan *pl, size_t *smem) {
   return CCL_OK;
 }
 
+// Raise a kernel's dynamic shared-memory limit once per size (not on every
+// launch, so that steady-state steps issue launches only).
 template <typename K> static void allow_smem(K kernel, size_t smem) {
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+  if (smem <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::map<const void *, size_t> done;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &v = done[(const void *)kernel];
+  if (v < smem) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    v = smem;
+  }
 }
 
 static int batch_check(int batch, int nrows) {

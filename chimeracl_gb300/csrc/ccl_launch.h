@@ -107,7 +107,23 @@ template <typename T> struct Ops {
                            int nf, cudaStream_t s);
   static int mul_phase(int nrows, int nx, void *a, const void *phs,
                        cudaStream_t s);
+  static int grad_combine(int M, int nrows, int nx, const void *kx,
+                          const void *const *rho, const void *const *Pm,
+                          const void *const *Pp, void *const *dN, cudaStream_t s);
+  static int rot_combine(int M, int nrows, int nx, const void *kx,
+                         const void *const *G, const void *const *Qm,
+                         const void *const *Qp, const void *const *poiss,
+                         void *const *B, cudaStream_t s);
 };
+
+// ccl_umma.cu (BF16x3 tensor-core Hankel GEMM, FP32 operands)
+size_t umma_split_bytes(int m, int k);
+template <typename TA>
+int umma_split_a(const TA *A, int m, int k, void *out, size_t bytes, cudaStream_t s);
+int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const void *const *Ap,
+                    const void *const *X, const long *ldx, void *const *Y, const long *ldy,
+                    double are, double aim, double beta, cudaStream_t s);
+int umma_status(int reset);
 
 size_t index_sort_ws_bytes(long np, long ncells);
 int iota_u32(uint32_t *a, long n, cudaStream_t s);

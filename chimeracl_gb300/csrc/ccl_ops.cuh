@@ -261,4 +261,55 @@ int Ops<T>::mul_phase(int nrows, int nx, void *a, const void *phs,
   return CCL_OK;
 }
 
+template <typename T>
+int Ops<T>::grad_combine(int M, int nrows, int nx, const void *kx, const void *const *rho,
+                         const void *const *Pm, const void *const *Pp, void *const *dN,
+                         cudaStream_t s) {
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "grad_combine: M=%d", M);
+  ptrs<4> r, pm, pp;
+  ptrs<12> d;
+  for (int m = 0; m <= M; m++) {
+    CCL_REQUIRE(rho[m], CCL_ERR_ARG, "grad_combine: null rho %d", m);
+    r.p[m] = (void *)rho[m];
+    pm.p[m] = Pm ? (void *)Pm[m] : nullptr;
+    pp.p[m] = Pp ? (void *)Pp[m] : nullptr;
+    for (int c = 0; c < 3; c++) {
+      CCL_REQUIRE(dN[3 * m + c], CCL_ERR_ARG, "grad_combine: null output %d", 3 * m + c);
+      d.p[3 * m + c] = dN[3 * m + c];
+    }
+  }
+  long n = (long)nrows * nx;
+  if (n == 0) return CCL_OK;
+  dim3 grid(grid_for(n, 256, 4), M + 1);
+  k_grad_combine<T><<<grid, 256, 0, s>>>(n, nx, (const T *)kx, r, pm, pp, d);
+  CCL_LAUNCH_CHECK("grad_combine");
+  return CCL_OK;
+}
+
+template <typename T>
+int Ops<T>::rot_combine(int M, int nrows, int nx, const void *kx, const void *const *G,
+                        const void *const *Qm, const void *const *Qp, const void *const *poiss,
+                        void *const *B, cudaStream_t s) {
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "rot_combine: M=%d", M);
+  ptrs<12> g, qm, qp, b;
+  ptrs<4> po;
+  for (int m = 0; m <= M; m++) {
+    po.p[m] = poiss ? (void *)poiss[m] : nullptr;
+    for (int c = 0; c < 3; c++) {
+      const int j = 3 * m + c;
+      CCL_REQUIRE(G[j] && B[j], CCL_ERR_ARG, "rot_combine: null field %d", j);
+      g.p[j] = (void *)G[j];
+      b.p[j] = B[j];
+      qm.p[j] = Qm ? (void *)Qm[j] : nullptr;
+      qp.p[j] = Qp ? (void *)Qp[j] : nullptr;
+    }
+  }
+  long n = (long)nrows * nx;
+  if (n == 0) return CCL_OK;
+  dim3 grid(grid_for(n, 256, 4), M + 1);
+  k_rot_combine<T><<<grid, 256, 0, s>>>(n, nx, (const T *)kx, g, qm, qp, po, b);
+  CCL_LAUNCH_CHECK("rot_combine");
+  return CCL_OK;
+}
+
 }  // namespace ccl

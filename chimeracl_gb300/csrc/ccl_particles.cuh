@@ -64,29 +64,6 @@ __device__ __forceinline__ u32 cell_key(T xp, T yp, T zp, const KeyGrid &g) {
   return (u32)(nrc * nxc);
 }
 
-// keys + per-cell counts; counts aggregated per warp with match_any so that
-// a warp of cell-sorted particles issues one atomic per distinct cell.
-template <typename T>
-__global__ void k_keys(long np, const T *__restrict__ x,
-                       const T *__restrict__ y, const T *__restrict__ z,
-                       KeyGrid g, u32 *__restrict__ keys,
-                       u32 *__restrict__ counts) {
-  const int lane = threadIdx.x & 31;
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long base = (blockIdx.x * (long)blockDim.x + threadIdx.x) & ~31L; base < np;
-       base += stride) {
-    long i = base + lane;
-    bool valid = i < np;
-    u32 k = 0xffffffffu;
-    if (valid) {
-      k = cell_key<T>(x[i], y[i], z[i], g);
-      keys[i] = k;
-    }
-    unsigned peers = __match_any_sync(0xffffffffu, k);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&counts[k], __popc(peers));
-  }
-}
-
 // ---------------------------------------------------------------------
 // Exclusive scan of u32 (device-wide, reduce-then-scan).
 constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8,
@@ -162,6 +139,43 @@ static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
     *total_out = (part ? part[blockIdx.x] : 0) + tot;
 }
 
+// Keys + per-cell counts over tiles of ST_TILE consecutive particles; cell
+// counts are aggregated per warp with match_any (a warp of cell-sorted
+// particles issues one atomic per distinct cell); the particles outside the
+// window (overflow key) are counted per tile.
+constexpr int ST_THREADS = 256, ST_ITEMS = 8, ST_TILE = ST_THREADS * ST_ITEMS;
+
+template <typename T>
+__global__ void __launch_bounds__(ST_THREADS)
+    k_keys(long np, const T *__restrict__ x, const T *__restrict__ y,
+           const T *__restrict__ z, KeyGrid g, u32 *__restrict__ keys,
+           u32 *__restrict__ counts, u32 *__restrict__ tile_ovf) {
+  __shared__ u32 sh[32];
+  const int lane = threadIdx.x & 31;
+  const u32 C = (u32)(g.Nx - 1) * (u32)(g.Nr - 1);
+  const long base = (long)blockIdx.x * ST_TILE;
+  u32 novf = 0;
+#pragma unroll
+  for (int it = 0; it < ST_ITEMS; it++) {
+    const long i = base + it * ST_THREADS + threadIdx.x;
+    const bool valid = i < np;
+    u32 k = 0xffffffffu;
+    if (valid) {
+      k = cell_key<T>(x[i], y[i], z[i], g);
+      keys[i] = k;
+    }
+    novf += (valid && k == C) ? 1u : 0u;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (valid && k != C && lane == __ffs(peers) - 1) atomicAdd(&counts[k], __popc(peers));
+  }
+  u32 tot;
+  block_exclusive_scan(novf, sh, &tot);
+  if (threadIdx.x == 0) {
+    tile_ovf[blockIdx.x] = tot;
+    if (tot) atomicAdd(&counts[C], tot);
+  }
+}
+
 static inline long scan_ws_words(long L) {
   long w = 0;
   while (L > SCAN_TILE) {
@@ -194,120 +208,81 @@ static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
 }
 
 // ---------------------------------------------------------------------
-// Stable LSD radix sort of (key, particle number): per pass a tile
-// histogram, a device-wide scan of the (digit, tile) table, and a scatter
-// in which each warp ranks its 256 keys in order (match_any per round of 32)
-// so that the order of equal keys is the input order.
-constexpr int RS_THREADS = 256, RS_WARPS = RS_THREADS / 32, RS_ITEMS = 8,
-              RS_TILE = RS_THREADS * RS_ITEMS, RS_MAXBITS = 10;
-
-static __global__ void k_radix_hist(const u32 *__restrict__ keys, long n, int shift,
-                             int nbits, u32 *__restrict__ hist, int ntiles) {
-  extern __shared__ u32 shh[];
-  const int NB = 1 << nbits;
-  for (int d = threadIdx.x; d < NB; d += RS_THREADS) shh[d] = 0;
-  __syncthreads();
-  long base = (long)blockIdx.x * RS_TILE;
-#pragma unroll
-  for (int it = 0; it < RS_ITEMS; it++) {
-    long i = base + it * RS_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&shh[(keys[i] >> shift) & (NB - 1)], 1u);
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < NB; d += RS_THREADS)
-    hist[(long)d * ntiles + blockIdx.x] = shh[d];
-}
-
-static __global__ void k_radix_scatter(const u32 *__restrict__ kin,
-                                const u32 *__restrict__ vin, long n, int shift,
-                                int nbits, const u32 *__restrict__ offs,
-                                int ntiles, u32 *__restrict__ kout,
-                                u32 *__restrict__ vout) {
-  extern __shared__ u32 wh[];  // RS_WARPS x NB
-  const int NB = 1 << nbits;
-  for (int i = threadIdx.x; i < RS_WARPS * NB; i += RS_THREADS) wh[i] = 0;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Counting-sort scatter.  In-window particles take their slot in their
+// cell's segment through a per-cell cursor (one atomic per distinct cell per
+// warp; lanes of a warp keep index order); out-of-window particles take
+// cell_offset[C] + (overflow particles in earlier tiles) + (rank in this
+// tile), so that segment is in index order.  k_cell_fixup then sorts each
+// cell's segment by particle number (insertion sort: linear on the nearly
+// sorted segments this produces), which makes the result that of a stable
+// sort: within a cell, ascending particle number -- the order of the
+// reference's sort kernel run serially.
+static __global__ void __launch_bounds__(ST_THREADS)
+    k_scatter(long np, const u32 *__restrict__ keys, u32 C,
+              const u32 *__restrict__ cell_offset, u32 *__restrict__ cursor,
+              const u32 *__restrict__ ovf_off, u32 *__restrict__ sort_indx) {
+  __shared__ u32 sh[32];
+  const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  long base = (long)blockIdx.x * RS_TILE + (long)warp * (RS_TILE / RS_WARPS);
-  u32 kk[RS_ITEMS], vv[RS_ITEMS], pos[RS_ITEMS];
-  int dg[RS_ITEMS];
-  u32 *myh = wh + warp * NB;
+  const long base = (long)blockIdx.x * ST_TILE;
+  u32 tile_run = ovf_off[blockIdx.x] + cell_offset[C];
 #pragma unroll
-  for (int r = 0; r < RS_ITEMS; r++) {
-    long i = base + r * 32 + lane;
-    bool valid = i < n;
-    u32 k = valid ? kin[i] : 0u;
-    u32 v = valid ? (vin ? vin[i] : (u32)i) : 0u;
-    int d = valid ? (int)((k >> shift) & (NB - 1)) : NB;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    u32 rank = __popc(peers & lt);
-    u32 before = valid ? myh[d] : 0u;
-    __syncwarp();
-    if (valid && rank == 0) myh[d] = before + __popc(peers);
-    __syncwarp();
-    kk[r] = k;
-    vv[r] = v;
-    pos[r] = before + rank;
-    dg[r] = d;
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < NB; d += RS_THREADS) {
-    u32 run = 0;
-#pragma unroll
-    for (int w = 0; w < RS_WARPS; w++) {
-      u32 t = wh[w * NB + d];
-      wh[w * NB + d] = run;
-      run += t;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < RS_ITEMS; r++) {
-    int d = dg[r];
-    if (d < NB) {
-      u32 p = offs[(long)d * ntiles + blockIdx.x] + wh[warp * NB + d] + pos[r];
-      if (kout) kout[p] = kk[r];
-      vout[p] = vv[r];
-    }
+  for (int it = 0; it < ST_ITEMS; it++) {
+    const long i = base + it * ST_THREADS + threadIdx.x;
+    const bool valid = i < np;
+    const u32 k = valid ? keys[i] : 0xffffffffu;
+    const bool ovf = valid && k == C;
+    // overflow: block-ordered rank within this round of ST_THREADS items
+    u32 rtot;
+    const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
+    if (ovf) sort_indx[tile_run + r] = (u32)i;
+    tile_run += rtot;
+    // in-window: warp-aggregated cursor
+    const unsigned peers = __match_any_sync(0xffffffffu, (valid && !ovf) ? k : 0xffffffffu);
+    const int leader = __ffs(peers) - 1;
+    u32 b0 = 0;
+    if (valid && !ovf && lane == leader) b0 = atomicAdd(&cursor[k], __popc(peers));
+    b0 = __shfl_sync(0xffffffffu, b0, leader);
+    if (valid && !ovf) sort_indx[cell_offset[k] + b0 + __popc(peers & lt)] = (u32)i;
   }
 }
 
-static inline int radix_passes(u32 maxkey, int *bits_per_pass) {
-  int bits = 32 - __builtin_clz(maxkey | 1u);
-  int np = (bits + RS_MAXBITS - 1) / RS_MAXBITS;
-  *bits_per_pass = (bits + np - 1) / np;
-  return np;
+static __global__ void k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset,
+                             u32 *__restrict__ sort_indx) {
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < (long)C;
+       c += (long)gridDim.x * blockDim.x) {
+    const u32 p0 = cell_offset[c], p1 = cell_offset[c + 1];
+    for (u32 a = p0 + 1; a < p1; a++) {
+      const u32 v = sort_indx[a];
+      u32 b = a;
+      while (b > p0 && sort_indx[b - 1] > v) {
+        sort_indx[b] = sort_indx[b - 1];
+        b--;
+      }
+      sort_indx[b] = v;
+    }
+  }
 }
 
 struct SortWs {
-  u32 *k[2], *v[2], *hist, *scan;
+  u32 *cursor, *tile_ovf, *scan;
 };
 
 static inline size_t sort_ws_bytes(long np, long ncells) {
-  int bpp;
-  radix_passes((u32)ncells, &bpp);
-  long ntiles = (np + RS_TILE - 1) / RS_TILE;
-  long hist = (1L << bpp) * ntiles;
-  long scanw = scan_ws_words(hist > ncells + 1 ? hist : ncells + 1);
-  long words = 4 * np + hist + scanw + 64;
+  long ntiles = (np + ST_TILE - 1) / ST_TILE;
+  long scanw = scan_ws_words(ncells + 1 > ntiles ? ncells + 1 : ntiles);
+  long words = ncells + 1 + ntiles + 1 + scanw + 64;
   return (size_t)words * 4 + 256;
 }
 
 static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
-  int bpp;
-  radix_passes((u32)ncells, &bpp);
-  long ntiles = (np + RS_TILE - 1) / RS_TILE;
-  long hist = (1L << bpp) * ntiles;
+  long ntiles = (np + ST_TILE - 1) / ST_TILE;
   uintptr_t p = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
   u32 *w = (u32 *)p;
   SortWs s;
-  s.k[0] = w;
-  s.k[1] = w + np;
-  s.v[0] = w + 2 * np;
-  s.v[1] = w + 3 * np;
-  s.hist = w + 4 * np;
-  s.scan = s.hist + hist;
+  s.cursor = w;
+  s.tile_ovf = w + ncells + 1;
+  s.scan = s.tile_ovf + ntiles + 1;
   return s;
 }
 
@@ -322,9 +297,11 @@ int index_sort(long np, const T *x, const T *y, const T *z, KeyGrid g,
               "index_sort: workspace %zu < %zu bytes", ws_bytes,
               sort_ws_bytes(np, C));
   SortWs w = carve_sort_ws(ws, np, C);
+  const long ntiles = (np + ST_TILE - 1) / ST_TILE;
   cudaMemsetAsync(counts, 0, (C + 1) * sizeof(u32), s);
   if (np > 0) {
-    k_keys<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, g, indx, counts);
+    k_keys<T><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, x, y, z, g, indx, counts,
+                                                      w.tile_ovf);
     CCL_LAUNCH_CHECK("keys");
   }
   int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1,
@@ -333,28 +310,14 @@ int index_sort(long np, const T *x, const T *y, const T *z, KeyGrid g,
   k_copy_u32<<<1, 1, 0, s>>>(cell_offset + C, np_stay);
   CCL_LAUNCH_CHECK("np_stay");
   if (np == 0) return CCL_OK;
-  int bpp;
-  int npass = radix_passes((u32)C, &bpp);
-  long ntiles = (np + RS_TILE - 1) / RS_TILE;
-  size_t smem_h = (size_t)(1 << bpp) * 4, smem_s = RS_WARPS * smem_h;
-  const u32 *kin = indx, *vin = nullptr;
-  for (int p = 0; p < npass; p++) {
-    int shift = p * bpp;
-    k_radix_hist<<<(unsigned)ntiles, RS_THREADS, smem_h, s>>>(
-        kin, np, shift, bpp, w.hist, (int)ntiles);
-    CCL_LAUNCH_CHECK("radix_hist");
-    rc = scan_exclusive(w.hist, (1L << bpp) * ntiles, w.hist, nullptr, w.scan,
-                        s);
-    if (rc) return rc;
-    bool last = p == npass - 1;
-    u32 *kout = last ? nullptr : w.k[p & 1];
-    u32 *vout = last ? sort_indx : w.v[p & 1];
-    k_radix_scatter<<<(unsigned)ntiles, RS_THREADS, smem_s, s>>>(
-        kin, vin, np, shift, bpp, w.hist, (int)ntiles, kout, vout);
-    CCL_LAUNCH_CHECK("radix_scatter");
-    kin = kout;
-    vin = vout;
-  }
+  rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
+  if (rc) return rc;
+  cudaMemsetAsync(w.cursor, 0, C * sizeof(u32), s);
+  k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
+                                                    w.cursor, w.tile_ovf, sort_indx);
+  CCL_LAUNCH_CHECK("scatter");
+  k_cell_fixup<<<grid_for(C, 256), 256, 0, s>>>((u32)C, cell_offset, sort_indx);
+  CCL_LAUNCH_CHECK("cell_fixup");
   return CCL_OK;
 }
 

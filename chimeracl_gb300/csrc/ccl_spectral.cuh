@@ -169,4 +169,84 @@ __global__ void k_cast_c2d(long n, const T *in, T *out) {
   CCL_GRID_STRIDE(i, n) out[i] = in[2 * i];
 }
 
+// ---------------------------------------------------------------------
+// Spectral gradient and curl, combine step.  The radial derivative matrix
+// products arrive precomputed (one batched GEMM launch): for mode m,
+//   Pm[m] = dDHT_minus_m . f_{m-1}  (for m = 0: dDHT_minus_0 . f_{+1}, read
+//           here through the m=-1 mirror (-Re, +Im) at column (nx-ix) mod nx,
+//           which commutes with the real radial matrix), Pp[m] = dDHT_plus_m .
+//           f_{m+1}; NULL where the reference has no such term.
+// Gradient (transformer_methods_cl.py:87-133):
+//   Nx = i kx rho_m,  Ny = -T- + T+,  Nz = -i (T- + T+).
+template <typename T>
+__device__ __forceinline__ cplx<T> ld_mode(const T *p, long i, long ir, long ix, int nx,
+                                           bool mirror) {
+  if (!p) {
+    cplx<T> z = {T(0), T(0)};
+    return z;
+  }
+  if (!mirror) return ld_c(p, i);
+  const long io = ix == 0 ? 0 : nx - ix;
+  cplx<T> q = ld_c(p, ir * nx + io);
+  q.re = -q.re;
+  return q;
+}
+
+template <typename T>
+__global__ void k_grad_combine(long n, int nx, const T *__restrict__ kx, ptrs<4> rho,
+                               ptrs<4> Pm, ptrs<4> Pp, ptrs<12> dN) {
+  const int m = blockIdx.y;
+  CCL_GRID_STRIDE(i, n) {
+    const long ir = i / nx, ix = i - ir * nx;
+    const T k = kx[ix];
+    const cplx<T> r = ld_c((const T *)rho.p[m], i);
+    const cplx<T> tm = ld_mode((const T *)Pm.p[m], i, ir, ix, nx, m == 0);
+    const cplx<T> tp = ld_mode((const T *)Pp.p[m], i, ir, ix, nx, false);
+    const cplx<T> gx = {k * (-r.im), k * r.re};
+    const cplx<T> gy = {-tm.re + tp.re, -tm.im + tp.im};
+    const cplx<T> gz = {tm.im + tp.im, -(tm.re + tp.re)};
+    st_c((T *)dN.p[3 * m], i, gx);
+    st_c((T *)dN.p[3 * m + 1], i, gy);
+    st_c((T *)dN.p[3 * m + 2], i, gz);
+  }
+}
+
+// Curl (transformer_methods_cl.py:185-263), with U-_c, U+_c the products of
+// component c (same mirror rule), times the Poisson factor 1/w^2 of
+// field_poiss_vec when `poiss` is given:
+//   Bx = (-U-_z + i U-_y) + (U+_z + i U+_y)
+//   By = -i (kx Gz + U-_x + U+_x)
+//   Bz = i kx Gy + U-_x - U+_x
+template <typename T>
+__global__ void k_rot_combine(long n, int nx, const T *__restrict__ kx, ptrs<12> G,
+                              ptrs<12> Qm, ptrs<12> Qp, ptrs<4> poiss, ptrs<12> B) {
+  const int m = blockIdx.y;
+  CCL_GRID_STRIDE(i, n) {
+    const long ir = i / nx, ix = i - ir * nx;
+    const T k = kx[ix];
+    const cplx<T> gy = ld_c((const T *)G.p[3 * m + 1], i);
+    const cplx<T> gz = ld_c((const T *)G.p[3 * m + 2], i);
+    cplx<T> um[3], up[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      um[c] = ld_mode((const T *)Qm.p[3 * m + c], i, ir, ix, nx, m == 0);
+      up[c] = ld_mode((const T *)Qp.p[3 * m + c], i, ir, ix, nx, false);
+    }
+    cplx<T> bx = {-um[2].re - um[1].im + up[2].re - up[1].im,
+                  -um[2].im + um[1].re + up[2].im + up[1].re};
+    const cplx<T> sy = {k * gz.re + um[0].re + up[0].re, k * gz.im + um[0].im + up[0].im};
+    cplx<T> by = {sy.im, -sy.re};
+    cplx<T> bz = {-k * gy.im + um[0].re - up[0].re, k * gy.re + um[0].im - up[0].im};
+    if (poiss.p[m]) {
+      const T f = ((const T *)poiss.p[m])[i];
+      bx.re *= f; bx.im *= f;
+      by.re *= f; by.im *= f;
+      bz.re *= f; bz.im *= f;
+    }
+    st_c((T *)B.p[3 * m], i, bx);
+    st_c((T *)B.p[3 * m + 1], i, by);
+    st_c((T *)B.p[3 * m + 2], i, bz);
+  }
+}
+
 }  // namespace ccl

@@ -10,8 +10,7 @@
 // no-swizzle core-matrix layout, produced by k_umma_split_a) is copied once
 // into shared memory and stays resident.  X is staged per 128-deep K chunk:
 // each thread loads one 8 (k) x 8 (n) block of FP32, splits it and writes
-// one K-major 8x8 bf16 core matrix for X_hi and one for X_lo (rows written in
-// a per-thread rotated order so a quarter-warp hits distinct banks).  Two X
+// one K-major 8x8 bf16 core matrix for X_hi and one for X_lo.  Two X
 // buffers and two TMEM accumulators (128 lanes x 64 columns each) let thread
 // 0 issue the next chunk's MMAs while the others stage and drain.  Every
 // mbarrier wait is bounded; a wait that gives up records an error code in a
@@ -27,7 +26,7 @@ namespace ccl {
 
 constexpr int UM_THREADS = 128, UM_BM = 128, UM_BN = 64, UM_BK = 128;
 constexpr int UM_MAXK = 256, UM_MAXBATCH = 32;
-constexpr int UM_TILES_PER_CTA = 4;
+constexpr int UM_MAX_TILES_PER_CTA = 4;
 constexpr long UM_SPIN_LIMIT = 20000000L;  // ~ a second of try_wait polls
 
 __device__ int g_umma_error = 0;
@@ -173,7 +172,7 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int kp, i
 // ---------------------------------------------------------------- GEMM
 template <bool CPLX, bool ACC>
 __global__ void __launch_bounds__(UM_THREADS, 1)
-    k_umma_gemm(UmmaBatch b, int M, int K, int KP, float are, float aim) {
+    k_umma_gemm(UmmaBatch b, int M, int K, int KP, int tiles_per_cta, float are, float aim) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   unsigned char *sA = sm;                                   // umma_tile_bytes(KP)
@@ -186,9 +185,9 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int e = blockIdx.z, mt = blockIdx.y;
   const int N = b.ncols[e];
-  const int n_begin = blockIdx.x * UM_TILES_PER_CTA * UM_BN;
+  const int n_begin = blockIdx.x * tiles_per_cta * UM_BN;
   if (n_begin >= N) return;
-  const int ntiles = min(UM_TILES_PER_CTA, (N - n_begin + UM_BN - 1) / UM_BN);
+  const int ntiles = min(tiles_per_cta, (N - n_begin + UM_BN - 1) / UM_BN);
   const int nkc = KP / UM_BK;
   const float *__restrict__ X = b.X[e];
   float *__restrict__ Y = b.Y[e];
@@ -303,8 +302,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
       unsigned char *dst_hi = sX + buf * x_stage + (nb * (UM_BK / 8) + kb) * 128;
       unsigned char *dst_lo = dst_hi + x_lo_off;
 #pragma unroll
-      for (int rr = 0; rr < 8; rr++) {
-        const int c = (rr + tid) & 7;  // core-matrix row = column n of the block
+      for (int c = 0; c < 8; c++) {  // core-matrix row = column n of the block
         __nv_bfloat16 h[8], l[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) {
@@ -416,14 +414,26 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
   }
   const int kp = umma_kpad(k);
   const size_t smem = umma_smem(kp);
-  dim3 grid((nmax + UM_TILES_PER_CTA * UM_BN - 1) / (UM_TILES_PER_CTA * UM_BN),
-            (m + UM_BM - 1) / UM_BM, batch);
+  // N tiles per CTA: amortise the resident A tile over up to 4 tiles, but
+  // keep at least ~3 CTAs per SM of work in the launch (one CTA is resident
+  // per SM at this shared-memory size)
+  const int mtiles = (m + UM_BM - 1) / UM_BM;
+  long tiles = 0;
+  for (int i = 0; i < batch; i++) tiles += (ncols[i] + UM_BN - 1) / UM_BN;
+  tiles *= mtiles;
+  int tpc = (int)(tiles / (3L * kNumSM));
+  tpc = tpc < 1 ? 1 : (tpc > UM_MAX_TILES_PER_CTA ? UM_MAX_TILES_PER_CTA : tpc);
+  dim3 grid((nmax + tpc * UM_BN - 1) / (tpc * UM_BN), mtiles, batch);
   const float ar = (float)are, ai = (float)aim;
 #define CCL_UMMA(C, A_)                                                              \
   {                                                                                  \
     auto kern = k_umma_gemm<C, A_>;                                                  \
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    kern<<<grid, UM_THREADS, smem, s>>>(b, m, k, kp, ar, ai);                        \
+    static size_t set_smem = 0; /* the attribute is set once per size, not per launch */ \
+    if (set_smem < smem) {                                                           \
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+      set_smem = smem;                                                               \
+    }                                                                                \
+    kern<<<grid, UM_THREADS, smem, s>>>(b, m, k, kp, tpc, ar, ai);                   \
   }
   if (cplx) {
     if (beta == 1.0) CCL_UMMA(true, true) else CCL_UMMA(true, false)

@@ -69,15 +69,17 @@ class Communicator:
 
     ``precision='fp64'`` is the plain FP64 drop-in (double particles,
     complex128 fields).  ``precision='fp32'`` runs the same kernels in single
-    precision.  ``seed`` seeds the host generator of the plasma injector's
+    precision.  ``precision='mixed'`` is FP32 with the radial Hankel and
+    derivative GEMMs as BF16x3 split-precision products on the tensor cores
+    (FP32 accumulation).  ``seed`` seeds the host generator of the plasma injector's
     random draws.  Keyword arguments of the reference's OpenCL context choice
     (``answers``, ``interactive``) are accepted and ignored."""
 
     def __init__(self, precision="fp64", device=0, seed=0, verbose=False, **ctx_kw_args):
         _lib.require_cuda()
         _lib.load()
-        if precision not in ("fp64", "fp32"):
-            raise ValueError(f"precision must be 'fp64' or 'fp32', not {precision!r}")
+        if precision not in ("fp64", "fp32", "mixed"):
+            raise ValueError(f"precision must be 'fp64', 'fp32' or 'mixed', not {precision!r}")
         self.device = torch.device("cuda", device)
         torch.cuda.set_device(self.device)
         self.ctx = self.device
@@ -94,6 +96,7 @@ class Communicator:
         self.real = torch.float64 if precision == "fp64" else torch.float32
         self.cplx = torch.complex128 if precision == "fp64" else torch.complex64
         self.ccl = CCL_F64 if precision == "fp64" else CCL_F32
+        self.dht_impl = "bf16x3" if precision == "mixed" else "simt"
         # host<->device traffic issued by the methods (injector draws,
         # profile knots, lazy scalar reads), for end-to-end accounting
         self.h2d_bytes = 0

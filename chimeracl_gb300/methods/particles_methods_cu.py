@@ -137,13 +137,20 @@ class ParticleMethodsCU(GenericMethodsCU):
         Np = self.Args["Np"]
         C = grid.Args["Nxm1Nrm1"]
         dev, D = self.comm.device, self.DataDev
-        i32 = torch.int32
-        D["indx_in_cell"] = torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np]
-        D["sum_in_cell"] = torch.empty(C + 1, dtype=i32, device=dev)
-        D["cell_offset"] = torch.empty(C + 2, dtype=i32, device=dev)
-        D["sort_indx"] = torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np]
-        ws_bytes = sort_workspace_bytes(Np, C)
-        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        # buffers persist while Np and the grid are unchanged, so a step
+        # between window shifts allocates nothing (and can be graph-captured)
+        key = (Np, C)
+        bufs = getattr(self, "_sort_bufs", None)
+        if bufs is None or bufs[0] != key:
+            i32 = torch.int32
+            ws_bytes = sort_workspace_bytes(Np, C)
+            bufs = (key, torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np],
+                    torch.empty(C + 1, dtype=i32, device=dev),
+                    torch.empty(C + 2, dtype=i32, device=dev),
+                    torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np],
+                    torch.empty(ws_bytes, dtype=torch.uint8, device=dev), ws_bytes)
+            self._sort_bufs = bufs
+        _, D["indx_in_cell"], D["sum_in_cell"], D["cell_offset"], D["sort_indx"], ws, ws_bytes = bufs
         G = grid.Args
         call("ccl_index_sort", self._dt, Np, D["x"].data_ptr(), D["y"].data_ptr(),
              D["z"].data_ptr(), G["Nx"], float(G["Xmin"]), float(G["dx_inv"]), G["Nr"],

@@ -48,18 +48,51 @@ class TransformerMethodsCU(GenericMethodsCU):
         """The Hankel GEMM needs no preparation; matrices are uploaded by
         send_args_to_dev."""
 
-    def _dht(self, Y, A, X, ldx, ldy, ncols, cplx, alpha=1.0, beta=0.0, xoff=0, yoff=0):
-        """Y = beta*Y + alpha*(A X) on one matrix pair (offsets in elements of
-        the tensors' own dtype)."""
-        m = A.shape[0]
+    def _bf16x3(self, name):
+        """Split, tiled bf16 hi/lo form of a Hankel-type matrix for the
+        tensor-core GEMM (built once per matrix)."""
+        key = "_bf16x3_" + name
+        t = self.DataDev.get(key)
+        if t is None:
+            import ctypes
+            A = self.DataDev[name]
+            m, k = A.shape
+            nb = ctypes.c_size_t(0)
+            call("ccl_dht_bf16x3_prepare_bytes", m, k, ctypes.byref(nb))
+            t = torch.empty(nb.value, dtype=torch.uint8, device=self.comm.device)
+            call("ccl_dht_bf16x3_prepare", self._ccl_of(A), A.data_ptr(), m, k, t.data_ptr(),
+                 nb.value, stream())
+            self.DataDev[key] = t
+        return t
+
+    def _gemm(self, names, X, ldx, Y, ldy, ncols, cplx=False, alpha=1.0, beta=0.0):
+        """Y[i] = beta Y[i] + alpha (A[i] X[i]) for the matrices `names`
+        (pointers X, Y as ints), one launch: the BF16x3 tensor-core kernel in
+        the mixed form when k <= 256 and the rows are 16-byte aligned, else
+        the SIMT kernel in the compute precision."""
         a = complex(alpha)
+        m, k = self.DataDev[names[0]].shape
+        b = len(names)
+        if (self.comm.dht_impl == "bf16x3" and k <= 256
+                and all(p % 16 == 0 for p in X) and all(l % 4 == 0 for l in ldx)):
+            mats = [self._bf16x3(n) for n in names]
+            call("ccl_dht_bf16x3_gemm_batch", b, m, k, ints(ncols), int(cplx), PP(mats), PP(X),
+                 longs(ldx), PP(Y), longs(ldy), a.real, a.imag, float(beta), stream())
+        else:
+            mats = [self._real_dev(n) for n in names]
+            call("ccl_dht_gemm_batch", self._dt, b, m, k, ints(ncols), int(cplx), PP(mats), PP(X),
+                 longs(ldx), PP(Y), longs(ldy), a.real, a.imag, float(beta), stream())
+
+    def _dht(self, Y, A, X, ldx, ldy, ncols, cplx, alpha=1.0, beta=0.0, xoff=0, yoff=0):
+        """Y = beta*Y + alpha*(A X) on one matrix pair; A given by name
+        (offsets in elements of the tensors' own dtype)."""
         xp = X.data_ptr() + xoff * X.element_size()
         yp = Y.data_ptr() + yoff * Y.element_size()
-        call("ccl_dht_gemm", self._dt, 1, m, A.shape[1], ncols, int(cplx), PP([A]), PP([xp]), ldx,
-             PP([yp]), ldy, a.real, a.imag, float(beta), stream())
+        self._gemm([A], [xp], [ldx], [yp], [ldy], [ncols], cplx, alpha, beta)
 
     def _cdot(self, out, A, X):
-        """out = A X for a complex (Nr-1, Nx) field (the reference's _cdot)."""
+        """out = A X for a complex (Nr-1, Nx) field and the matrix named A
+        (the reference's _cdot)."""
         nx = X.shape[-1]
         self._dht(out, A, X, 2 * nx, 2 * nx, 2 * nx, True)
 
@@ -84,7 +117,7 @@ class TransformerMethodsCU(GenericMethodsCU):
                 f = None if filt is None else filt[m]
                 fptr = None if f is None else f.data_ptr()
                 if mode == "full":
-                    mat = self._real_dev("DHT_m" + s)
+                    mat = "DHT_m" + s
                     if m == 0:
                         buf = self.DataDev["fld_buff1_d"]
                         self._dht(buf, mat, rs, Nx, Nx, Nx, False, xoff=Nx)
@@ -99,7 +132,7 @@ class TransformerMethodsCU(GenericMethodsCU):
                          int(m == 0), sp.data_ptr(), phs.data_ptr(), fptr, stream())
             else:
                 if mode == "full":
-                    mat = self._real_dev("DHT_inv_m" + s)
+                    mat = "DHT_inv_m" + s
                     if m == 0:
                         buf = self.DataDev["fld_buff0_d"]
                         call("ccl_fft_backward_rows", self._dt, nrows, Nx, sp.data_ptr(),
@@ -148,10 +181,9 @@ class TransformerMethodsCU(GenericMethodsCU):
         if dir == 0:
             fl = [None if filt is None else filt[m] for _, m in ent]
             if mode == "full":
-                mats = [self._real_dev("DHT_m" + str(m)) for _, m in ent]
                 outg = [self._work(i, False) if m == 0 else sp[i] for i, (_, m) in enumerate(ent)]
-                call("ccl_dht_gemm_batch", self._dt, b, nrows, nrows, ints(ncol), 0, PP(mats),
-                     PP(rows1), longs(ncol), PP(outg), longs(ncol), 1.0, 0.0, 0.0, stream())
+                self._gemm(["DHT_m" + str(m) for _, m in ent], rows1, ncol,
+                           [t.data_ptr() for t in outg], ncol, ncol)
                 fin = outg
             else:
                 fin = rows1
@@ -162,9 +194,8 @@ class TransformerMethodsCU(GenericMethodsCU):
                 bufs = [self._work(i, m != 0) for i, (_, m) in enumerate(ent)]
                 call("ccl_fft_backward_batch", self._dt, b, nrows, Nx, PP(sp), PP(bufs),
                      longs([Nx] * b), ints(real), phs.data_ptr(), stream())
-                mats = [self._real_dev("DHT_inv_m" + str(m)) for _, m in ent]
-                call("ccl_dht_gemm_batch", self._dt, b, nrows, nrows, ints(ncol), 0, PP(mats),
-                     PP(bufs), longs(ncol), PP(rows1), longs(ncol), 1.0, 0.0, 0.0, stream())
+                self._gemm(["DHT_inv_m" + str(m) for _, m in ent],
+                           [t.data_ptr() for t in bufs], ncol, rows1, ncol, ncol)
             else:
                 call("ccl_fft_backward_batch", self._dt, b, nrows, Nx, PP(sp), PP(rows1),
                      longs([Nx] * b), ints(real), phs.data_ptr(), stream())
@@ -218,32 +249,39 @@ class TransformerMethodsCU(GenericMethodsCU):
              self.DataDev["buff_fb_m-1_" + comp].data_ptr(),
              self.DataDev[fld + "_fb_m1"].data_ptr(), stream())
 
+    def _products(self, terms):
+        """One batched GEMM launch: out_i = D_i X_i for the (matrix name, X)
+        pairs of ``terms`` (None entries skipped); returns the outputs in
+        order (None where the term is None)."""
+        A = self.Args
+        nx = A["Nx"]
+        live = [(i, t) for i, t in enumerate(terms) if t is not None]
+        outs = [None] * len(terms)
+        for k in range(0, len(live), MAX_BATCH):
+            part = live[k:k + MAX_BATCH]
+            bufs = [self._work(j, True) for j in range(k, k + len(part))]
+            self._gemm([t[0] for _, t in part], [t[1].data_ptr() for _, t in part],
+                       [2 * nx] * len(part), [b.data_ptr() for b in bufs], [2 * nx] * len(part),
+                       [2 * nx] * len(part))
+            for (i, _), b in zip(part, bufs):
+                outs[i] = b
+        return outs
+
     def field_grad(self, scl_in, vec_out):
-        """Spectral gradient (transformer_methods_cl.py:87-133)."""
+        """Spectral gradient (transformer_methods_cl.py:87-133): the
+        radial-derivative products of every mode in one batched GEMM, then one
+        combine kernel (i kx term, m=-1 mirror, mode coupling)."""
         A, D = self.Args, self.DataDev
         M = A["M"]
-        kx = self._real_dev("kx")
-        b0 = D["fld_buff0_c"]
-        self._get_mm1_scl(scl_in)
-        for m in range(M + 1):
-            s = str(m)
-            ox, oy, oz = (D[vec_out + c + "_fb_m" + s] for c in A["vec_comps"])
-            for o in (ox, oy, oz):
-                self.set_to(o, 0.0)
-            self.ab_dot_x(1j, kx, D[scl_in + "_fb_m" + s], ox)
-            if m > 0:
-                f = D[scl_in + "_fb_m" + str(m - 1)]
-            elif M > 0:
-                f = D["buff_fb_m-1_x"]
-            else:
-                continue
-            self._cdot(b0, self._real_dev("dDHT_minus_m" + s), f)
-            self.zpaxz(oy, -1.0, b0)
-            self.zpaxz(oz, -1.0j, b0)
-            if m < M:
-                self._cdot(b0, self._real_dev("dDHT_plus_m" + s), D[scl_in + "_fb_m" + str(m + 1)])
-                self.append_c2c(oy, b0)
-                self.zpaxz(oz, -1.0j, b0)
+        f = [D[scl_in + "_fb_m" + str(m)] for m in range(M + 1)]
+        pm = [(("dDHT_minus_m%d" % m), f[m - 1] if m > 0 else f[1])
+              if (m > 0 or M > 0) else None for m in range(M + 1)]
+        pp = [("dDHT_plus_m%d" % m, f[m + 1]) if m < M else None for m in range(M + 1)]
+        prods = self._products(pm + pp)
+        out = [D[vec_out + c + "_fb_m" + str(m)] for m in range(M + 1) for c in A["vec_comps"]]
+        call("ccl_grad_combine", self._dt, M, A["Nr"] - 1, A["Nx"],
+             self._real_dev("kx").data_ptr(), PP(f), PP(prods[:M + 1]), PP(prods[M + 1:]),
+             PP(out), stream())
 
     def field_div(self, vec_in, scl_out):
         """Spectral divergence (transformer_methods_cl.py:135-183)."""
@@ -265,47 +303,37 @@ class TransformerMethodsCU(GenericMethodsCU):
             else:
                 continue
             self.axpbyz(-1.0j, fz, -1.0, fy, b0)
-            self._cdot(b1, self._real_dev("dDHT_minus_m" + s), b0)
+            self._cdot(b1, "dDHT_minus_m" + s, b0)
             self.append_c2c(out, b1)
             if m < M:
                 fy, fz = D[vec_in + "y_fb_m" + str(m + 1)], D[vec_in + "z_fb_m" + str(m + 1)]
                 self.axpbyz(-1.0j, fz, 1.0, fy, b0)
-                self._cdot(b1, self._real_dev("dDHT_plus_m" + s), b0)
+                self._cdot(b1, "dDHT_plus_m" + s, b0)
                 self.append_c2c(out, b1)
 
-    def field_rot(self, fld_in, fld_out):
-        """Spectral curl (transformer_methods_cl.py:185-263)."""
+    def field_rot(self, fld_in, fld_out, poisson=False):
+        """Spectral curl (transformer_methods_cl.py:185-263): the
+        radial-derivative products of every mode and component in one batched
+        GEMM, then one combine kernel; with ``poisson`` the 1/w^2 factor of
+        field_poiss_vec is applied in the same pass."""
         A, D = self.Args, self.DataDev
         M = A["M"]
-        kx = self._real_dev("kx")
-        b0, b1 = D["fld_buff0_c"], D["fld_buff1_c"]
-        self._get_mm1_vec(fld_in)
+        comps = A["vec_comps"]
+        G = [D[fld_in + c + "_fb_m" + str(m)] for m in range(M + 1) for c in comps]
+        qm, qp = [], []
         for m in range(M + 1):
-            s = str(m)
-            ox, oy, oz = (D[fld_out + c + "_fb_m" + s] for c in A["vec_comps"])
-            for o in (ox, oy, oz):
-                self.set_to(o, 0.0)
-            self.ab_dot_x(-1.0j, kx, D[fld_in + "z_fb_m" + s], oy)
-            self.ab_dot_x(1.0j, kx, D[fld_in + "y_fb_m" + s], oz)
-            if m > 0:
-                fx, fy, fz = (D[fld_in + c + "_fb_m" + str(m - 1)] for c in A["vec_comps"])
-            elif M > 0:
-                fx, fy, fz = (D["buff_fb_m-1_" + c] for c in A["vec_comps"])
-            else:
-                continue
-            dm = self._real_dev("dDHT_minus_m" + s)
-            self.axpbyz(-1.0, fz, 1.0j, fy, b0)
-            self._cdot(b1, dm, b0)
-            self.append_c2c(ox, b1)
-            self._cdot(b0, dm, fx)
-            self.zpaxz(oy, -1.0j, b0)
-            self.zpaxz(oz, 1.0, b0)
-            if m < M:
-                fx, fy, fz = (D[fld_in + c + "_fb_m" + str(m + 1)] for c in A["vec_comps"])
-                dp = self._real_dev("dDHT_plus_m" + s)
-                self.axpbyz(1.0, fz, 1.0j, fy, b0)
-                self._cdot(b1, dp, b0)
-                self.append_c2c(ox, b1)
-                self._cdot(b0, dp, fx)
-                self.zpaxz(oy, -1.0j, b0)
-                self.zpaxz(oz, -1.0, b0)
+            for ci in range(3):
+                if m > 0:
+                    qm.append(("dDHT_minus_m%d" % m, G[3 * (m - 1) + ci]))
+                elif M > 0:
+                    qm.append(("dDHT_minus_m0", G[3 + ci]))  # G_{+1}, mirrored in the combine
+                else:
+                    qm.append(None)
+                qp.append(("dDHT_plus_m%d" % m, G[3 * (m + 1) + ci]) if m < M else None)
+        prods = self._products(qm + qp)
+        n = 3 * (M + 1)
+        out = [D[fld_out + c + "_fb_m" + str(m)] for m in range(M + 1) for c in comps]
+        poiss = PP([self._real_dev("Poiss_m" + str(m)) for m in range(M + 1)]) if poisson else None
+        call("ccl_rot_combine", self._dt, M, A["Nr"] - 1, A["Nx"],
+             self._real_dev("kx").data_ptr(), PP(G), PP(prods[:n]), PP(prods[n:]), poiss,
+             PP(out), stream())

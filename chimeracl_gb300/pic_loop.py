@@ -8,7 +8,13 @@ damping; B from G; backward transforms of E, B; gather + Boris push.
 
 With ``timit=True`` each phase is timed on the device with CUDA events under
 the reference's twelve phase names (device time, no host synchronisation
-inside the step; ``Timer`` is filled when read through ``timings()``)."""
+inside the step; ``Timer`` is filled when read through ``timings()``).
+
+With ``graphs=True`` the steps between window shifts -- which change no
+particle count and allocate nothing -- run as a CUDA graph: the first such
+step after a shift is captured, later ones replay it (the launch sequence of
+a step is ~150 kernels).  A signature of every device buffer and particle
+count guards the replay; anything that changes it is captured anew."""
 import numpy as np
 import torch
 
@@ -29,7 +35,7 @@ def timer_plot(Timer):
 
 class PIC_loop:
     def __init__(self, solvers=(), species=(), frames=(), diags=(), timit=False,
-                 fuse_smooth=True):
+                 fuse_smooth=True, graphs=False):
         self.solvers = list(solvers)
         self.mainsolver = self.solvers[0]
         self.species = list(species)
@@ -42,6 +48,11 @@ class PIC_loop:
         self.it = 0
         self.Timer = {k: 0.0 for k in loop_steps}
         self._events = []
+        self.graphs = graphs
+        self._graph = None
+        self._graph_sig = None
+        self.graph_replays = 0
+        self.graph_captures = 0
 
     def timer_start(self):
         if self.timit:
@@ -63,10 +74,44 @@ class PIC_loop:
             self._events = []
         return self.Timer
 
+    def _frame_due(self):
+        return any(np.mod(self.it, fr.Args["Steps"]) == 0 for fr in self.frames)
+
+    def _signature(self):
+        sig = []
+        for obj in list(self.solvers) + list(self.species):
+            for k, v in obj.DataDev.items():
+                if isinstance(v, torch.Tensor):
+                    sig.append((k, v.data_ptr(), v.numel()))
+            sig.append(obj.Args.get("Np", None) if hasattr(obj.Args, "get") else None)
+        for sol in self.solvers:
+            sig.append(float(sol.Args["Xmin"]))
+        return tuple(sig)
+
     def step(self):
         for diag in self.diags:
             diag.make_record(self.it)
+        use_graph = (self.graphs and not self.timit and not self.diags
+                     and not self._frame_due() and self.it > 0)
+        if not use_graph:
+            self._graph = None
+            self._body(graph_mode=False)
+        else:
+            sig = self._signature()
+            if self._graph is None or sig != self._graph_sig:
+                self._graph = None
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._body(graph_mode=True)
+                self._graph = g
+                self._graph_sig = self._signature()
+                self.graph_captures += 1
+            self._graph.replay()
+            self.graph_replays += 1
+        self.it += 1
+        return self.it
 
+    def _body(self, graph_mode):
         self.timer_start()
         for frame in self.frames:
             if np.mod(self.it, frame.Args["Steps"]) == 0:
@@ -113,14 +158,19 @@ class PIC_loop:
                 solver.fields_smooth(flds=["rho", "Jx", "Jy", "Jz"])
                 self.timer_record("smooth")
 
-            # dN0 <- dN1: the old gradient becomes N0 by exchanging buffers,
-            # and field_grad overwrites dN1 (pic_loop.py:106-111 copies)
+            # dN0 <- dN1 (pic_loop.py:106-111).  Eagerly the buffers are
+            # exchanged (field_grad overwrites dN1 entirely); a captured graph
+            # would freeze one exchange, so graph mode copies as the
+            # reference does.
             self.timer_start()
             D = solver.DataDev
             for m in range(M + 1):
                 for c in solver.Args["vec_comps"]:
                     s = c + "_fb_m" + str(m)
-                    D["dN0" + s], D["dN1" + s] = D["dN1" + s], D["dN0" + s]
+                    if graph_mode:
+                        D["dN0" + s].copy_(D["dN1" + s])
+                    else:
+                        D["dN0" + s], D["dN1" + s] = D["dN1" + s], D["dN0" + s]
             self.timer_record("data_copy")
 
             self.timer_start()
@@ -144,5 +194,3 @@ class PIC_loop:
 
         for parts in self.species:
             parts.free_mp()
-        self.it += 1
-        return self.it

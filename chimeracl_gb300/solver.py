@@ -44,9 +44,9 @@ class Solver(Grid, Transformer, SolverMethodsCU):
                  prof.data_ptr(), nf, stream())
 
     def restore_B_fb(self):
-        """B = rot(G) / w^2 in spectral space (solver.py:37-39)."""
-        self.field_rot("G", "B")
-        self.field_poiss_vec("B")
+        """B = rot(G) / w^2 in spectral space (solver.py:37-39); the 1/w^2
+        factor (field_poiss_vec) is applied in the curl's combine pass."""
+        self.field_rot("G", "B", poisson=True)
 
     def _make_ms_coefficients(self):
         """cos(w dt), sin(w dt) w and 1/w^2 per mode (solver.py:41-52), in

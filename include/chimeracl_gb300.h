@@ -251,6 +251,27 @@ int ccl_dht_gemm_batch(int dtype, int batch, int m, int k, const int *ncols,
                        double alpha_re, double alpha_im, double beta,
                        void *stream);
 
+/* BF16x3 form of the Hankel GEMM on the tensor cores (tcgen05, FP32
+ * accumulation), for FP32 operands: A = A_hi + A_lo and X = X_hi + X_lo in
+ * bf16, A X ~ A_hi X_hi + A_hi X_lo + A_lo X_hi (relative error ~1e-5).
+ * The constant matrix is split once: ccl_dht_bf16x3_prepare writes the
+ * split, tiled form of A (m x k, row-major, k <= 256, dtype CCL_F64 or
+ * CCL_F32) into `out` (ccl_dht_bf16x3_prepare_bytes bytes, 16-byte aligned).
+ * ccl_dht_bf16x3_gemm_batch then takes prepared matrices and the arguments
+ * of ccl_dht_gemm_batch (X rows 16-byte aligned: ldx % 4 == 0).
+ * ccl_dht_bf16x3_status returns (and with reset != 0 clears) the kernels'
+ * device error flag: 0 = ok, else a bounded wait gave up (the kernel then
+ * skipped its work and released its tensor memory).  It synchronises. */
+int ccl_dht_bf16x3_prepare_bytes(int m, int k, size_t *bytes);
+int ccl_dht_bf16x3_prepare(int dtype, const void *A, int m, int k, void *out,
+                           size_t bytes, void *stream);
+int ccl_dht_bf16x3_gemm_batch(int batch, int m, int k, const int *ncols,
+                              int cplx, const void *const *A_prepared,
+                              const void *const *X, const long *ldx,
+                              void *const *Y, const long *ldy, double alpha_re,
+                              double alpha_im, double beta, void *stream);
+int ccl_dht_bf16x3_status(int reset);
+
 /* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
  * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,
  * dN0_x..z, dN1_x..z; c1 = cos(w dt), c2 = sin(w dt) w, c3 = 1/w^2 (real).
@@ -265,6 +286,27 @@ int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
  * transformer_generic.cl:3-24). */
 int ccl_get_m1(int dtype, int nrows, int nx, void *out, const void *in,
                void *stream);
+
+/* Combine step of the spectral gradient (field_grad,
+ * transformer_methods_cl.py:87-133) for all modes at once, given the radial
+ * derivative products from one batched GEMM: Pm[m] = dDHT_minus_m rho_{m-1}
+ * (for m = 0: dDHT_minus_0 rho_{+1}, taken through the m=-1 mirror here),
+ * Pp[m] = dDHT_plus_m rho_{m+1}; entries NULL where absent (host arrays of
+ * M+1 device pointers, or NULL).  Writes dN[3m+c] = (i kx rho_m,
+ * -T- + T+, -i(T- + T+)), c = x, y, z (complex (nrows, nx)). */
+int ccl_grad_combine(int dtype, int M, int nrows, int nx, const void *kx,
+                     const void *const *rho, const void *const *Pm,
+                     const void *const *Pp, void *const *dN, void *stream);
+
+/* Combine step of the spectral curl (field_rot,
+ * transformer_methods_cl.py:185-263) for all modes, given the products
+ * Qm[3m+c] = dDHT_minus_m G_{c,m-1} (m = 0: of G_{c,+1}, mirrored here) and
+ * Qp[3m+c] = dDHT_plus_m G_{c,m+1}; poiss (M+1 real arrays, or NULL)
+ * multiplies the result by 1/w^2 (field_poiss_vec, :66-71).  Writes B[3m+c]. */
+int ccl_rot_combine(int dtype, int M, int nrows, int nx, const void *kx,
+                    const void *const *G, const void *const *Qm,
+                    const void *const *Qp, const void *const *poiss,
+                    void *const *B, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Elementwise  (chimeraCL/methods/generic_methods_cl.py, generic.cl)  */

@@ -78,3 +78,24 @@ def test_density_profile_injection(cuda):
     _sort_equal(e, oe)
     assert compare_fields(sol, osol, dens=cfg["eons_in"]["dens"]) < 1e-11
     _particles_equal(e, oe, tol=1e-11)
+
+
+def test_graph_replay_matches_eager(cuda):
+    """Steps between window shifts replayed as a CUDA graph give exactly the
+    eager steps' result (same kernels, same inputs)."""
+    cfg = small_lpa(Nx=128, Nr=32, M=1, seed=23, steps=10)
+    runs = []
+    for graphs in (False, True):
+        sol, e, i, loop = build_product(cfg, precision="fp64")
+        loop.graphs = graphs
+        for _ in range(24):
+            loop.step()
+        torch.cuda.synchronize()
+        runs.append((sol, e, loop))
+    (s0, e0, l0), (s1, e1, l1) = runs
+    assert l1.graph_replays >= 18 and l1.graph_captures >= 2
+    for k, v in s0.DataDev.items():
+        if isinstance(v, torch.Tensor) and not k.startswith(("_", "buff_fb", "phs", "fld_buff")):
+            assert torch.equal(v, s1.DataDev[k]), k
+    for k in ("x", "y", "z", "px", "py", "pz", "g_inv", "w"):
+        assert torch.equal(e0.DataDev[k], e1.DataDev[k]), k
