@@ -304,6 +304,7 @@ def time_arm(cfg, precision, steps, warmup, device_index, dist):
         dist.barrier()
     torch.cuda.synchronize()
     n0 = _lib.launch_count()
+    c0, r0 = loop.graph_kernels_captured, loop.graph_kernels_replayed
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(device_index) as clk:
         time.sleep(0.3)  # let the sampler start before the timed region
@@ -316,7 +317,9 @@ def time_arm(cfg, precision, steps, warmup, device_index, dist):
     if dist:
         dist.barrier()
     ms = e0.elapsed_time(e1)
-    launches = _lib.launch_count() - n0
+    # library kernels that ran: launched eagerly, or replayed from a graph
+    launches = (_lib.launch_count() - n0 - (loop.graph_kernels_captured - c0)
+                + (loop.graph_kernels_replayed - r0))
     return dict(solver=solver, eons=eons, ions=ions, loop=loop, ms=ms, np_sum=np_sum,
                 launches=launches, clocks=clk.summary())
 

@@ -53,6 +53,11 @@ class PIC_loop:
         self._graph_sig = None
         self.graph_replays = 0
         self.graph_captures = 0
+        # library kernels per captured step, and totals captured / replayed
+        # (a replay runs the captured kernels without launching them again)
+        self._graph_kernels = 0
+        self.graph_kernels_captured = 0
+        self.graph_kernels_replayed = 0
 
     def timer_start(self):
         if self.timit:
@@ -100,14 +105,19 @@ class PIC_loop:
             sig = self._signature()
             if self._graph is None or sig != self._graph_sig:
                 self._graph = None
+                from . import _lib
+                n0 = _lib.launch_count()
                 g = torch.cuda.CUDAGraph()
                 with torch.cuda.graph(g):
                     self._body(graph_mode=True)
+                self._graph_kernels = _lib.launch_count() - n0
                 self._graph = g
                 self._graph_sig = self._signature()
                 self.graph_captures += 1
+                self.graph_kernels_captured += self._graph_kernels
             self._graph.replay()
             self.graph_replays += 1
+            self.graph_kernels_replayed += self._graph_kernels
         self.it += 1
         return self.it
 
