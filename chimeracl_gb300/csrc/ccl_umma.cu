@@ -5,39 +5,29 @@
 // A real (m x k, k <= 256), X FP32 (k x ncols real columns, interleaved
 // complex allowed), Y FP32.
 //
-// CTA = 128 threads (one warpgroup), one 128-row M tile of one batch entry
-// and a run of 64-column N tiles.  The pre-split A tile (hi then lo, K-major,
-// no-swizzle core-matrix layout, produced by k_umma_split_a) is copied once
-// into shared memory and stays resident.  X is staged per 128-deep K chunk:
-// each thread loads one 8 (k) x 8 (n) block of FP32, splits it and writes
-// one K-major 8x8 bf16 core matrix for X_hi and one for X_lo.  Two X
-// buffers and two TMEM accumulators (128 lanes x 64 columns each) let thread
-// 0 issue the next chunk's MMAs while the others stage and drain.  Every
-// mbarrier wait is bounded; a wait that gives up records an error code in a
-// device flag, the CTA skips the rest of its work, drains what it issued
-// (bounded) and frees its TMEM.
+// The pre-split A (hi then lo per 128-row tile, K-major, no-swizzle
+// core-matrix layout, produced by k_umma_split_a) is bulk-copied into shared
+// memory and stays resident while a CTA walks its N tiles; X is split into
+// bf16 hi/lo on the fly.  Every mbarrier wait is bounded; a wait that gives up
+// records an error code in a device flag, the CTA skips the rest of its work,
+// drains what it issued (bounded) and frees its TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "ccl_common.cuh"
 #include "ccl_launch.h"
 
 namespace ccl {
 
-constexpr int UM_THREADS = 128, UM_BM = 128, UM_BN = 64, UM_BK = 128;
+constexpr int UM_BM = 128, UM_BK = 128;
 constexpr int UM_MAXK = 256, UM_MAXBATCH = 32;
-constexpr int UM_MAX_TILES_PER_CTA = 4;
 constexpr long UM_SPIN_LIMIT = 20000000L;  // ~ a second of try_wait polls
 
 __device__ int g_umma_error = 0;
-
-struct UmmaBatch {
-  const void *A[UM_MAXBATCH];  // pre-split A tiles
-  const float *X[UM_MAXBATCH];
-  float *Y[UM_MAXBATCH];
-  int ncols[UM_MAXBATCH];
-  long ldx[UM_MAXBATCH], ldy[UM_MAXBATCH];
-};
 
 // bytes of one pre-split M tile: hi and lo, 128 rows x kp columns of bf16
 __host__ __device__ constexpr long umma_tile_bytes(int kp) { return 2L * UM_BM * kp * 2; }
@@ -170,196 +160,384 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int kp, i
 }
 
 // ---------------------------------------------------------------- GEMM
+// Persistent, warp-specialised kernel.  Work item = (batch entry e, 128-row
+// M tile mt, 128-column N tile nt), ordered (e, mt, nt); CTA c takes a
+// contiguous run of items, so the resident A tile is reloaded only when
+// (e, mt) changes (one bulk copy into shared memory).
+//   warps 0-3  epilogue: TMEM lanes 32w..32w+31 (= output rows) -> alpha,
+//              optional +Y, row-contiguous stores
+//   warps 4-11 converters: raw FP32 stage (32 k x 128 n) -> K-major bf16
+//              hi/lo core matrices in a ring of UM_NS slots.  They issue no
+//              global loads, so their proxy fence has nothing to drain.
+//   warp 12    lane 0: TMA producer, one 2-D tensor copy per stage into a
+//              ring of UM_NR raw slots (out-of-range rows/columns read as 0)
+//   warp 13    lane 0: A bulk copies and the MMAs (3 per 16-deep k step),
+//              double-buffered 128 x 128 FP32 accumulators in TMEM
+// Every wait is bounded (and gives up early once another role has aborted);
+// the MMA thread drains its MMAs and the producer its copies before the CTA
+// releases TMEM and exits.
+constexpr int UM_EPI_WARPS = 4, UM_CVT_WARPS = 8;
+constexpr int UM_THREADS2 = (UM_EPI_WARPS + UM_CVT_WARPS + 2) * 32;  // 448
+constexpr int UM_TN = 128;        // N tile (columns of X / Y)
+constexpr int UM_KC = 32;         // K depth of one stage
+constexpr int UM_NS = 2;          // bf16 slots
+constexpr int UM_NR = 4;          // raw FP32 slots
+constexpr uint32_t UM_SLOT = 2u * UM_KC * UM_TN * 2;  // hi + lo bf16: 16 KB
+constexpr uint32_t UM_RAW = (uint32_t)UM_KC * UM_TN * 4;  // FP32: 16 KB
+constexpr int UM_CVT_THREADS = UM_CVT_WARPS * 32;
+
+struct UmmaWork {
+  const void *A[UM_MAXBATCH];
+  float *Y[UM_MAXBATCH];
+  int ncols[UM_MAXBATCH];
+  int ntn[UM_MAXBATCH];    // N tiles of the entry
+  int base[UM_MAXBATCH];   // first item of the entry
+  long ldy[UM_MAXBATCH];
+  int batch, items, mtiles;
+};
+
+// X of every entry as a 2-D tensor map (inner dim = columns, box 128 x 32)
+struct UmmaArgs {
+  CUtensorMap tx[UM_MAXBATCH];
+  UmmaWork w;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// 2-D tiled tensor copy global -> shared; x (columns) must be a multiple of
+// 4 floats (16 bytes), which every N tile origin is
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// bounded wait that also gives up once `abort` is set by another role
+__device__ __forceinline__ bool mbar_wait_ab(uint64_t *bar, uint32_t parity,
+                                             volatile int *abort) {
+  for (long i = 0; i < UM_SPIN_LIMIT; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 255 && *abort) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void um_fail(volatile int *abort, int code) {
+  if (!*abort) atomicCAS(&g_umma_error, 0, code);
+  *abort = 1;
+}
+
+__device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, int &mt,
+                                          int &nt) {
+  e = 0;
+  while (e + 1 < w.batch && w.base[e + 1] <= item) e++;
+  const int r = item - w.base[e];
+  mt = r / w.ntn[e];
+  nt = r - mt * w.ntn[e];
+}
+
+// converter: k rows kb*8 .. +7, columns n, n+1 of a raw stage -> one core
+// matrix row (8 k values) of hi and of lo for each column; core matrix
+// (gn = n/8, kb) at (gn*4 + kb)*128, row n%8; hi block, then lo block
+__device__ __forceinline__ void cvt_stage(const float *raw, unsigned char *slot, int kb,
+                                          int ncol_local, uint4 (&o)[4]) {
+  __nv_bfloat16 h[2][8], l[2][8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const float2 t = *(const float2 *)(raw + (kb * 8 + q) * UM_TN + ncol_local);
+    h[0][q] = __float2bfloat16_rn(t.x);
+    h[1][q] = __float2bfloat16_rn(t.y);
+    l[0][q] = __float2bfloat16_rn(t.x - __bfloat162float(h[0][q]));
+    l[1][q] = __float2bfloat16_rn(t.y - __bfloat162float(h[1][q]));
+  }
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    o[2 * c] = {pack_bf16(h[c][0], h[c][1]), pack_bf16(h[c][2], h[c][3]),
+                pack_bf16(h[c][4], h[c][5]), pack_bf16(h[c][6], h[c][7])};
+    o[2 * c + 1] = {pack_bf16(l[c][0], l[c][1]), pack_bf16(l[c][2], l[c][3]),
+                    pack_bf16(l[c][4], l[c][5]), pack_bf16(l[c][6], l[c][7])};
+  }
+}
+
 template <bool CPLX, bool ACC>
-__global__ void __launch_bounds__(UM_THREADS, 1)
-    k_umma_gemm(UmmaBatch b, int M, int K, int KP, int tiles_per_cta, float are, float aim) {
+__global__ void __launch_bounds__(UM_THREADS2, 1)
+    k_umma_gemm(const __grid_constant__ UmmaArgs args, int M, int K, int KP, int vec_y,
+                float are, float aim) {
   extern __shared__ __align__(1024) unsigned char smraw[];
+  const UmmaWork &w = args.w;
   unsigned char *sm = (unsigned char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  unsigned char *sA = sm;                                   // umma_tile_bytes(KP)
-  unsigned char *sX = sA + umma_tile_bytes(KP);             // 2 stages x 32 KB
-  uint64_t *bar = (uint64_t *)(sX + 2 * 2 * UM_BK * UM_BN * 2);  // [2]
-  uint32_t *tmem_slot = (uint32_t *)(bar + 2);
-  int *abort_flag = (int *)(tmem_slot + 1);
-  int *last_issued = abort_flag + 1;  // last stage whose MMAs were committed
+  const uint32_t a_bytes = (uint32_t)umma_tile_bytes(KP);
+  unsigned char *sA = sm;
+  unsigned char *sX = sA + a_bytes;       // UM_NS bf16 slots
+  unsigned char *sR = sX + UM_NS * UM_SLOT;  // UM_NR raw slots
+  uint64_t *full = (uint64_t *)(sR + UM_NR * UM_RAW);
+  uint64_t *empty = full + UM_NS;
+  uint64_t *rfull = empty + UM_NS;
+  uint64_t *rempty = rfull + UM_NR;
+  uint64_t *tfull = rempty + UM_NR;  // [2]
+  uint64_t *tempty = tfull + 2;      // [2]
+  uint64_t *abar = tempty + 2;
+  uint64_t *dbar = abar + 1;
+  uint32_t *tmem_slot = (uint32_t *)(dbar + 1);
+  volatile int *abort = (volatile int *)(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int e = blockIdx.z, mt = blockIdx.y;
-  const int N = b.ncols[e];
-  const int n_begin = blockIdx.x * tiles_per_cta * UM_BN;
-  if (n_begin >= N) return;
-  const int ntiles = min(tiles_per_cta, (N - n_begin + UM_BN - 1) / UM_BN);
-  const int nkc = KP / UM_BK;
-  const float *__restrict__ X = b.X[e];
-  float *__restrict__ Y = b.Y[e];
-  const long ldx = b.ldx[e], ldy = b.ldy[e];
+  const int nkc = (K + UM_KC - 1) / UM_KC;
+  const int i0 = (int)((long)blockIdx.x * w.items / gridDim.x);
+  const int i1 = (int)((long)(blockIdx.x + 1) * w.items / gridDim.x);
+  const int S = (i1 - i0) * nkc;  // stages of this CTA
 
-  // TMEM: 2 accumulators of 64 columns
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
         smem_u32(tmem_slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    *abort_flag = 0;
-    *last_issued = -1;
+    for (int i = 0; i < UM_NS; i++) {
+      mbar_init(&full[i], UM_CVT_THREADS);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < UM_NR; i++) {
+      mbar_init(&rfull[i], 1);
+      mbar_init(&rempty[i], UM_CVT_THREADS);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], UM_EPI_WARPS * 32);
+    }
+    mbar_init(abar, 1);
+    mbar_init(dbar, 1);
+    *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // resident A tile
-  {
-    const uint4 *src = (const uint4 *)((const unsigned char *)b.A[e] + mt * umma_tile_bytes(KP));
-    uint4 *dst = (uint4 *)sA;
-    const int n16 = (int)(umma_tile_bytes(KP) / 16);
-    for (int i = tid; i < n16; i += UM_THREADS) dst[i] = src[i];
-  }
-  fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t idesc = umma_idesc(UM_BM, UM_BN);
-  const uint32_t sA_u = smem_u32(sA), sX_u = smem_u32(sX);
-  const uint32_t a_lo_off = (uint32_t)(umma_tile_bytes(KP) / 2);
-  const uint32_t a_sbo = (uint32_t)(KP / 8) * 128;
-  const uint32_t x_stage = 2 * UM_BK * UM_BN * 2, x_lo_off = UM_BK * UM_BN * 2;
-  const uint32_t x_sbo = (UM_BK / 8) * 128;
-  bool ok = true;
 
-  // thread's 8x8 staging block within a 128 (k) x 64 (n) chunk
-  const int nb = tid & 7, kb = tid >> 3;
-
-  auto epilogue = [&](int t) {
-    const int st_last = t * nkc + nkc - 1;
-    bool got = mbar_wait(&bar[st_last & 1], (st_last >> 1) & 1);
-    if (!got) {
-      atomicExch(&g_umma_error, 2);
-      *abort_flag = 1;
-    }
-    tc_fence_after();
-    const int gm = mt * UM_BM + warp * 32 + lane;
-    const int n0 = n_begin + t * UM_BN;
-    const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((t & 1) * UM_BN);
-#pragma unroll
-    for (int q = 0; q < UM_BN / 16; q++) {
-      float v[16];
-      tmem_ld16(tbase + q * 16, v);
-      tmem_wait_ld();
-      if (got && gm < M) {
-        float *yrow = Y + (long)gm * ldy;
-#pragma unroll
-        for (int c = 0; c < 16; c += 2) {
-          const int gn = n0 + q * 16 + c;
-          if (gn >= N) break;
-          float r0, r1;
-          if (CPLX) {
-            r0 = are * v[c] - aim * v[c + 1];
-            r1 = are * v[c + 1] + aim * v[c];
-          } else {
-            r0 = are * v[c];
-            r1 = are * v[c + 1];
-          }
-          if (ACC) {
-            r0 += yrow[gn];
-            if (gn + 1 < N) r1 += yrow[gn + 1];
-          }
-          yrow[gn] = r0;
-          if (gn + 1 < N) yrow[gn + 1] = r1;
-        }
+  if (warp < UM_EPI_WARPS) {
+    // ------------------------------------------------------------ epilogue
+    // tcgen05.ld is warp-collective: every exit decision is taken warp-wide
+    for (int j = 0, item = i0; item < i1; j++, item++) {
+      if (__any_sync(0xffffffffu, *abort)) break;
+      int e, mt, nt;
+      um_decode(w, item, e, mt, nt);
+      const int b = j & 1;
+      const bool got = mbar_wait_ab(&tfull[b], (j >> 1) & 1, abort);
+      if (!__all_sync(0xffffffffu, got)) {
+        um_fail(abort, 2);
+        break;
       }
-    }
-    tc_fence_before();
-  };
-
-  const int S = ntiles * nkc;
-  for (int st = 0; st < S; st++) {
-    const int buf = st & 1, t = st / nkc, kc = st - t * nkc;
-    if (st >= 2 && tid == 0) {
-      if (!mbar_wait(&bar[buf], ((st - 2) >> 1) & 1)) {
-        atomicExch(&g_umma_error, 1);
-        *abort_flag = 1;
-      }
-    }
-    __syncthreads();
-    if (*abort_flag) { ok = false; break; }
-    // stage X chunk: rows kc*128 + kb*8 + r, columns n_begin + t*64 + nb*8 + c
-    {
-      float v[8][8];
-      const int n = n_begin + t * UM_BN + nb * 8;
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        const int kk = kc * UM_BK + kb * 8 + r;
-        const float *row = X + (long)kk * ldx + n;
-        if (kk < K && n + 8 <= N) {
-          float4 p = *(const float4 *)row, q = *(const float4 *)(row + 4);
-          v[r][0] = p.x; v[r][1] = p.y; v[r][2] = p.z; v[r][3] = p.w;
-          v[r][4] = q.x; v[r][5] = q.y; v[r][6] = q.z; v[r][7] = q.w;
-        } else {
-#pragma unroll
-          for (int c = 0; c < 8; c++) v[r][c] = (kk < K && n + c < N) ? row[c] : 0.f;
-        }
-      }
-      unsigned char *dst_hi = sX + buf * x_stage + (nb * (UM_BK / 8) + kb) * 128;
-      unsigned char *dst_lo = dst_hi + x_lo_off;
-#pragma unroll
-      for (int c = 0; c < 8; c++) {  // core-matrix row = column n of the block
-        __nv_bfloat16 h[8], l[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          h[r] = __float2bfloat16_rn(v[r][c]);
-          l[r] = __float2bfloat16_rn(v[r][c] - __bfloat162float(h[r]));
-        }
-        uint4 ph = {pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]),
-                    pack_bf16(h[6], h[7])};
-        uint4 pl = {pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]),
-                    pack_bf16(l[6], l[7])};
-        *(uint4 *)(dst_hi + c * 16) = ph;
-        *(uint4 *)(dst_lo + c * 16) = pl;
-      }
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
       tc_fence_after();
-      const uint32_t d = tmem + (uint32_t)((t & 1) * UM_BN);
-      const uint32_t xs = sX_u + buf * x_stage;
+      const int N = w.ncols[e];
+      const int gm = mt * UM_BM + warp * 32 + lane;
+      const int n0 = nt * UM_TN;
+      float *__restrict__ yrow = w.Y[e] + (long)gm * w.ldy[e];
+      const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * UM_TN);
+#pragma unroll 1
+      for (int q = 0; q < UM_TN / 32; q++) {
+        float v[32];
+        tmem_ld16(tb + q * 32, v);
+        tmem_ld16(tb + q * 32 + 16, v + 16);
+        tmem_wait_ld();
+        if (gm < M) {
+          const int c0 = n0 + q * 32;
+          if (vec_y && c0 + 32 <= N) {
 #pragma unroll
-      for (int ks = 0; ks < UM_BK / 16; ks++) {
-        const uint32_t ja = (uint32_t)(kc * (UM_BK / 8) + 2 * ks) * 128;
-        const uint64_t ahi = smem_desc(sA_u + ja, 128, a_sbo);
-        const uint64_t alo = smem_desc(sA_u + a_lo_off + ja, 128, a_sbo);
-        const uint64_t bhi = smem_desc(xs + (uint32_t)(2 * ks) * 128, 128, x_sbo);
-        const uint64_t blo = smem_desc(xs + x_lo_off + (uint32_t)(2 * ks) * 128, 128, x_sbo);
-        umma_bf16(d, ahi, bhi, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
-        umma_bf16(d, ahi, blo, idesc, 1u);
-        umma_bf16(d, alo, bhi, idesc, 1u);
+            for (int c = 0; c < 32; c += 4) {
+              float4 r;
+              if (CPLX) {
+                r.x = are * v[c] - aim * v[c + 1];
+                r.y = are * v[c + 1] + aim * v[c];
+                r.z = are * v[c + 2] - aim * v[c + 3];
+                r.w = are * v[c + 3] + aim * v[c + 2];
+              } else {
+                r.x = are * v[c];
+                r.y = are * v[c + 1];
+                r.z = are * v[c + 2];
+                r.w = are * v[c + 3];
+              }
+              if (ACC) {
+                const float4 o = *(const float4 *)(yrow + c0 + c);
+                r.x += o.x; r.y += o.y; r.z += o.z; r.w += o.w;
+              }
+              *(float4 *)(yrow + c0 + c) = r;
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 32; c += 2) {
+              const int gn = c0 + c;
+              if (gn >= N) break;
+              float r0, r1;
+              if (CPLX) {
+                r0 = are * v[c] - aim * v[c + 1];
+                r1 = are * v[c + 1] + aim * v[c];
+              } else {
+                r0 = are * v[c];
+                r1 = are * v[c + 1];
+              }
+              if (ACC) {
+                r0 += yrow[gn];
+                if (gn + 1 < N) r1 += yrow[gn + 1];
+              }
+              yrow[gn] = r0;
+              if (gn + 1 < N) yrow[gn + 1] = r1;
+            }
+          }
+        }
       }
-      umma_commit(&bar[buf]);
-      *last_issued = st;
+      tc_fence_before();
+      mbar_arrive(&tempty[b]);
     }
-    if (kc == 0 && t >= 1) {
-      epilogue(t - 1);
-      __syncthreads();
+  } else if (warp < UM_EPI_WARPS + UM_CVT_WARPS) {
+    // ---------------------------------------------------------- converters
+    const int ct = tid - UM_EPI_WARPS * 32;
+    const int cw = ct >> 5;
+    const int kb = cw >> 1;                              // k block 0..3
+    const int ncol_local = 2 * ((cw & 1) * 32 + lane);   // 0..126
+    const uint32_t o0 = (uint32_t)(((ncol_local >> 3) * (UM_KC / 8) + kb) * 128 +
+                                   (ncol_local & 7) * 16);
+    for (int s = 0; s < S; s++) {
+      if (*abort) break;
+      const int r = s % UM_NR, slot = s % UM_NS;
+      if (!mbar_wait_ab(&rfull[r], (s / UM_NR) & 1, abort)) {
+        um_fail(abort, 7);
+        break;
+      }
+      uint4 o[4];
+      cvt_stage((const float *)(sR + r * UM_RAW), sX + slot * UM_SLOT, kb, ncol_local, o);
+      // the raw slot's values are consumed; the next tensor copy into it
+      // (async proxy) must not overtake these generic-proxy reads, and the
+      // barrier's release alone does not order across proxies
+      fence_async_smem();
+      mbar_arrive(&rempty[r]);
+      if (s >= UM_NS && !mbar_wait_ab(&empty[slot], ((s / UM_NS) - 1) & 1, abort)) {
+        um_fail(abort, 1);
+        break;
+      }
+      unsigned char *dst = sX + slot * UM_SLOT + o0;
+      *(uint4 *)(dst) = o[0];              // column n: hi
+      *(uint4 *)(dst + UM_SLOT / 2) = o[1];  //           lo
+      *(uint4 *)(dst + 16) = o[2];         // column n+1 (next core-matrix row)
+      *(uint4 *)(dst + 16 + UM_SLOT / 2) = o[3];
+      fence_async_smem();
+      mbar_arrive(&full[slot]);
     }
+  } else if (warp == UM_EPI_WARPS + UM_CVT_WARPS) {
+    // ------------------------------------------------- TMA producer (one lane)
+    if (lane == 0) {
+      int issued = 0;
+      for (int s = 0; s < S; s++) {
+        if (*abort) break;
+        const int r = s % UM_NR;
+        if (s >= UM_NR && !mbar_wait_ab(&rempty[r], ((s / UM_NR) - 1) & 1, abort)) {
+          um_fail(abort, 8);
+          break;
+        }
+        int e, mt, nt;
+        um_decode(w, i0 + s / nkc, e, mt, nt);
+        mbar_expect_tx(&rfull[r], UM_RAW);
+        tma_load_2d(sR + r * UM_RAW, &args.tx[e], nt * UM_TN, (s % nkc) * UM_KC, &rfull[r]);
+        issued = s + 1;
+      }
+      // every copy this lane issued has landed before the CTA may exit
+      for (int s = issued - UM_NR < 0 ? 0 : issued - UM_NR; s < issued; s++)
+        (void)mbar_wait(&rfull[s % UM_NR], (s / UM_NR) & 1);
+    }
+  } else if (lane == 0) {
+    // ------------------------------------------------------ MMA (one lane)
+    const uint32_t idesc = umma_idesc(UM_BM, UM_TN);
+    const uint32_t sA_u = smem_u32(sA), sX_u = smem_u32(sX);
+    const uint32_t a_sbo = (uint32_t)(KP / 8) * 128, a_lo = a_bytes / 2;
+    const uint32_t x_sbo = (UM_KC / 8) * 128;
+    int a_key = -1, a_phase = 0, d_phase = 0, s = 0;
+    bool issued = false;
+    for (int j = 0, item = i0; item < i1; j++, item++) {
+      if (*abort) break;
+      int e, mt, nt;
+      um_decode(w, item, e, mt, nt);
+      const int key = e * 1024 + mt;
+      if (key != a_key) {
+        if (issued) {  // every MMA reading the old tile has completed
+          umma_commit(dbar);
+          if (!mbar_wait_ab(dbar, d_phase & 1, abort)) { um_fail(abort, 3); break; }
+          d_phase++;
+          issued = false;
+        }
+        const unsigned char *src = (const unsigned char *)w.A[e] + (long)mt * a_bytes;
+        mbar_expect_tx(abar, a_bytes);
+        for (uint32_t off = 0; off < a_bytes; off += 32768u)
+          bulk_g2s(sA + off, src + off, min(32768u, a_bytes - off), abar);
+        // the copy must land before anything else happens in this CTA
+        if (!mbar_wait(abar, a_phase & 1)) { um_fail(abort, 4); break; }
+        a_phase++;
+        a_key = key;
+      }
+      const int b = j & 1;
+      if (j >= 2 && !mbar_wait_ab(&tempty[b], ((j - 2) >> 1) & 1, abort)) {
+        um_fail(abort, 5);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t)(b * UM_TN);
+      bool ok = true;
+      for (int kc = 0; kc < nkc; kc++, s++) {
+        const int slot = s % UM_NS;
+        if (!mbar_wait_ab(&full[slot], (s / UM_NS) & 1, abort)) {
+          um_fail(abort, 6);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t xs = sX_u + slot * UM_SLOT;
+#pragma unroll
+        for (int ks = 0; ks < UM_KC / 16; ks++) {
+          const uint32_t ja = (uint32_t)(kc * (UM_KC / 8) + 2 * ks) * 128;
+          const uint64_t ahi = smem_desc(sA_u + ja, 128, a_sbo);
+          const uint64_t alo = smem_desc(sA_u + a_lo + ja, 128, a_sbo);
+          const uint64_t bhi = smem_desc(xs + (uint32_t)(2 * ks) * 128, 128, x_sbo);
+          const uint64_t blo = smem_desc(xs + UM_SLOT / 2 + (uint32_t)(2 * ks) * 128, 128, x_sbo);
+          umma_bf16(d, ahi, bhi, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+          umma_bf16(d, ahi, blo, idesc, 1u);
+          umma_bf16(d, alo, bhi, idesc, 1u);
+        }
+        umma_commit(&empty[slot]);
+        issued = true;
+      }
+      if (!ok) break;
+      umma_commit(&tfull[b]);
+    }
+    // drain: whatever was issued completes before TMEM is released
+    umma_commit(dbar);
+    (void)mbar_wait(dbar, d_phase & 1);
   }
-  if (ok) {
-    epilogue(ntiles - 1);
-  } else if (tid == 0) {
-    // drain: the MMAs of the last committed stage (bounded) before TMEM is
-    // released; the stages before it completed in issue order
-    const int li = *last_issued;
-    if (li >= 0) (void)mbar_wait(&bar[li & 1], (li >> 1) & 1);
-  }
+  __syncwarp();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
 }
 
 static size_t umma_smem(int kp) {
-  return 1024 + umma_tile_bytes(kp) + 2 * 2 * UM_BK * UM_BN * 2 + 64;
+  return 1024 + umma_tile_bytes(kp) + UM_NS * UM_SLOT + UM_NR * UM_RAW + 256;
 }
 
 size_t umma_split_bytes(int m, int k) {
@@ -384,6 +562,30 @@ int umma_split_a(const TA *A, int m, int k, void *out, size_t bytes, cudaStream_
   return CCL_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); looked up once
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+static int device_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return kNumSM;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    return kNumSM;
+  return n;
+}
+
 int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const void *const *Ap,
                     const void *const *X, const long *ldx, void *const *Y, const long *ldy,
                     double are, double aim, double beta, cudaStream_t s) {
@@ -392,38 +594,55 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
               "umma: m=%d k=%d (k <= %d)", m, k, UM_MAXK);
   CCL_REQUIRE(beta == 0.0 || beta == 1.0, CCL_ERR_ARG, "umma: beta must be 0 or 1");
   if (batch == 0) return CCL_OK;
-  UmmaBatch b;
-  int nmax = 0;
+  static UmmaArgs args;  // host staging of the kernel parameters
+  static std::mutex args_mu;
+  std::lock_guard<std::mutex> lock(args_mu);
+  UmmaWork &w = args.w;
+  auto encode = encode_tiled();
+  CCL_REQUIRE(encode, CCL_ERR_CUDA, "umma: cuTensorMapEncodeTiled unavailable");
+  const int mtiles = (m + UM_BM - 1) / UM_BM;
+  int vec_y = 1;
+  long items = 0;
   for (int i = 0; i < batch; i++) {
     CCL_REQUIRE(Ap[i] && X[i] && Y[i], CCL_ERR_ARG, "umma: null operand %d", i);
     CCL_REQUIRE(ncols[i] > 0 && (!cplx || ncols[i] % 2 == 0), CCL_ERR_ARG,
                 "umma: entry %d ncols %d", i, ncols[i]);
     CCL_REQUIRE(ldx[i] >= ncols[i] && ldy[i] >= ncols[i], CCL_ERR_ARG,
                 "umma: entry %d ldx %ld / ldy %ld < ncols %d", i, ldx[i], ldy[i], ncols[i]);
-    // the staging loads read 8 floats at a time: rows must be 16-B aligned
+    // X is read by tensor copies: 16-B aligned base and row pitch
     CCL_REQUIRE(((uintptr_t)X[i] & 15) == 0 && ldx[i] % 4 == 0, CCL_ERR_ARG,
                 "umma: entry %d X not 16-B aligned (ldx %ld)", i, ldx[i]);
+    {
+      const cuuint64_t dims[2] = {(cuuint64_t)ncols[i], (cuuint64_t)k};
+      const cuuint64_t pitch[1] = {(cuuint64_t)ldx[i] * 4};
+      const cuuint32_t box[2] = {(cuuint32_t)UM_TN, (cuuint32_t)UM_KC};
+      const cuuint32_t estr[2] = {1, 1};
+      CUresult r = encode(&args.tx[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)X[i], dims,
+                          pitch, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      CCL_REQUIRE(r == CUDA_SUCCESS, CCL_ERR_CUDA, "umma: tensor map of entry %d (error %d)", i,
+                  (int)r);
+    }
     CCL_REQUIRE(((uintptr_t)Ap[i] & 15) == 0, CCL_ERR_ARG, "umma: entry %d A not aligned", i);
-    b.A[i] = Ap[i];
-    b.X[i] = (const float *)X[i];
-    b.Y[i] = (float *)Y[i];
-    b.ncols[i] = ncols[i];
-    b.ldx[i] = ldx[i];
-    b.ldy[i] = ldy[i];
-    if (ncols[i] > nmax) nmax = ncols[i];
+    if (((uintptr_t)Y[i] & 15) != 0 || ldy[i] % 4 != 0) vec_y = 0;
+    w.A[i] = Ap[i];
+    w.Y[i] = (float *)Y[i];
+    w.ncols[i] = ncols[i];
+    w.ntn[i] = (ncols[i] + UM_TN - 1) / UM_TN;
+    w.base[i] = (int)items;
+    w.ldy[i] = ldy[i];
+    items += (long)mtiles * w.ntn[i];
   }
+  CCL_REQUIRE(items < (1L << 30), CCL_ERR_ARG, "umma: %ld work items", items);
+  w.batch = batch;
+  w.items = (int)items;
+  w.mtiles = mtiles;
   const int kp = umma_kpad(k);
   const size_t smem = umma_smem(kp);
-  // N tiles per CTA: amortise the resident A tile over up to 4 tiles, but
-  // keep at least ~3 CTAs per SM of work in the launch (one CTA is resident
-  // per SM at this shared-memory size)
-  const int mtiles = (m + UM_BM - 1) / UM_BM;
-  long tiles = 0;
-  for (int i = 0; i < batch; i++) tiles += (ncols[i] + UM_BN - 1) / UM_BN;
-  tiles *= mtiles;
-  int tpc = (int)(tiles / (3L * kNumSM));
-  tpc = tpc < 1 ? 1 : (tpc > UM_MAX_TILES_PER_CTA ? UM_MAX_TILES_PER_CTA : tpc);
-  dim3 grid((nmax + tpc * UM_BN - 1) / (tpc * UM_BN), mtiles, batch);
+  static int sms = 0;
+  if (!sms) sms = device_sm_count();
+  const int grid = (int)(items < sms ? items : sms);
   const float ar = (float)are, ai = (float)aim;
 #define CCL_UMMA(C, A_)                                                              \
   {                                                                                  \
@@ -433,7 +652,7 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
       set_smem = smem;                                                               \
     }                                                                                \
-    kern<<<grid, UM_THREADS, smem, s>>>(b, m, k, kp, tpc, ar, ai);                   \
+    kern<<<grid, UM_THREADS2, smem, s>>>(args, m, k, kp, vec_y, ar, ai);                \
   }
   if (cplx) {
     if (beta == 1.0) CCL_UMMA(true, true) else CCL_UMMA(true, false)

@@ -89,3 +89,65 @@ def test_bf16x3_rejects_large_k_and_misaligned(cuda):
     rc = lib.ccl_dht_bf16x3_gemm_batch(1, 64, 64, ints([64]), 0, PP([p]), PP([p + 4]),
                                        longs([64]), PP([p]), longs([64]), 1.0, 0.0, 0.0, None)
     assert rc == 1 and b"aligned" in lib.ccl_last_error()
+
+
+def test_bf16x3_batch_many_items(cuda):
+    """More work items than CTAs: each CTA walks several N tiles and reloads
+    its resident A tile when the (entry, M tile) changes; complex alpha and
+    accumulation into Y."""
+    rng = np.random.default_rng(11)
+    m = k = 255
+    mats = [rng.normal(size=(m, k)) for _ in range(3)]
+    preps = [prepare(a, CCL_F32) for a in mats]
+    ncols = [4096, 2048, 4096, 4096, 1000, 4096, 2048, 4096]
+    which = [0, 1, 2, 0, 1, 2, 0, 1]
+    al = 0.5 - 1.25j
+    Xs = [rng.normal(size=(k, n)).astype(np.float32) for n in ncols]
+    Y0 = [rng.normal(size=(m, n)).astype(np.float32) for n in ncols]
+    Xd = [torch.from_numpy(x).cuda() for x in Xs]
+    Yd = [torch.from_numpy(y.copy()).cuda() for y in Y0]
+    call("ccl_dht_bf16x3_gemm_batch", len(ncols), m, k, ints(ncols), 1,
+         PP([preps[w] for w in which]), PP(Xd), longs(ncols), PP(Yd), longs(ncols),
+         al.real, al.imag, 1.0, _lib.stream())
+    torch.cuda.synchronize()
+    assert _lib.load().ccl_dht_bf16x3_status(1) == 0
+    for i in range(len(ncols)):
+        A32 = mats[which[i]].astype(np.float32).astype(np.float64)
+        T = A32 @ Xs[i].astype(np.float64)
+        Rc = (Y0[i][:, 0::2] + 1j * Y0[i][:, 1::2]) + al * (T[:, 0::2] + 1j * T[:, 1::2])
+        ref = np.empty_like(T)
+        ref[:, 0::2], ref[:, 1::2] = Rc.real, Rc.imag
+        err = np.abs(Yd[i].cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err < TOL, (i, err)
+
+
+def test_bf16x3_repeated_launches(cuda):
+    """Back-to-back launches over many work items must each give the same,
+    correct result (a stage-ring reuse race shows up only intermittently)."""
+    rng = np.random.default_rng(5)
+    m = k = 255
+    A = rng.normal(size=(m, k))
+    Ap = prepare(A, CCL_F32)
+    b, n = 6, 4096
+    Xs = [rng.normal(size=(k, n)).astype(np.float32) for _ in range(b)]
+    Xd = [torch.from_numpy(x).cuda() for x in Xs]
+    Yd = [torch.empty((m, n), dtype=torch.float32, device="cuda") for _ in range(b)]
+    A32 = A.astype(np.float32).astype(np.float64)
+    refs = [A32 @ x.astype(np.float64) for x in Xs]
+    first = None
+    for it in range(8):
+        for y in Yd:
+            y.fill_(float("nan"))
+        call("ccl_dht_bf16x3_gemm_batch", b, m, k, ints([n] * b), 0, PP([Ap] * b), PP(Xd),
+             longs([n] * b), PP(Yd), longs([n] * b), 1.0, 0.0, 0.0, _lib.stream())
+        torch.cuda.synchronize()
+        assert _lib.load().ccl_dht_bf16x3_status(1) == 0
+        got = [y.cpu().numpy() for y in Yd]
+        for i in range(b):
+            err = np.abs(got[i] - refs[i]).max() / np.abs(refs[i]).max()
+            assert err < TOL, (it, i, err)
+        if first is None:
+            first = got
+        else:
+            for i in range(b):
+                assert np.array_equal(first[i], got[i]), (it, i)
