@@ -226,17 +226,24 @@ static __global__ void __launch_bounds__(ST_THREADS)
   const unsigned lt = (1u << lane) - 1u;
   const long base = (long)blockIdx.x * ST_TILE;
   u32 tile_run = ovf_off[blockIdx.x] + cell_offset[C];
+  // overflow items of this tile (block-uniform): the exclusive tile offsets
+  // end at np - (in-window total)
+  const u32 ovf_next =
+      blockIdx.x + 1 < gridDim.x ? ovf_off[blockIdx.x + 1] : (u32)np - cell_offset[C];
+  const bool tile_has_ovf = ovf_next != ovf_off[blockIdx.x];
 #pragma unroll
   for (int it = 0; it < ST_ITEMS; it++) {
     const long i = base + it * ST_THREADS + threadIdx.x;
     const bool valid = i < np;
     const u32 k = valid ? keys[i] : 0xffffffffu;
     const bool ovf = valid && k == C;
-    // overflow: block-ordered rank within this round of ST_THREADS items
-    u32 rtot;
-    const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
-    if (ovf) sort_indx[tile_run + r] = (u32)i;
-    tile_run += rtot;
+    if (tile_has_ovf) {
+      // overflow: block-ordered rank within this round of ST_THREADS items
+      u32 rtot;
+      const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
+      if (ovf) sort_indx[tile_run + r] = (u32)i;
+      tile_run += rtot;
+    }
     // in-window: warp-aggregated cursor
     const unsigned peers = __match_any_sync(0xffffffffu, (valid && !ovf) ? k : 0xffffffffu);
     const int leader = __ffs(peers) - 1;
@@ -247,10 +254,45 @@ static __global__ void __launch_bounds__(ST_THREADS)
   }
 }
 
-static __global__ void k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset,
-                             u32 *__restrict__ sort_indx) {
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < (long)C;
-       c += (long)gridDim.x * blockDim.x) {
+// One block per FX_CELLS consecutive cells: their segments are contiguous
+// in sort_indx, so the block stages them in shared memory with coalesced
+// loads, each thread insertion-sorts its cell there, and the block writes
+// the range back (only if some cell changed).  A range larger than the
+// staging buffer (cells far denser than the mean) is sorted in place.
+constexpr int FX_CELLS = 256, FX_CAP = 8192;
+static __global__ void __launch_bounds__(FX_CELLS)
+    k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, u32 *__restrict__ sort_indx) {
+  __shared__ u32 sh[FX_CAP];
+  __shared__ int changed;
+  const long c0 = (long)blockIdx.x * FX_CELLS;
+  const long c1 = c0 + FX_CELLS < (long)C ? c0 + FX_CELLS : (long)C;
+  const long c = c0 + threadIdx.x;
+  const u32 lo = cell_offset[c0], n = cell_offset[c1] - lo;
+  if (n <= (u32)FX_CAP) {
+    if (threadIdx.x == 0) changed = 0;
+    for (u32 i = threadIdx.x; i < n; i += FX_CELLS) sh[i] = sort_indx[lo + i];
+    __syncthreads();
+    if (c < c1) {
+      const u32 p0 = cell_offset[c] - lo, p1 = cell_offset[c + 1] - lo;
+      bool moved = false;
+      for (u32 a = p0 + 1; a < p1; a++) {
+        const u32 v = sh[a];
+        u32 b = a;
+        while (b > p0 && sh[b - 1] > v) {
+          sh[b] = sh[b - 1];
+          b--;
+        }
+        if (b != a) {
+          sh[b] = v;
+          moved = true;
+        }
+      }
+      if (moved) changed = 1;
+    }
+    __syncthreads();
+    if (changed)
+      for (u32 i = threadIdx.x; i < n; i += FX_CELLS) sort_indx[lo + i] = sh[i];
+  } else if (c < c1) {
     const u32 p0 = cell_offset[c], p1 = cell_offset[c + 1];
     for (u32 a = p0 + 1; a < p1; a++) {
       const u32 v = sort_indx[a];
@@ -316,7 +358,9 @@ int index_sort(long np, const T *x, const T *y, const T *z, KeyGrid g,
   k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
                                                     w.cursor, w.tile_ovf, sort_indx);
   CCL_LAUNCH_CHECK("scatter");
-  k_cell_fixup<<<grid_for(C, 256), 256, 0, s>>>((u32)C, cell_offset, sort_indx);
+  if (C > 0)
+    k_cell_fixup<<<(unsigned)((C + FX_CELLS - 1) / FX_CELLS), FX_CELLS, 0, s>>>(
+        (u32)C, cell_offset, sort_indx);
   CCL_LAUNCH_CHECK("cell_fixup");
   return CCL_OK;
 }

@@ -136,6 +136,20 @@ def test_index_sort_presorted_and_clustered(cuda, port):
         np.testing.assert_array_equal(b, a)
 
 
+def test_index_sort_nearly_sorted_full_size(cuda, port):
+    # the step's case: cell-ordered particles moved by less than a cell,
+    # 2048 x 256 nodes at about 8 per cell
+    rng = np.random.default_rng(8)
+    g = geom(2048, 256)
+    p = particles(rng, 4_000_000, g, spill=0.0, boundaries=False)
+    _, _, _, srt = oracle_sort(port, p, g)
+    p = {k: v[srt].copy() for k, v in p.items()}
+    p["x"] += rng.uniform(-0.4, 0.4, p["x"].size) * g["dx"]
+    p["y"] += rng.uniform(-0.4, 0.4, p["y"].size) * g["dr"]
+    for a, b in zip(oracle_sort(port, p, g), gpu_sort(p, g)[:4]):
+        np.testing.assert_array_equal(b, a)
+
+
 def test_index_sort_workspace_too_small(cuda):
     g = geom()
     n = 100
