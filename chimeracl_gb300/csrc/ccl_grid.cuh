@@ -22,10 +22,113 @@ namespace ccl {
 constexpr int DEP_TX = 32, DEP_TR = 8, DEP_THREADS = DEP_TX * DEP_TR;
 constexpr int DEP_NTX = DEP_TX - 1, DEP_NTR = DEP_TR - 1;
 
-struct DepGrid {
-  int Nx, Nr;
-  double xmin, dx_inv, rmin, dr_inv;
-};
+// One particle's contribution to the 2x2 corner sums of its cell, in the
+// reference's operation order (grid_deposit_m1.cl:105-138 scalar,
+// 259-316 vector).
+template <typename T, int M, bool VEC>
+__device__ __forceinline__ void dep_particle(T (&s)[4][(VEC ? 3 : 1) * (1 + 2 * M)], T xp,
+                                             T yp, T zp, T wraw, T ux, T uy, T uz, T gi, T q,
+                                             const GridP<T> &g, T fix, T fir) {
+  constexpr int NK = VEC ? 3 : 1;
+  T wp;
+  if (VEC)
+    wp = wraw * gi * q;
+  else
+    wp = wraw * q;
+  const T rp = sqrt(yp * yp + zp * zp);
+  T rinv;
+  if (VEC)
+    rinv = rp > T(0) ? T(1) / rp : T(0);  // grid_deposit_m1.cl:280-281
+  else
+    rinv = T(1) / rp;                     // grid_deposit_m1.cl:115
+  T e[M + 1][2];
+  if (M >= 1) {
+    e[1][0] = yp * rinv;
+    e[1][1] = zp * rinv;
+  }
+#pragma unroll
+  for (int m = 2; m <= M; m++) {  // e^{i m phi} by recurrence (m >= 2)
+    e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+    e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+  }
+  T sX1 = (xp - g.xmin) * g.dx_inv - fix;
+  T sX0 = T(1) - sX1;
+  T sR1 = (rp - g.rmin) * g.dr_inv - fir;
+  T sR0 = T(1) - sR1;
+  sX0 *= wp;
+  sX1 *= wp;
+  const T C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+  const T jp[3] = {ux, uy, uz};
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+      constexpr int B = 1 + 2 * M;
+      if (VEC) {
+        T jproj = C[c] * jp[k];
+        s[c][k * B] += C[c] * jp[k];
+#pragma unroll
+        for (int m = 1; m <= M; m++) {
+          s[c][k * B + 2 * m - 1] += jproj * e[m][0];
+          s[c][k * B + 2 * m] += jproj * e[m][1];
+        }
+      } else {
+        s[c][0] += C[c];
+#pragma unroll
+        for (int m = 1; m <= M; m++) {
+          s[c][2 * m - 1] += C[c] * e[m][0];
+          s[c][2 * m] += C[c] * e[m][1];
+        }
+      }
+    }
+  }
+}
+
+// FP32 form (the mixed-precision step; no bit-exact counterpart): the same
+// corner sums with 1/r from rsqrt and the per-particle moments (1, e^{im phi}
+// per component) formed once, then one FMA per (corner, moment).
+template <int M, bool VEC>
+__device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (1 + 2 * M)],
+                                             float xp, float yp, float zp, float wraw, float ux,
+                                             float uy, float uz, float gi, float q,
+                                             const GridP<float> &g, float fix, float fir) {
+  constexpr int NK = VEC ? 3 : 1, B = 1 + 2 * M;
+  const float wp = VEC ? wraw * gi * q : wraw * q;
+  const float r2 = yp * yp + zp * zp;
+  const float rinv = r2 > 0.f ? rsqrtf(r2) : (VEC ? 0.f : __int_as_float(0x7f800000));
+  const float rp = r2 > 0.f ? r2 * rinv : 0.f;
+  float e[M + 1][2];
+  e[0][0] = 1.f;
+  e[0][1] = 0.f;
+  if (M >= 1) {
+    e[1][0] = yp * rinv;
+    e[1][1] = zp * rinv;
+  }
+#pragma unroll
+  for (int m = 2; m <= M; m++) {
+    e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+    e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+  }
+  const float sX1 = (xp - g.xmin) * g.dx_inv - fix, sX0 = 1.f - sX1;
+  const float sR1 = (rp - g.rmin) * g.dr_inv - fir, sR0 = 1.f - sR1;
+  const float wX0 = sX0 * wp, wX1 = sX1 * wp;
+  const float C[4] = {sR0 * wX0, sR0 * wX1, sR1 * wX0, sR1 * wX1};
+  const float jp[3] = {VEC ? ux : 1.f, uy, uz};
+  float mom[NK * B];
+#pragma unroll
+  for (int k = 0; k < NK; k++) {
+    mom[k * B] = jp[k];
+#pragma unroll
+    for (int m = 1; m <= M; m++) {
+      mom[k * B + 2 * m - 1] = jp[k] * e[m][0];
+      mom[k * B + 2 * m] = jp[k] * e[m][1];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+#pragma unroll
+    for (int qq = 0; qq < NK * B; qq++) s[c][qq] = fmaf(C[c], mom[qq], s[c][qq]);
+}
 
 // Field pointer bundle: for a scalar deposit f[m] (m = 0..M); for a vector
 // deposit f[3m + k].  Mode 0 is real, modes >= 1 complex.
@@ -36,7 +139,7 @@ __global__ void __launch_bounds__(DEP_THREADS)
               const T *__restrict__ y, const T *__restrict__ z,
               const T *__restrict__ ux, const T *__restrict__ uy,
               const T *__restrict__ uz, const T *__restrict__ g_inv,
-              const T *__restrict__ w, T q, DepGrid g, ptrs<12> f) {
+              const T *__restrict__ w, T q, GridP<T> g, ptrs<12> f) {
   constexpr int NK = VEC ? 3 : 1;       // vector components
   constexpr int NQ = NK * (1 + 2 * M);  // reals per node
   __shared__ T acc[NQ][DEP_NTR][DEP_NTX];
@@ -73,69 +176,15 @@ __global__ void __launch_bounds__(DEP_THREADS)
   if (valid) {
     const long cg = (long)ix + (long)ir * (Nx - 1);
     const u32 p0 = cell_off[cg], p1 = cell_off[cg + 1];
-    const T xmin = (T)g.xmin, dx_inv = (T)g.dx_inv, rmin = (T)g.rmin,
-            dr_inv = (T)g.dr_inv;
     const T fix = (T)ix, fir = (T)ir;
     for (u32 ip = p0; ip < p1; ip++) {
       const u32 p = sort_indx[ip];
-      const T xp = x[p], yp = y[p], zp = z[p];
-      T wp;
-      if (VEC)
-        wp = w[p] * g_inv[p] * q;
+      const T a = VEC ? ux[p] : T(0), b = VEC ? uy[p] : T(0), c = VEC ? uz[p] : T(0),
+              d = VEC ? g_inv[p] : T(0);
+      if constexpr (sizeof(T) == 4)
+        dep_particle_f32<M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, fix, fir);
       else
-        wp = w[p] * q;
-      const T rp = sqrt(yp * yp + zp * zp);
-      T rinv;
-      if (VEC)
-        rinv = rp > T(0) ? T(1) / rp : T(0);  // grid_deposit_m1.cl:280-281
-      else
-        rinv = T(1) / rp;                     // grid_deposit_m1.cl:115
-      T e[M + 1][2];
-      if (M >= 1) {
-        e[1][0] = yp * rinv;
-        e[1][1] = zp * rinv;
-      }
-#pragma unroll
-      for (int m = 2; m <= M; m++) {  // e^{i m phi} by recurrence (m >= 2)
-        e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
-        e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
-      }
-      T sX1 = (xp - xmin) * dx_inv - fix;
-      T sX0 = T(1) - sX1;
-      T sR1 = (rp - rmin) * dr_inv - fir;
-      T sR0 = T(1) - sR1;
-      sX0 *= wp;
-      sX1 *= wp;
-      const T C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
-      T jp[3] = {T(0), T(0), T(0)};
-      if (VEC) {
-        jp[0] = ux[p];
-        jp[1] = uy[p];
-        jp[2] = uz[p];
-      }
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-#pragma unroll
-        for (int k = 0; k < NK; k++) {
-          constexpr int B = 1 + 2 * M;
-          if (VEC) {
-            T jproj = C[c] * jp[k];
-            s[c][k * B] += C[c] * jp[k];
-#pragma unroll
-            for (int m = 1; m <= M; m++) {
-              s[c][k * B + 2 * m - 1] += jproj * e[m][0];
-              s[c][k * B + 2 * m] += jproj * e[m][1];
-            }
-          } else {
-            s[c][0] += C[c];
-#pragma unroll
-            for (int m = 1; m <= M; m++) {
-              s[c][2 * m - 1] += C[c] * e[m][0];
-              s[c][2 * m] += C[c] * e[m][1];
-            }
-          }
-        }
-      }
+        dep_particle<T, M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, fix, fir);
     }
   }
 
@@ -179,7 +228,7 @@ __global__ void __launch_bounds__(DEP_THREADS)
 template <typename T, int M, bool VEC>
 int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
               const T *y, const T *z, const T *ux, const T *uy, const T *uz,
-              const T *g_inv, const T *w, int charge, DepGrid g,
+              const T *g_inv, const T *w, int charge, GridP<T> g,
               void *const *flds, cudaStream_t s) {
   ptrs<12> f;
   const int nptr = (VEC ? 3 : 1) * (M + 1);
@@ -190,8 +239,8 @@ int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
   dim3 grid((g.Nx + DEP_NTX - 1) / DEP_NTX, (g.Nr + DEP_NTR - 1) / DEP_NTR);
   // the reference passes the charge as a signed char (grid_methods_cl.py:259)
   T q = (T)(signed char)charge;
-  k_deposit<T, M, VEC><<<grid, DEP_THREADS, 0, s>>>(
-      sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w, q, g, f);
+  k_deposit<T, M, VEC><<<grid, DEP_THREADS, 0, s>>>(sort_indx, cell_off, x, y, z, ux, uy, uz,
+                                                    g_inv, w, q, g, f);
   CCL_LAUNCH_CHECK("deposit");
   return CCL_OK;
 }
@@ -199,7 +248,7 @@ int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
 template <typename T, bool VEC>
 int deposit(int M, const u32 *sort_indx, const u32 *cell_off, const T *x,
             const T *y, const T *z, const T *ux, const T *uy, const T *uz,
-            const T *g_inv, const T *w, int charge, DepGrid g,
+            const T *g_inv, const T *w, int charge, GridP<T> g,
             void *const *flds, cudaStream_t s) {
   switch (M) {
     case 0:
@@ -279,7 +328,7 @@ __global__ void __launch_bounds__(256)
                   const T *__restrict__ z, T *__restrict__ px,
                   T *__restrict__ py, T *__restrict__ pz,
                   T *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
-                  const u32 *__restrict__ np_stay_p, T dt, DepGrid g,
+                  const u32 *__restrict__ np_stay_p, T dt, GridP<T> g,
                   ptrs<24> f) {
   const u32 np_stay = *np_stay_p;
   const int Nx = g.Nx, nxc = Nx - 1, nrc = g.Nr - 1;
@@ -289,8 +338,7 @@ __global__ void __launch_bounds__(256)
     if (p >= np_stay) continue;  // grid_deposit_m1.cl:367-368
     const T xp = x[p], yp = y[p], zp = z[p];
     const T rp = sqrt(yp * yp + zp * zp);
-    const T xmin = (T)g.xmin, dx_inv = (T)g.dx_inv, rmin = (T)g.rmin,
-            dr_inv = (T)g.dr_inv;
+    const T xmin = g.xmin, dx_inv = g.dx_inv, rmin = g.rmin, dr_inv = g.dr_inv;
     const int ix = floor_to_int<T>(floor((xp - xmin) * dx_inv), -1);
     const int ir = floor_to_int<T>(floor((rp - rmin) * dr_inv), 1 << 30);
     if (!(ix > 0 && ix < nxc - 1 && ir < nrc - 1)) continue;
@@ -358,10 +406,101 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// FP32 form of the gather + push (the mixed-precision step; no bit-exact
+// counterpart): per field component the mode-0 and mode-m node sums are
+// formed first and combined once with e^{-i m phi}; 1/r and the Lorentz
+// factors from rsqrt.  The physics and the node weights are those of the
+// exact kernel above.
+template <int M>
+__global__ void __launch_bounds__(256)
+    k_gather_push_f32(long np, const float *__restrict__ x, const float *__restrict__ y,
+                      const float *__restrict__ z, float *__restrict__ px,
+                      float *__restrict__ py, float *__restrict__ pz,
+                      float *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
+                      const u32 *__restrict__ np_stay_p, float dt, GridP<float> g,
+                      ptrs<24> f) {
+  const u32 np_stay = *np_stay_p;
+  const int Nx = g.Nx, nxc = Nx - 1, nrc = g.Nr - 1;
+  const float dt_2 = 0.5f * dt;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x) {
+    const u32 p = sort_indx[i];
+    if (p >= np_stay) continue;
+    const float xp = x[p], yp = y[p], zp = z[p];
+    const float r2 = yp * yp + zp * zp;
+    const float rinv = r2 > 0.f ? rsqrtf(r2) : __int_as_float(0x7f800000);
+    const float rp = r2 > 0.f ? r2 * rinv : 0.f;
+    const float fx = (xp - g.xmin) * g.dx_inv, fr = (rp - g.rmin) * g.dr_inv;
+    const int ix = floor_to_int<float>(floorf(fx), -1);
+    const int ir = floor_to_int<float>(floorf(fr), 1 << 30);
+    if (!(ix > 0 && ix < nxc - 1 && ir < nrc - 1)) continue;
+    const unsigned ig = (unsigned)ix + (unsigned)ir * (unsigned)Nx;
+    const float sX1 = fx - (float)ix, sX0 = 1.f - sX1;
+    const float sR1 = fr - (float)ir, sR0 = 1.f - sR1;
+    const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+    const unsigned nodes[4] = {ig, ig + 1, ig + (unsigned)Nx, ig + (unsigned)Nx + 1};
+    float e[M + 1][2];
+    if (M >= 1) {
+      e[1][0] = yp * rinv;
+      e[1][1] = -zp * rinv;
+    }
+#pragma unroll
+    for (int m = 2; m <= M; m++) {
+      e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+      e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+    }
+    float fld[6];  // ex ey ez bx by bz at the particle
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const float *f0 = (const float *)f.p[k];
+      float a = 0.f;
+#pragma unroll
+      for (int c = 0; c < 4; c++) a = fmaf(C[c], __ldg(f0 + nodes[c]), a);
+#pragma unroll
+      for (int m = 1; m <= M; m++) {
+        const float2 *fm = (const float2 *)f.p[6 * m + k];
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const float2 v = __ldg(fm + nodes[c]);
+          re = fmaf(C[c], v.x, re);
+          im = fmaf(C[c], v.y, im);
+        }
+        a = fmaf(2.f * re, e[m][0], a);
+        a = fmaf(-2.f * im, e[m][1], a);
+      }
+      fld[k] = a;
+    }
+    // Boris push (grid_deposit_m1.cl:440-505)
+    float um[3];
+    um[0] = px[p] + dt_2 * fld[0];
+    um[1] = py[p] + dt_2 * fld[1];
+    um[2] = pz[p] + dt_2 * fld[2];
+    const float gi0 = rsqrtf(1.f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+    float t[3], sv[3], u0[3], up[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) t[k] = dt_2 * fld[3 + k] * gi0;
+    const float f2 = __fdividef(2.f, 1.f + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
+    u0[0] = um[0] + um[1] * t[2] - um[2] * t[1];
+    u0[1] = um[1] - um[0] * t[2] + um[2] * t[0];
+    u0[2] = um[2] + um[0] * t[1] - um[1] * t[0];
+    up[0] = um[0] + u0[1] * sv[2] - u0[2] * sv[1];
+    up[1] = um[1] - u0[0] * sv[2] + u0[2] * sv[0];
+    up[2] = um[2] + u0[0] * sv[1] - u0[1] * sv[0];
+    const float u[3] = {up[0] + dt_2 * fld[0], up[1] + dt_2 * fld[1], up[2] + dt_2 * fld[2]};
+    px[p] = u[0];
+    py[p] = u[1];
+    pz[p] = u[2];
+    g_inv[p] = rsqrtf(1.f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  }
+}
+
 template <typename T>
 int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
                 T *py, T *pz, T *g_inv, const u32 *sort_indx,
-                const u32 *np_stay, double factor_push, DepGrid g,
+                const u32 *np_stay, double factor_push, GridP<T> g,
                 const void *const *flds, cudaStream_t s) {
   if (np == 0) return CCL_OK;
   ptrs<24> f;
@@ -371,9 +510,13 @@ int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
   }
   int nb = grid_for(np, 256, 16);
   T dt = (T)factor_push;
-#define CCL_GP(MM)                                                             \
-  k_gather_push<T, MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv,     \
-                                          sort_indx, np_stay, dt, g, f)
+#define CCL_GP(MM)                                                                     \
+  if constexpr (sizeof(T) == 4)                                                        \
+    k_gather_push_f32<MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx, \
+                                             np_stay, dt, g, f);                       \
+  else                                                                                 \
+    k_gather_push<T, MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx,  \
+                                            np_stay, dt, g, f)
   switch (M) {
     case 0: CCL_GP(0); break;
     case 1: CCL_GP(1); break;

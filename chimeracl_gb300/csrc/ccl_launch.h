@@ -9,8 +9,8 @@
 
 namespace ccl {
 
-struct KeyGrid;
-struct DepGrid;
+template <typename T>
+struct GridP;
 
 // ccl_fft.cu
 template <typename T>

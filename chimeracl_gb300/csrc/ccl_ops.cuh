@@ -25,7 +25,7 @@ int Ops<T>::index_sort(long np, const void *x, const void *y, const void *z,
                        uint32_t *cell_offset, uint32_t *sort_indx,
                        uint32_t *np_stay, void *ws, size_t ws_bytes,
                        cudaStream_t s) {
-  KeyGrid g = {Nx, Nr, xmin, dx_inv, rmin, dr_inv};
+  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
   return ccl::index_sort<T>(np, (const T *)x, (const T *)y, (const T *)z, g,
                             indx, counts, cell_offset, sort_indx, np_stay, ws,
                             ws_bytes, s);
@@ -80,7 +80,7 @@ int Ops<T>::deposit(int vec, int M, const uint32_t *sort_indx,
                     int charge, int Nx, double xmin, double dx_inv, int Nr,
                     double rmin, double dr_inv, void *const *flds,
                     cudaStream_t s) {
-  DepGrid g = {Nx, Nr, xmin, dx_inv, rmin, dr_inv};
+  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
   if (vec)
     return ccl::deposit<T, true>(M, sort_indx, cell_off, (const T *)x,
                                  (const T *)y, (const T *)z, (const T *)ux,
@@ -134,7 +134,7 @@ int Ops<T>::gather_push(int M, long np, const void *x, const void *y,
                         double xmin, double dx_inv, int Nr, double rmin,
                         double dr_inv, const void *const *flds,
                         cudaStream_t s) {
-  DepGrid g = {Nx, Nr, xmin, dx_inv, rmin, dr_inv};
+  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
   return ccl::gather_push<T>(M, np, (const T *)x, (const T *)y, (const T *)z,
                              (T *)px, (T *)py, (T *)pz, (T *)g_inv, sort_indx,
                              np_stay, factor_push, g, flds, s);

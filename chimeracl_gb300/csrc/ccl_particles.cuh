@@ -37,9 +37,12 @@ int push_x(long np, T *x, T *y, T *z, const T *px, const T *py, const T *pz,
 // ---------------------------------------------------------------------
 // Cell key of a particle (particles_generic.cl:106-125).  Coordinates are
 // converted to double so that the FP32 form sorts with the same key rule.
-struct KeyGrid {
+// Grid geometry in the particles' own precision (converted once on the
+// host: the FP32 kernels then never touch the FP64 pipe)
+template <typename T>
+struct GridP {
   int Nx, Nr;
-  double xmin, dx_inv, rmin, dr_inv;
+  T xmin, dx_inv, rmin, dr_inv;
 };
 
 template <typename T>
@@ -54,11 +57,11 @@ __device__ __forceinline__ int floor_to_int(T f, int bad) {
 // pipe (a few FP64 instructions per particle cost more than the whole
 // kernel's memory traffic on this part).
 template <typename T>
-__device__ __forceinline__ u32 cell_key(T xp, T yp, T zp, const KeyGrid &g) {
+__device__ __forceinline__ u32 cell_key(T xp, T yp, T zp, const GridP<T> &g) {
   int nxc = g.Nx - 1, nrc = g.Nr - 1;
   T r = sqrt(yp * yp + zp * zp);
-  int ix = floor_to_int<T>(floor((xp - (T)g.xmin) * (T)g.dx_inv), -1);
-  int ir = floor_to_int<T>(floor((r - (T)g.rmin) * (T)g.dr_inv), -1);
+  int ix = floor_to_int<T>(floor((xp - g.xmin) * g.dx_inv), -1);
+  int ir = floor_to_int<T>(floor((r - g.rmin) * g.dr_inv), -1);
   if (ix > 0 && ix < nxc - 1 && ir < nrc - 1 && ir >= 0)
     return (u32)(ix + ir * nxc);
   return (u32)(nrc * nxc);
@@ -148,7 +151,7 @@ constexpr int ST_THREADS = 256, ST_ITEMS = 8, ST_TILE = ST_THREADS * ST_ITEMS;
 template <typename T>
 __global__ void __launch_bounds__(ST_THREADS)
     k_keys(long np, const T *__restrict__ x, const T *__restrict__ y,
-           const T *__restrict__ z, KeyGrid g, u32 *__restrict__ keys,
+           const T *__restrict__ z, GridP<T> g, u32 *__restrict__ keys,
            u32 *__restrict__ counts, u32 *__restrict__ tile_ovf) {
   __shared__ u32 sh[32];
   const int lane = threadIdx.x & 31;
@@ -331,7 +334,7 @@ static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
 static __global__ void k_copy_u32(const u32 *src, u32 *dst) { *dst = *src; }
 
 template <typename T>
-int index_sort(long np, const T *x, const T *y, const T *z, KeyGrid g,
+int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
                u32 *indx, u32 *counts, u32 *cell_offset, u32 *sort_indx,
                u32 *np_stay, void *ws, size_t ws_bytes, cudaStream_t s) {
   long C = (long)(g.Nx - 1) * (g.Nr - 1);

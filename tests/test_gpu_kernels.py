@@ -12,7 +12,7 @@ import pytest
 import torch
 
 from chimeracl_gb300 import _lib
-from chimeracl_gb300._lib import CCL_F64, PP, call
+from chimeracl_gb300._lib import CCL_F32, CCL_F64, PP, call
 
 pytestmark = pytest.mark.gpu
 
@@ -268,6 +268,62 @@ def test_deposit_bit_exact(cuda, port, M, vec):
         np.testing.assert_array_equal(host(d[k]), ref[k], err_msg=k)
 
 
+def to32(a):
+    return a.astype(np.complex64 if np.iscomplexobj(a) else np.float32)
+
+
+def to64(a):
+    return a.astype(np.complex128 if np.iscomplexobj(a) else np.float64)
+
+
+@pytest.mark.parametrize("M,vec", [(0, False), (1, False), (1, True), (2, True)])
+def test_deposit_fp32(cuda, port, M, vec):
+    """The FP32 deposit (row-staged kernel) against the FP64 oracle on the
+    same FP32 inputs, with one dense cluster so that a tile row holds more
+    particles than one staging round (relative 1e-5 of the deposited
+    magnitude: FP32 sums of a few hundred terms)."""
+    rng = np.random.default_rng(40 + M + 5 * vec)
+    g = geom(160, 40)
+    p = particles(rng, 60000, g)
+    p["x"][:3000] = g["Xmin"] + g["dx"] * rng.uniform(20.1, 27.9, 3000)
+    p["y"][:3000] = g["dr"] * rng.uniform(5.1, 5.9, 3000)
+    p["z"][:3000] = 0.0
+    p = {k: v.astype(np.float32).astype(np.float64) for k, v in p.items()}
+    _, _, off, srt = oracle_sort(port, p, g)
+    names = ["J" + c for c in "xyz"] if vec else ["rho"]
+    f0 = {k: to64(to32(v)) for k, v in fields(rng, g["Nr"], g["Nx"], M, names).items()}
+    ref = {k: v.copy() for k, v in f0.items()}
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    nxnr4 = (g["Nr"]) // 2 * (g["Nx"]) // 2
+    charge = -1
+    if vec:
+        port.depose_vector(M, nxnr4, srt, p["x"], p["y"], p["z"], p["px"], p["py"], p["pz"],
+                           p["g_inv"], p["w"], off, charge, g["Nx"], g["Xmin"], g["dx_inv"],
+                           g["Nr"], g["Rmin"], g["dr_inv"], [ref[k] for k in order])
+    else:
+        port.depose_scalar(M, nxnr4, srt, p["x"], p["y"], p["z"], p["w"], off, charge, g["Nx"],
+                           g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"],
+                           [ref[k] for k in order])
+    d = {k: dev(to32(v)) for k, v in f0.items()}
+    pd = {k: dev(to32(v)) for k, v in p.items()}
+    args = (g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"])
+    if vec:
+        call("ccl_deposit_vector", CCL_F32, M, dev(srt).data_ptr(), dev(off).data_ptr(),
+             pd["x"].data_ptr(), pd["y"].data_ptr(), pd["z"].data_ptr(), pd["px"].data_ptr(),
+             pd["py"].data_ptr(), pd["pz"].data_ptr(), pd["g_inv"].data_ptr(), pd["w"].data_ptr(),
+             charge, *args, PP([d[k] for k in order]), S())
+    else:
+        call("ccl_deposit_scalar", CCL_F32, M, dev(srt).data_ptr(), dev(off).data_ptr(),
+             pd["x"].data_ptr(), pd["y"].data_ptr(), pd["z"].data_ptr(), pd["w"].data_ptr(),
+             charge, *args, PP([d[k] for k in order]), S())
+    for k in order:
+        inc = ref[k] - f0[k]
+        got = host(d[k])
+        assert got.shape == ref[k].shape and got.dtype == to32(ref[k]).dtype
+        err = np.abs(to64(got) - ref[k]).max() / np.abs(inc).max()
+        assert err < 1e-5, (k, err)
+
+
 @pytest.mark.parametrize("M", [0, 1, 2])
 def test_postproc_and_warp_axis_bit_exact(cuda, port, M):
     rng = np.random.default_rng(20 + M)
@@ -316,6 +372,37 @@ def test_gather_push_bit_exact(cuda, port, M):
          g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], PP(fd), S())
     for k in ref:
         np.testing.assert_array_equal(host(pd[k]), ref[k], err_msg=k)
+
+
+@pytest.mark.parametrize("M", [0, 1, 2])
+def test_gather_push_fp32(cuda, port, M):
+    """The FP32 gather + Boris kernel against the FP64 oracle on the same
+    FP32-rounded inputs (no particles exactly on cell faces, where the two
+    precisions may pick different but equivalent cells)."""
+    rng = np.random.default_rng(50 + M)
+    g = geom(128, 32)
+    p = {k: to64(to32(v)) for k, v in particles(rng, 50000, g, boundaries=False).items()}
+    _, _, off, srt = oracle_sort(port, p, g)
+    np_stay = int(off[-2])
+    names = ["E" + c for c in "xyz"] + ["B" + c for c in "xyz"]
+    f = {k: to64(to32(v)) for k, v in fields(rng, g["Nr"], g["Nx"], M, names).items()}
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    ref = {k: p[k].copy() for k in ("px", "py", "pz", "g_inv")}
+    fp = 0.37
+    port.gather_and_push(M, p["x"], p["y"], p["z"], ref["px"], ref["py"], ref["pz"], ref["g_inv"],
+                         srt, fp, p["x"].size, np_stay, g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"],
+                         g["Rmin"], g["dr_inv"], [f[k] for k in order])
+    pd = {k: dev(to32(v)) for k, v in p.items()}
+    fd = [dev(to32(f[k])) for k in order]
+    nst = torch.tensor([np_stay], dtype=torch.int32, device="cuda")
+    call("ccl_gather_push", CCL_F32, M, p["x"].size, pd["x"].data_ptr(), pd["y"].data_ptr(),
+         pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(), pd["pz"].data_ptr(),
+         pd["g_inv"].data_ptr(), dev(srt).data_ptr(), nst.data_ptr(), fp, g["Nx"], g["Xmin"],
+         g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], PP(fd), S())
+    for k in ref:
+        got = to64(host(pd[k]))
+        err = np.abs(got - ref[k]).max() / np.abs(ref[k]).max()
+        assert err < 2e-5, (k, err)
 
 
 # ------------------------------------------------------------------- spectral
