@@ -307,6 +307,200 @@ __global__ void __launch_bounds__(FFT_THREADS)
 }
 
 // ---------------------------------------------------------------------
+// Register-resident transform for N = 512, 1024, 2048, 4096: N/8 threads,
+// 8 points each.  Radix-8 Stockham passes in registers (then one radix-4 or
+// radix-2 pass for N = 8^a * 4 or * 2); between passes the row goes through
+// shared memory once, padded by one point in eight so that the strided
+// pass writes are free of bank conflicts.  Thread j reads its input points
+// x[j + r N/8] straight from HBM and ends holding X[j + q N/8], q = 0..7, so
+// the first and last passes touch global memory directly (and a backward
+// transform's output is exactly the layout a forward transform starts from).
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
+
+template <int N> struct RegFft {
+  static constexpr int TH = N / 8;
+  static constexpr int P8 = N == 4096 ? 4 : 3;             // radix-8 passes
+  static constexpr int TAIL = N == 2048 ? 4 : (N == 1024 ? 2 : 1);  // last radix
+  static constexpr int SMEM_PTS = N + N / 8;
+};
+
+template <typename T, bool INV, int N>
+__device__ __forceinline__ void fft_reg(cplx<T> (&v)[8], cplx<T> *sm,
+                                        const cplx<T> *__restrict__ tw) {
+  using F = RegFft<N>;
+  const int j = threadIdx.x;
+  int Ns = 1;
+#pragma unroll
+  for (int p = 0; p < F::P8; p++) {
+    const int k = j & (Ns - 1);
+    if (p > 0) {
+      const int ts = N / (8 * Ns);
+#pragma unroll
+      for (int r = 1; r < 8; r++) v[r] = cmul(v[r], twid(tw, (long)(r * k) * ts, INV));
+    }
+    dft8<T, INV>(v);
+    const bool last = (p == F::P8 - 1) && F::TAIL == 1;
+    if (!last) {
+      const int ob = (j / Ns) * Ns * 8 + k;
+      __syncthreads();  // the previous pass's reads are done
+#pragma unroll
+      for (int r = 0; r < 8; r++) sm[fpad(ob + r * Ns)] = v[r];
+      __syncthreads();
+      if (p < F::P8 - 1) {
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = sm[fpad(j + r * F::TH)];
+      }
+    }
+    Ns *= 8;
+  }
+  if (F::TAIL == 4) {
+    // butterflies jj = j + t N/8 (t = 0, 1), points jj + r N/4; Ns = N/4
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const int jj = j + t * F::TH;
+      cplx<T> a[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) a[r] = sm[fpad(jj + r * (N / 4))];
+#pragma unroll
+      for (int r = 1; r < 4; r++) a[r] = cmul(a[r], twid(tw, (long)(r * jj), INV));
+      dft4<T, INV>(a[0], a[1], a[2], a[3]);
+#pragma unroll
+      for (int r = 0; r < 4; r++) v[t + 2 * r] = a[r];  // X[j + (t + 2r) N/8]
+    }
+  } else if (F::TAIL == 2) {
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int jj = j + t * F::TH;
+      cplx<T> a0 = sm[fpad(jj)], a1 = sm[fpad(jj + N / 2)];
+      a1 = cmul(a1, twid(tw, (long)jj, INV));
+      v[t] = cadd(a0, a1);      // X[j + t N/8]
+      v[t + 4] = csub(a0, a1);  // X[j + (t + 4) N/8]
+    }
+  }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8)
+    k_fft_fwd_reg(FftBatch b, const T *__restrict__ phs, const cplx<T> *__restrict__ tw) {
+  __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
+  constexpr int TH = N / 8;
+  const int j = threadIdx.x, e = blockIdx.y;
+  const long row = blockIdx.x;
+  const T *in = (const T *)b.in[e] + row * b.ld[e] * (b.real[e] ? 1 : 2);
+  cplx<T> v[8];
+  if (b.real[e]) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = {in[j + r * TH], T(0)};
+  } else {
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = ld_c(in, j + r * TH);
+  }
+  fft_reg<T, false, N>(v, sm, tw);
+  T *out = (T *)b.out[e] + row * N * 2;
+  const T *filt = b.filt[e] ? (const T *)b.filt[e] + row * N : nullptr;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int ix = j + q * TH;
+    cplx<T> r = mul_phs(v[q], ld_c(phs, ix));
+    if (filt) {
+      const T f = filt[ix];
+      r.re = f * r.re;
+      r.im = f * r.im;
+    }
+    st_c(out, ix, r);
+  }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8)
+    k_fft_bwd_reg(FftBatch b, const T *__restrict__ phs, const cplx<T> *__restrict__ tw) {
+  __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
+  constexpr int TH = N / 8;
+  const int j = threadIdx.x, e = blockIdx.y;
+  const long row = blockIdx.x;
+  const T *in = (const T *)b.in[e] + row * N * 2;
+  cplx<T> v[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = mul_phs(ld_c(in, j + r * TH), ld_c(phs, j + r * TH));
+  fft_reg<T, true, N>(v, sm, tw);
+  const T inv_n = (T)(1.0 / (double)N);
+  T *out = (T *)b.out[e];
+  const long ld = b.ld[e];
+  if (b.real[e]) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) out[row * ld + j + q * TH] = v[q].re * inv_n;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      cplx<T> r = {v[q].re * inv_n, v[q].im * inv_n};
+      st_c(out, row * ld + j + q * TH, r);
+    }
+  }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8, sizeof(T) == 4 && N <= 2048 ? 6144 / N : 1)
+    k_damp_reg(FftBatch b, const T *__restrict__ phs_p, const T *__restrict__ phs_m,
+               const T *__restrict__ prof, u32 nf, const cplx<T> *__restrict__ tw) {
+  __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
+  constexpr int TH = N / 8;
+  const int j = threadIdx.x, e = blockIdx.y;
+  const u32 un = (u32)N;
+  const long row = blockIdx.x;
+  T *spec = (T *)b.out[e] + row * N * 2;
+  T *rs = (T *)b.filt[e];
+  const bool rs_real = b.real[e] != 0;
+  cplx<T> v[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = mul_phs(ld_c(spec, j + r * TH), ld_c(phs_p, j + r * TH));
+  fft_reg<T, true, N>(v, sm, tw);
+  const T inv_n = (T)(1.0 / (double)N);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const u32 ux = (u32)(j + q * TH);
+    cplx<T> w = v[q];
+    w.re = w.re * inv_n;
+    w.im = rs_real ? T(0) : w.im * inv_n;
+    if (ux < nf) { w.re *= prof[ux]; w.im *= prof[ux]; }
+    if (ux > un - nf) { w.re *= prof[un - ux]; w.im *= prof[un - ux]; }
+    if (rs_real) rs[(row + 1) * N + ux] = w.re;
+    else st_c(rs, (row + 1) * N + ux, w);
+    v[q] = w;
+    if (row == 0) {  // the ghost row is damped in place as well
+      if (rs_real) {
+        T g = rs[ux];
+        if (ux < nf) g *= prof[ux];
+        if (ux > un - nf) g *= prof[un - ux];
+        rs[ux] = g;
+      } else {
+        cplx<T> g = ld_c(rs, ux);
+        if (ux < nf) { g.re *= prof[ux]; g.im *= prof[ux]; }
+        if (ux > un - nf) { g.re *= prof[un - ux]; g.im *= prof[un - ux]; }
+        st_c(rs, ux, g);
+      }
+    }
+  }
+  fft_reg<T, false, N>(v, sm, tw);
+#pragma unroll
+  for (int q = 0; q < 8; q++) st_c(spec, j + q * TH, mul_phs(v[q], ld_c(phs_m, j + q * TH)));
+}
+
+// (double at N = 4096 would need more than the 48 KB of static shared memory)
+template <typename T> static bool reg_size(int n) {
+  return n == 512 || n == 1024 || n == 2048 || (n == 4096 && sizeof(T) == 4);
+}
+
+#define CCL_REG_DISPATCH(N_, LAUNCH)                     \
+  switch (N_) {                                          \
+    case 512: LAUNCH(512); break;                        \
+    case 1024: LAUNCH(1024); break;                      \
+    case 2048: LAUNCH(2048); break;                      \
+    case 4096:                                           \
+      if constexpr (sizeof(T) == 4) { LAUNCH(4096); }    \
+      break;                                             \
+  }
+
+// ---------------------------------------------------------------------
 // Twiddle tables W_N^t = e^{-2 pi i t/N}, built once per (device, N, type)
 // by a device kernel (sincospi) and kept for the life of the process.
 template <typename T> __global__ void k_twiddles(int n, cplx<T> *tw) {
@@ -391,9 +585,15 @@ int fft_forward_batch(int batch, int nrows, int nx, const void *const *in,
   }
   const cplx<T> *tw = twiddles<T>(nx, s);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-  auto kern = k_fft_fwd<T>;
-  allow_smem(kern, smem);
-  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  if (reg_size<T>(nx)) {
+#define CCL_L(NN) k_fft_fwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
+    CCL_REG_DISPATCH(nx, CCL_L)
+#undef CCL_L
+  } else {
+    auto kern = k_fft_fwd<T>;
+    allow_smem(kern, smem);
+    kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  }
   CCL_LAUNCH_CHECK("fft_forward");
   return CCL_OK;
 }
@@ -421,9 +621,15 @@ int fft_backward_batch(int batch, int nrows, int nx, const void *const *in,
   }
   const cplx<T> *tw = twiddles<T>(nx, s);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-  auto kern = k_fft_bwd<T>;
-  allow_smem(kern, smem);
-  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  if (reg_size<T>(nx)) {
+#define CCL_L(NN) k_fft_bwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
+    CCL_REG_DISPATCH(nx, CCL_L)
+#undef CCL_L
+  } else {
+    auto kern = k_fft_bwd<T>;
+    allow_smem(kern, smem);
+    kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(pl, b, (const T *)phs, tw);
+  }
   CCL_LAUNCH_CHECK("fft_backward");
   return CCL_OK;
 }
@@ -450,10 +656,18 @@ int damp_batch(int batch, int nrows, int nx, void *const *spec,
   }
   const cplx<T> *tw = twiddles<T>(nx, s);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
-  auto kern = k_damp<T>;
-  allow_smem(kern, smem);
-  kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(
-      pl, b, (const T *)phs_p, (const T *)phs_m, (const T *)prof, (u32)nf, tw);
+  if (reg_size<T>(nx)) {
+#define CCL_L(NN)                                                                           \
+  k_damp_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs_p, (const T *)phs_m, \
+                                                          (const T *)prof, (u32)nf, tw)
+    CCL_REG_DISPATCH(nx, CCL_L)
+#undef CCL_L
+  } else {
+    auto kern = k_damp<T>;
+    allow_smem(kern, smem);
+    kern<<<dim3(nrows, batch), FFT_THREADS, smem, s>>>(
+        pl, b, (const T *)phs_p, (const T *)phs_m, (const T *)prof, (u32)nf, tw);
+  }
   CCL_LAUNCH_CHECK("damp");
   return CCL_OK;
 }

@@ -517,6 +517,26 @@ def test_fft_rows(cuda, nx):
     assert np.abs(got[1:] - ref.real).max() <= FFT_TOL * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("nx", [512, 768, 1024, 2048, 4096])
+def test_fft_rows_fp32(cuda, nx):
+    """FP32 transforms (register-resident kernels at 512..4096) against
+    numpy's FFT of the same FP32 data; bar 2e-6 of the largest magnitude."""
+    rng = np.random.default_rng(nx + 1)
+    nr = 21
+    x = cplx(rng, nr, nx).astype(np.complex64)
+    phs = np.exp(1j * rng.uniform(0, 6, nx)).astype(np.complex64)
+    filt = rng.uniform(0, 1, (nr, nx)).astype(np.float32)
+    out = torch.empty((nr, nx), dtype=torch.complex64, device="cuda")
+    call("ccl_fft_forward_rows", CCL_F32, nr, nx, dev(x).data_ptr(), nx, 0, out.data_ptr(),
+         dev(phs).data_ptr(), dev(filt).data_ptr(), S())
+    ref = np.fft.fft(x.astype(np.complex128), axis=1) * phs * filt
+    assert np.abs(host(out) - ref).max() <= 2e-6 * np.abs(ref).max()
+    call("ccl_fft_backward_rows", CCL_F32, nr, nx, dev(x).data_ptr(), out.data_ptr(), nx, 0,
+         dev(phs).data_ptr(), S())
+    ref = np.fft.ifft(x.astype(np.complex128) * phs, axis=1)
+    assert np.abs(host(out) - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
 def test_fft_unsupported_length(cuda):
     lib = _lib.load()
     t = torch.zeros(2 * 17 * 4, dtype=torch.float64, device="cuda")
@@ -525,10 +545,11 @@ def test_fft_unsupported_length(cuda):
     assert rc == 3
 
 
+@pytest.mark.parametrize("nx", [512, 2048])
 @pytest.mark.parametrize("real_mode", [True, False])
-def test_damp_rows(cuda, port, real_mode):
+def test_damp_rows(cuda, port, real_mode, nx):
     rng = np.random.default_rng(50 + real_mode)
-    nr, nx, nf = 31, 512, 100
+    nr, nf = 31, 100
     spec = cplx(rng, nr, nx)
     rs0 = rng.normal(size=(nr + 1, nx)) if real_mode else cplx(rng, nr + 1, nx)
     kx = 2 * np.pi * np.fft.fftfreq(nx, 0.05)
