@@ -28,6 +28,8 @@ SIGNATURES = {
     "ccl_index_sort_workspace": [_l, _l, C.POINTER(_sz)],
     "ccl_index_sort": [_i, _l, _vp, _vp, _vp, _i, _d, _d, _i, _d, _d,
                        _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp],
+    "ccl_index_sort_noalloc": [_i, _l, _vp, _vp, _vp, _i, _d, _d, _i, _d, _d,
+                               _vp, _vp, _vp, _vp, _vp, _vp],
     "ccl_align": [_i, _l, _i, _pp, _pp, _vp, _vp],
     "ccl_iota_u32": [_vp, _l, _vp],
     "ccl_fill_grid": [_i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp],

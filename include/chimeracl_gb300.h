@@ -80,6 +80,24 @@ int ccl_index_sort(int dtype, long np, const void *x, const void *y,
                    uint32_t *sort_indx, uint32_t *np_stay, void *workspace,
                    size_t workspace_bytes, void *stream);
 
+/* ccl_index_sort without a caller-owned workspace.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory for the
+ * sort (a host binding that owns no device allocator, or a process whose
+ * device memory is reserved up front by another framework).  The workspace is
+ * a file-scope 8 MiB device array -- enough for up to 2,000,000 cells with up
+ * to 2^26 particles; larger inputs return CCL_ERR_WORKSPACE without
+ * launching anything.  The first call on a device does a one-time set-up
+ * (looks up the array's device address) and should come before any stream
+ * capture.  Nothing is allocated.  Calls that overlap in time on one device
+ * (other streams, other host threads) share the array and race; outputs
+ * and their meaning are those of ccl_index_sort. */
+int ccl_index_sort_noalloc(int dtype, long np, const void *x, const void *y,
+                           const void *z, int Nx, double xmin, double dx_inv,
+                           int Nr, double rmin, double dr_inv,
+                           uint32_t *indx_in_cell, uint32_t *sum_in_cell,
+                           uint32_t *cell_offset, uint32_t *sort_indx,
+                           uint32_t *np_stay, void *stream);
+
 /* dst[c][i] = src[c][sort_indx[i]] for i < n, c < ncomp (ncomp <= 16).
  * `src`, `dst` are host arrays of ncomp device pointers.
  * Replaces align_and_damp -> data_align_dbl (particles_methods_cl.py:263-286,
