@@ -149,7 +149,8 @@ def launch_count():
 
 
 def stream():
-    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    """The current CUDA stream of the current device, as a raw handle."""
+    return C.c_void_p(torch._C._cuda_getCurrentRawStream(torch.cuda.current_device()))
 
 
 def sort_workspace_bytes(np_, ncells):

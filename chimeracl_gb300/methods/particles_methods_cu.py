@@ -197,9 +197,11 @@ class ParticleMethodsCU(GenericMethodsCU):
         self._upload(arr, v)
 
     def _upload(self, arr, v):
-        h = torch.from_numpy(v).to(arr.dtype)
+        """Host draws -> device, through pinned memory and without waiting
+        for the device (the pinned block is held until the copy is done)."""
+        h = torch.from_numpy(v).to(arr.dtype).pin_memory()
         self.comm.h2d_bytes += h.numel() * h.element_size()
-        arr.copy_(h)
+        arr.copy_(h, non_blocking=True)
 
     def _cumsum(self, arr_in, allocator=None, output_dtype=np.uint32):
         """[0, cumsum(arr_in)...] (particles_methods_cl.py:303-311)."""

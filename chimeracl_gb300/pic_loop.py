@@ -53,6 +53,7 @@ class PIC_loop:
         self._graph_sig = None
         self.graph_replays = 0
         self.graph_captures = 0
+        self._cap_stream = None
         # library kernels per captured step, and totals captured / replayed
         # (a replay runs the captured kernels without launching them again)
         self._graph_kernels = 0
@@ -108,8 +109,21 @@ class PIC_loop:
                 from . import _lib
                 n0 = _lib.launch_count()
                 g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g):
-                    self._body(graph_mode=True)
+                # capture on a persistent side stream (each graph with its own
+                # private memory pool); unlike torch.cuda.graph() this neither
+                # synchronises the device nor empties the allocator's cache at
+                # every re-capture
+                if self._cap_stream is None:
+                    self._cap_stream = torch.cuda.Stream()
+                cur = torch.cuda.current_stream()
+                self._cap_stream.wait_stream(cur)
+                with torch.cuda.stream(self._cap_stream):
+                    g.capture_begin()
+                    try:
+                        self._body(graph_mode=True)
+                    finally:
+                        g.capture_end()
+                cur.wait_stream(self._cap_stream)
                 self._graph_kernels = _lib.launch_count() - n0
                 self._graph = g
                 self._graph_sig = self._signature()
