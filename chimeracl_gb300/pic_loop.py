@@ -97,45 +97,57 @@ class PIC_loop:
     def step(self):
         for diag in self.diags:
             diag.make_record(self.it)
-        use_graph = (self.graphs and not self.timit and not self.diags
-                     and not self._frame_due() and self.it > 0)
+        use_graph = self.graphs and not self.timit and not self.diags and self.it > 0
         if not use_graph:
             self._graph = None
             self._body(graph_mode=False)
+        elif self._frame_due():
+            # a window shift (host-driven injection, new array sizes) runs
+            # eagerly; the graph for the steps that follow is captured right
+            # after it, while the device still executes this step
+            self._graph = None
+            self._body(graph_mode=False)
+            self._capture()
         else:
-            sig = self._signature()
-            if self._graph is None or sig != self._graph_sig:
-                self._graph = None
-                from . import _lib
-                n0 = _lib.launch_count()
-                g = torch.cuda.CUDAGraph()
-                # capture on a persistent side stream (each graph with its own
-                # private memory pool); unlike torch.cuda.graph() this neither
-                # synchronises the device nor empties the allocator's cache at
-                # every re-capture
-                if self._cap_stream is None:
-                    self._cap_stream = torch.cuda.Stream()
-                cur = torch.cuda.current_stream()
-                self._cap_stream.wait_stream(cur)
-                with torch.cuda.stream(self._cap_stream):
-                    g.capture_begin()
-                    try:
-                        self._body(graph_mode=True)
-                    finally:
-                        g.capture_end()
-                cur.wait_stream(self._cap_stream)
-                self._graph_kernels = _lib.launch_count() - n0
-                self._graph = g
-                self._graph_sig = self._signature()
-                self.graph_captures += 1
-                self.graph_kernels_captured += self._graph_kernels
+            if self._graph is None or self._signature() != self._graph_sig:
+                self._capture()
             self._graph.replay()
             self.graph_replays += 1
             self.graph_kernels_replayed += self._graph_kernels
         self.it += 1
         return self.it
 
+    def _capture(self):
+        """Capture the step without its window shift (what every step between
+        shifts runs) into a CUDA graph, on a persistent side stream with the
+        graph's own memory pool; unlike torch.cuda.graph() this neither
+        synchronises the device nor empties the allocator's cache."""
+        from . import _lib
+        self._graph = None
+        n0 = _lib.launch_count()
+        g = torch.cuda.CUDAGraph()
+        if self._cap_stream is None:
+            self._cap_stream = torch.cuda.Stream()
+        cur = torch.cuda.current_stream()
+        self._cap_stream.wait_stream(cur)
+        with torch.cuda.stream(self._cap_stream):
+            g.capture_begin()
+            try:
+                self._step_part(graph_mode=True)
+            finally:
+                g.capture_end()
+        cur.wait_stream(self._cap_stream)
+        self._graph_kernels = _lib.launch_count() - n0
+        self._graph = g
+        self._graph_sig = self._signature()
+        self.graph_captures += 1
+        self.graph_kernels_captured += self._graph_kernels
+
     def _body(self, graph_mode):
+        self._frame_part()
+        self._step_part(graph_mode)
+
+    def _frame_part(self):
         self.timer_start()
         for frame in self.frames:
             if np.mod(self.it, frame.Args["Steps"]) == 0:
@@ -143,6 +155,7 @@ class PIC_loop:
                 frame.inject_plasma(species=self.species, grid=self.mainsolver)
         self.timer_record("frame")
 
+    def _step_part(self, graph_mode):
         for parts in self.species:
             self.timer_start()
             parts.push_coords(mode="half")
