@@ -99,3 +99,32 @@ def test_graph_replay_matches_eager(cuda):
             assert torch.equal(v, s1.DataDev[k]), k
     for k in ("x", "y", "z", "px", "py", "pz", "g_inv", "w"):
         assert torch.equal(e0.DataDev[k], e1.DataDev[k]), k
+
+
+class _Host:
+    """numpy view of a product object for the oracle's diagnostics()."""
+
+    def __init__(self, obj):
+        self.Args = obj.Args
+        self.D = {k: to_np(v) for k, v in obj.DataDev.items() if isinstance(v, torch.Tensor)}
+
+
+def test_full_run_diagnostics_fp64(cuda):
+    """The 512 x 64, M = 1 configuration (about 0.5M electrons, a0 = 2 laser,
+    moving window) for 200 steps -- ten window shifts with injection --
+    through the public API and through the oracle: field energy, on-axis Ez
+    wake amplitude and electron kinetic energy within 1e-6 relative."""
+    from oracle.pic_oracle import diagnostics
+    cfg = small_lpa(Nx=512, Nr=64, M=1, seed=21)
+    sol, e, i, loop = build_product(cfg)
+    osol, oe, oi, oloop = build_oracle(cfg)
+    for _ in range(200):
+        loop.step()
+        oloop.step()
+    torch.cuda.synchronize()
+    assert e.Args["Np"] == oe.Args["Np"]
+    got = diagnostics(_Host(sol), [_Host(e)])
+    ref = diagnostics(osol, [oe])
+    for k in ref:
+        err = abs(got[k] / ref[k] - 1.0)
+        assert err < 1e-6, (k, got[k], ref[k], err)
