@@ -255,25 +255,34 @@ __device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, i
 
 // converter: k rows kb*8 .. +7, columns n, n+1 of a raw stage -> one core
 // matrix row (8 k values) of hi and of lo for each column; core matrix
-// (gn = n/8, kb) at (gn*4 + kb)*128, row n%8; hi block, then lo block
-__device__ __forceinline__ void cvt_stage(const float *raw, unsigned char *slot, int kb,
-                                          int ncol_local, uint4 (&o)[4]) {
-  __nv_bfloat16 h[2][8], l[2][8];
+// (gn = n/8, kb) at (gn*4 + kb)*128, row n%8; hi block, then lo block.
+// Pairs of k values are rounded and packed by one cvt.rn.bf16x2 each.
+__device__ __forceinline__ uint32_t bf2_bits(__nv_bfloat162 h) {
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ void cvt_stage(const float *raw, int kb, int ncol_local,
+                                          uint4 (&o)[4]) {
+  float2 t[8];
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    const float2 t = *(const float2 *)(raw + (kb * 8 + q) * UM_TN + ncol_local);
-    h[0][q] = __float2bfloat16_rn(t.x);
-    h[1][q] = __float2bfloat16_rn(t.y);
-    l[0][q] = __float2bfloat16_rn(t.x - __bfloat162float(h[0][q]));
-    l[1][q] = __float2bfloat16_rn(t.y - __bfloat162float(h[1][q]));
-  }
+  for (int q = 0; q < 8; q++) t[q] = *(const float2 *)(raw + (kb * 8 + q) * UM_TN + ncol_local);
+  uint32_t hw[2][4], lw[2][4];
 #pragma unroll
-  for (int c = 0; c < 2; c++) {
-    o[2 * c] = {pack_bf16(h[c][0], h[c][1]), pack_bf16(h[c][2], h[c][3]),
-                pack_bf16(h[c][4], h[c][5]), pack_bf16(h[c][6], h[c][7])};
-    o[2 * c + 1] = {pack_bf16(l[c][0], l[c][1]), pack_bf16(l[c][2], l[c][3]),
-                    pack_bf16(l[c][4], l[c][5]), pack_bf16(l[c][6], l[c][7])};
+  for (int p = 0; p < 4; p++) {
+    // column n (.x) and n+1 (.y), k values 2p and 2p+1 (low half = lower k)
+    const __nv_bfloat162 h0 = __floats2bfloat162_rn(t[2 * p].x, t[2 * p + 1].x);
+    const __nv_bfloat162 h1 = __floats2bfloat162_rn(t[2 * p].y, t[2 * p + 1].y);
+    const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
+    const __nv_bfloat162 l0 = __floats2bfloat162_rn(t[2 * p].x - f0.x, t[2 * p + 1].x - f0.y);
+    const __nv_bfloat162 l1 = __floats2bfloat162_rn(t[2 * p].y - f1.x, t[2 * p + 1].y - f1.y);
+    hw[0][p] = bf2_bits(h0);
+    hw[1][p] = bf2_bits(h1);
+    lw[0][p] = bf2_bits(l0);
+    lw[1][p] = bf2_bits(l1);
   }
+  o[0] = make_uint4(hw[0][0], hw[0][1], hw[0][2], hw[0][3]);
+  o[1] = make_uint4(lw[0][0], lw[0][1], lw[0][2], lw[0][3]);
+  o[2] = make_uint4(hw[1][0], hw[1][1], hw[1][2], hw[1][3]);
+  o[3] = make_uint4(lw[1][0], lw[1][1], lw[1][2], lw[1][3]);
 }
 
 template <bool CPLX, bool ACC>
@@ -347,10 +356,11 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       }
       tc_fence_after();
       const int N = w.ncols[e];
-      const int gm = mt * UM_BM + warp * 32 + lane;
       const int n0 = nt * UM_TN;
-      float *__restrict__ yrow = w.Y[e] + (long)gm * w.ldy[e];
       const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * UM_TN);
+      const int gm = mt * UM_BM + warp * 32 + lane;
+      float *__restrict__ yrow = w.Y[e] + (long)gm * w.ldy[e];
+      // row-contiguous stores: lane = output row, 32 columns per chunk
 #pragma unroll 1
       for (int q = 0; q < UM_TN / 32; q++) {
         float v[32];
@@ -422,12 +432,7 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
         break;
       }
       uint4 o[4];
-      cvt_stage((const float *)(sR + r * UM_RAW), sX + slot * UM_SLOT, kb, ncol_local, o);
-      // the raw slot's values are consumed; the next tensor copy into it
-      // (async proxy) must not overtake these generic-proxy reads, and the
-      // barrier's release alone does not order across proxies
-      fence_async_smem();
-      mbar_arrive(&rempty[r]);
+      cvt_stage((const float *)(sR + r * UM_RAW), kb, ncol_local, o);
       if (s >= UM_NS && !mbar_wait_ab(&empty[slot], ((s / UM_NS) - 1) & 1, abort)) {
         um_fail(abort, 1);
         break;
@@ -437,7 +442,12 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       *(uint4 *)(dst + UM_SLOT / 2) = o[1];  //           lo
       *(uint4 *)(dst + 16) = o[2];         // column n+1 (next core-matrix row)
       *(uint4 *)(dst + 16 + UM_SLOT / 2) = o[3];
+      // one proxy fence orders both hand-offs against the async proxy: the
+      // raw slot's generic-proxy reads before the next tensor copy into it
+      // (the barrier's release alone does not order across proxies), and the
+      // bf16 stores before the MMAs that read them
       fence_async_smem();
+      mbar_arrive(&rempty[r]);
       mbar_arrive(&full[slot]);
     }
   } else if (warp == UM_EPI_WARPS + UM_CVT_WARPS) {
