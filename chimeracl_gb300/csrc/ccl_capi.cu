@@ -352,8 +352,8 @@ int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
 
 int ccl_dht_bf16x3_prepare_bytes(int m, int k, size_t *bytes) {
   NONNULL(bytes);
-  CCL_REQUIRE(m > 0 && k > 0 && k <= 256, CCL_ERR_UNSUPPORTED,
-              "%s: m=%d k=%d (k <= 256)", __func__, m, k);
+  CCL_REQUIRE(m > 0 && k > 0 && k <= 256 && m <= 256, CCL_ERR_UNSUPPORTED,
+              "%s: m=%d k=%d (m, k <= 256)", __func__, m, k);
   *bytes = umma_split_bytes(m, k);
   return CCL_OK;
 }

@@ -2,15 +2,13 @@
 // 5th-generation tensor cores (tcgen05.mma, FP32 accumulation in TMEM):
 //   Y = beta*Y + alpha * (A X),  A ~ A_hi + A_lo,  X ~ X_hi + X_lo  (bf16),
 //   A X ~ A_hi X_hi + A_hi X_lo + A_lo X_hi,
-// A real (m x k, k <= 256), X FP32 (k x ncols real columns, interleaved
+// A real (m x k, m, k <= 256), X FP32 (k x ncols real columns, interleaved
 // complex allowed), Y FP32.
 //
-// The pre-split A (hi then lo per 128-row tile, K-major, no-swizzle
-// core-matrix layout, produced by k_umma_split_a) is bulk-copied into shared
-// memory and stays resident while a CTA walks its N tiles; X is split into
-// bf16 hi/lo on the fly.  Every mbarrier wait is bounded; a wait that gives up
-// records an error code in a device flag, the CTA skips the rest of its work,
-// drains what it issued (bounded) and frees its TMEM.
+// A is split once into bf16 hi/lo (k_umma_split_a); X is split on the fly.
+// Every mbarrier wait is bounded; a wait that gives up records an error code
+// in a device flag, the CTA skips the rest of its work, drains what it issued
+// (bounded) and frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -23,16 +21,11 @@
 
 namespace ccl {
 
-constexpr int UM_BM = 128, UM_BK = 128;
 constexpr int UM_MAXK = 256, UM_MAXBATCH = 32;
 constexpr long UM_SPIN_LIMIT = 20000000L;  // ~ a second of try_wait polls
 
 __device__ int g_umma_error = 0;
 
-// bytes of one pre-split M tile: hi and lo, 128 rows x kp columns of bf16
-__host__ __device__ constexpr long umma_tile_bytes(int kp) { return 2L * UM_BM * kp * 2; }
-
-static inline int umma_kpad(int k) { return k <= UM_BK ? UM_BK : UM_MAXK; }
 
 // ------------------------------------------------------------------ PTX
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -126,29 +119,35 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo_k, __nv_bfloat16 
 }
 
 // ------------------------------------------------------------- A split
-// A (m x k, row-major, lda = k) -> per 128-row tile: hi block then lo block,
-// core matrix (g = row/8, j = col/8) at ((g * kp/8 + j) * 128) bytes, each
-// core matrix 8 rows x 8 consecutive k values.  Zero outside m x k.
+// The matrix A (m x k, row-major, lda = k, m <= 256) is stored for the MMA's
+// B operand, streamed per 32-deep K chunk: chunk c holds a hi block then a lo
+// block of NP x 32 bf16 (NP = 128 or 256 padded rows), K-major no-swizzle
+// core matrices, core matrix (g = row/8, j = (col%32)/8) at (g*4 + j)*128
+// bytes, each 8 rows x 8 consecutive k values.  Zero outside m x k.
+constexpr int UM_KC = 32;  // K depth of one stage
+__host__ __device__ constexpr int umma_np(int m) { return m <= 128 ? 128 : 256; }
+__host__ __device__ constexpr uint32_t umma_chunk_bytes(int np) { return 2u * np * UM_KC * 2; }
+
 template <typename TA>
-__global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int kp, int ntile,
+__global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int np, int nchunk,
                                uint4 *__restrict__ out) {
-  const long per_tile = (long)UM_BM * kp / 8;  // core-matrix rows (16 B) per block
-  const long total = (long)ntile * 2 * per_tile;
+  const long per_block = (long)np * (UM_KC / 8);  // 16-B rows of one hi or lo block
+  const long total = (long)nchunk * 2 * per_block;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < total;
        q += (long)gridDim.x * blockDim.x) {
-    long t = q / (2 * per_tile), rem = q - t * 2 * per_tile;
-    int lo = rem >= per_tile;
-    long w = rem - lo * per_tile;            // 16-B row index within the block
-    long cm = w / 8, i = w - cm * 8;         // core matrix, row within it
-    long g = cm / (kp / 8), j = cm - g * (kp / 8);
-    long row = t * UM_BM + g * 8 + i;
+    const long c = q / (2 * per_block), rem = q - c * 2 * per_block;
+    const int lo = rem >= per_block;
+    const long w = rem - lo * per_block;
+    const long cm = w / 8, i8 = w - cm * 8;
+    const long g = cm / (UM_KC / 8), j = cm - g * (UM_KC / 8);
+    const long row = g * 8 + i8;
     __nv_bfloat16 e[8];
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      long col = j * 8 + c;
-      float v = (row < m && col < k) ? (float)A[row * k + col] : 0.f;
-      __nv_bfloat16 h = __float2bfloat16_rn(v);
-      e[c] = lo ? __float2bfloat16_rn(v - __bfloat162float(h)) : h;
+    for (int t = 0; t < 8; t++) {
+      const long col = c * UM_KC + j * 8 + t;
+      const float v = (row < m && col < k) ? (float)A[row * k + col] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      e[t] = lo ? __float2bfloat16_rn(v - __bfloat162float(h)) : h;
     }
     uint4 o;
     o.x = pack_bf16(e[0], e[1]);
@@ -160,28 +159,31 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int kp, i
 }
 
 // ---------------------------------------------------------------- GEMM
-// Persistent, warp-specialised kernel.  Work item = (batch entry e, 128-row
-// M tile mt, 128-column N tile nt), ordered (e, mt, nt); CTA c takes a
-// contiguous run of items, so the resident A tile is reloaded only when
-// (e, mt) changes (one bulk copy into shared memory).
-//   warps 0-3  epilogue: TMEM lanes 32w..32w+31 (= output rows) -> alpha,
-//              optional +Y, row-contiguous stores
+// Persistent, warp-specialised kernel computing the transpose on the tensor
+// cores, Y^T = X^T A^T: the MMA's M = 128 columns of X (one work item = one
+// 128-column tile of one batch entry), its N = NP rows of A, K = 16 per
+// instruction.  Each X tile is therefore read and converted once for all
+// output rows; A streams per K chunk from L2 (it is shared by every CTA).
+//   warps 0-3  epilogue: TMEM lane = X column n, TMEM column = output row i;
+//              alpha (complex pairs are adjacent columns n, n+1: one shuffle),
+//              optional +Y, stores of 32 consecutive columns of one row per
+//              instruction (128 contiguous bytes)
 //   warps 4-11 converters: raw FP32 stage (32 k x 128 n) -> K-major bf16
-//              hi/lo core matrices in a ring of UM_NS slots.  They issue no
-//              global loads, so their proxy fence has nothing to drain.
-//   warp 12    lane 0: TMA producer, one 2-D tensor copy per stage into a
+//              hi/lo core matrices in a ring of UM_NS slots
+//   warp 12    lane 0: producer -- per stage one 2-D tensor copy of X into a
 //              ring of UM_NR raw slots (out-of-range rows/columns read as 0)
-//   warp 13    lane 0: A bulk copies and the MMAs (3 per 16-deep k step),
-//              double-buffered 128 x 128 FP32 accumulators in TMEM
+//              and one bulk copy of A's K chunk into a ring of UM_NA slots
+//   warp 13    lane 0: the MMAs (X_hi A_hi, X_lo A_hi, X_hi A_lo per 16-deep k
+//              step) into double-buffered 128 x NP FP32 accumulators in TMEM
 // Every wait is bounded (and gives up early once another role has aborted);
 // the MMA thread drains its MMAs and the producer its copies before the CTA
 // releases TMEM and exits.
 constexpr int UM_EPI_WARPS = 4, UM_CVT_WARPS = 8;
 constexpr int UM_THREADS2 = (UM_EPI_WARPS + UM_CVT_WARPS + 2) * 32;  // 448
-constexpr int UM_TN = 128;        // N tile (columns of X / Y)
-constexpr int UM_KC = 32;         // K depth of one stage
-constexpr int UM_NS = 2;          // bf16 slots
-constexpr int UM_NR = 4;          // raw FP32 slots
+constexpr int UM_TN = 128;        // X columns per work item (the MMA's M)
+constexpr int UM_NS = 2;          // bf16 X slots
+constexpr int UM_NR = 4;          // raw FP32 X slots
+constexpr int UM_NA = 3;          // A chunk slots
 constexpr uint32_t UM_SLOT = 2u * UM_KC * UM_TN * 2;  // hi + lo bf16: 16 KB
 constexpr uint32_t UM_RAW = (uint32_t)UM_KC * UM_TN * 4;  // FP32: 16 KB
 constexpr int UM_CVT_THREADS = UM_CVT_WARPS * 32;
@@ -190,10 +192,9 @@ struct UmmaWork {
   const void *A[UM_MAXBATCH];
   float *Y[UM_MAXBATCH];
   int ncols[UM_MAXBATCH];
-  int ntn[UM_MAXBATCH];    // N tiles of the entry
   int base[UM_MAXBATCH];   // first item of the entry
   long ldy[UM_MAXBATCH];
-  int batch, items, mtiles;
+  int batch, items;
 };
 
 // X of every entry as a 2-D tensor map (inner dim = columns, box 128 x 32)
@@ -244,13 +245,10 @@ __device__ __forceinline__ void um_fail(volatile int *abort, int code) {
   *abort = 1;
 }
 
-__device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, int &mt,
-                                          int &nt) {
+__device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, int &nt) {
   e = 0;
   while (e + 1 < w.batch && w.base[e + 1] <= item) e++;
-  const int r = item - w.base[e];
-  mt = r / w.ntn[e];
-  nt = r - mt * w.ntn[e];
+  nt = item - w.base[e];
 }
 
 // converter: k rows kb*8 .. +7, columns n, n+1 of a raw stage -> one core
@@ -285,25 +283,26 @@ __device__ __forceinline__ void cvt_stage(const float *raw, int kb, int ncol_loc
   o[3] = make_uint4(lw[1][0], lw[1][1], lw[1][2], lw[1][3]);
 }
 
-template <bool CPLX, bool ACC>
+template <bool CPLX, bool ACC, int NP>
 __global__ void __launch_bounds__(UM_THREADS2, 1)
-    k_umma_gemm(const __grid_constant__ UmmaArgs args, int M, int K, int KP, int vec_y,
-                float are, float aim) {
+    k_umma_gemm(const __grid_constant__ UmmaArgs args, int M, int K, float are, float aim) {
+  constexpr uint32_t ACH = umma_chunk_bytes(NP);  // A chunk: hi + lo
+  constexpr uint32_t TCOLS = 2 * NP;               // TMEM columns (two accumulators)
   extern __shared__ __align__(1024) unsigned char smraw[];
   const UmmaWork &w = args.w;
   unsigned char *sm = (unsigned char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  const uint32_t a_bytes = (uint32_t)umma_tile_bytes(KP);
-  unsigned char *sA = sm;
-  unsigned char *sX = sA + a_bytes;       // UM_NS bf16 slots
-  unsigned char *sR = sX + UM_NS * UM_SLOT;  // UM_NR raw slots
+  unsigned char *sA = sm;                     // UM_NA A chunks
+  unsigned char *sX = sA + UM_NA * ACH;       // UM_NS bf16 X slots
+  unsigned char *sR = sX + UM_NS * UM_SLOT;   // UM_NR raw X slots
   uint64_t *full = (uint64_t *)(sR + UM_NR * UM_RAW);
   uint64_t *empty = full + UM_NS;
   uint64_t *rfull = empty + UM_NS;
   uint64_t *rempty = rfull + UM_NR;
-  uint64_t *tfull = rempty + UM_NR;  // [2]
+  uint64_t *afull = rempty + UM_NR;
+  uint64_t *aempty = afull + UM_NA;
+  uint64_t *tfull = aempty + UM_NA;  // [2]
   uint64_t *tempty = tfull + 2;      // [2]
-  uint64_t *abar = tempty + 2;
-  uint64_t *dbar = abar + 1;
+  uint64_t *dbar = tempty + 2;
   uint32_t *tmem_slot = (uint32_t *)(dbar + 1);
   volatile int *abort = (volatile int *)(tmem_slot + 1);
 
@@ -314,8 +313,9 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
   const int S = (i1 - i0) * nkc;  // stages of this CTA
 
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-        smem_u32(tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TCOLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
@@ -327,11 +327,14 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       mbar_init(&rfull[i], 1);
       mbar_init(&rempty[i], UM_CVT_THREADS);
     }
+    for (int i = 0; i < UM_NA; i++) {
+      mbar_init(&afull[i], 1);
+      mbar_init(&aempty[i], 1);
+    }
     for (int i = 0; i < 2; i++) {
       mbar_init(&tfull[i], 1);
       mbar_init(&tempty[i], UM_EPI_WARPS * 32);
     }
-    mbar_init(abar, 1);
     mbar_init(dbar, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -346,8 +349,8 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
     // tcgen05.ld is warp-collective: every exit decision is taken warp-wide
     for (int j = 0, item = i0; item < i1; j++, item++) {
       if (__any_sync(0xffffffffu, *abort)) break;
-      int e, mt, nt;
-      um_decode(w, item, e, mt, nt);
+      int e, nt;
+      um_decode(w, item, e, nt);
       const int b = j & 1;
       const bool got = mbar_wait_ab(&tfull[b], (j >> 1) & 1, abort);
       if (!__all_sync(0xffffffffu, got)) {
@@ -356,60 +359,31 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       }
       tc_fence_after();
       const int N = w.ncols[e];
-      const int n0 = nt * UM_TN;
-      const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * UM_TN);
-      const int gm = mt * UM_BM + warp * 32 + lane;
-      float *__restrict__ yrow = w.Y[e] + (long)gm * w.ldy[e];
-      // row-contiguous stores: lane = output row, 32 columns per chunk
+      const int n = nt * UM_TN + warp * 32 + lane;  // this lane's column of X and Y
+      const bool nin = n < N;
+      float *__restrict__ ycol = w.Y[e] + n;
+      const long ldy = w.ldy[e];
+      const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * NP);
+      const int mrow = M < NP ? M : NP;
 #pragma unroll 1
-      for (int q = 0; q < UM_TN / 32; q++) {
-        float v[32];
-        tmem_ld16(tb + q * 32, v);
-        tmem_ld16(tb + q * 32 + 16, v + 16);
+      for (int i0c = 0; i0c < mrow; i0c += 16) {
+        float v[16];
+        tmem_ld16(tb + i0c, v);
         tmem_wait_ld();
-        if (gm < M) {
-          const int c0 = n0 + q * 32;
-          if (vec_y && c0 + 32 <= N) {
 #pragma unroll
-            for (int c = 0; c < 32; c += 4) {
-              float4 r;
-              if (CPLX) {
-                r.x = are * v[c] - aim * v[c + 1];
-                r.y = are * v[c + 1] + aim * v[c];
-                r.z = are * v[c + 2] - aim * v[c + 3];
-                r.w = are * v[c + 3] + aim * v[c + 2];
-              } else {
-                r.x = are * v[c];
-                r.y = are * v[c + 1];
-                r.z = are * v[c + 2];
-                r.w = are * v[c + 3];
-              }
-              if (ACC) {
-                const float4 o = *(const float4 *)(yrow + c0 + c);
-                r.x += o.x; r.y += o.y; r.z += o.z; r.w += o.w;
-              }
-              *(float4 *)(yrow + c0 + c) = r;
-            }
+        for (int t = 0; t < 16; t++) {
+          float r;
+          if (CPLX) {  // (re, im) = columns (n even, n odd): partner via shuffle
+            const float o = __shfl_xor_sync(0xffffffffu, v[t], 1);
+            r = (lane & 1) ? are * v[t] + aim * o : are * v[t] - aim * o;
           } else {
-#pragma unroll
-            for (int c = 0; c < 32; c += 2) {
-              const int gn = c0 + c;
-              if (gn >= N) break;
-              float r0, r1;
-              if (CPLX) {
-                r0 = are * v[c] - aim * v[c + 1];
-                r1 = are * v[c + 1] + aim * v[c];
-              } else {
-                r0 = are * v[c];
-                r1 = are * v[c + 1];
-              }
-              if (ACC) {
-                r0 += yrow[gn];
-                if (gn + 1 < N) r1 += yrow[gn + 1];
-              }
-              yrow[gn] = r0;
-              if (gn + 1 < N) yrow[gn + 1] = r1;
-            }
+            r = are * v[t];
+          }
+          const int i = i0c + t;
+          if (nin && i < M) {
+            float *yp = ycol + (long)i * ldy;
+            if (ACC) r += *yp;
+            *yp = r;
           }
         }
       }
@@ -451,123 +425,111 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       mbar_arrive(&full[slot]);
     }
   } else if (warp == UM_EPI_WARPS + UM_CVT_WARPS) {
-    // ------------------------------------------------- TMA producer (one lane)
+    // --------------------------------------------------- producer (one lane)
     if (lane == 0) {
-      int issued = 0;
+      int issued_x = 0, issued_a = 0;
       for (int s = 0; s < S; s++) {
         if (*abort) break;
-        const int r = s % UM_NR;
+        const int r = s % UM_NR, a = s % UM_NA;
         if (s >= UM_NR && !mbar_wait_ab(&rempty[r], ((s / UM_NR) - 1) & 1, abort)) {
           um_fail(abort, 8);
           break;
         }
-        int e, mt, nt;
-        um_decode(w, i0 + s / nkc, e, mt, nt);
+        int e, nt;
+        um_decode(w, i0 + s / nkc, e, nt);
+        const int kc = s % nkc;
         mbar_expect_tx(&rfull[r], UM_RAW);
-        tma_load_2d(sR + r * UM_RAW, &args.tx[e], nt * UM_TN, (s % nkc) * UM_KC, &rfull[r]);
-        issued = s + 1;
+        tma_load_2d(sR + r * UM_RAW, &args.tx[e], nt * UM_TN, kc * UM_KC, &rfull[r]);
+        issued_x = s + 1;
+        if (s >= UM_NA && !mbar_wait_ab(&aempty[a], ((s / UM_NA) - 1) & 1, abort)) {
+          um_fail(abort, 9);
+          break;
+        }
+        mbar_expect_tx(&afull[a], ACH);
+        bulk_g2s(sA + a * ACH, (const unsigned char *)w.A[e] + (long)kc * ACH, ACH, &afull[a]);
+        issued_a = s + 1;
       }
       // every copy this lane issued has landed before the CTA may exit
-      for (int s = issued - UM_NR < 0 ? 0 : issued - UM_NR; s < issued; s++)
+      for (int s = issued_x - UM_NR < 0 ? 0 : issued_x - UM_NR; s < issued_x; s++)
         (void)mbar_wait(&rfull[s % UM_NR], (s / UM_NR) & 1);
+      for (int s = issued_a - UM_NA < 0 ? 0 : issued_a - UM_NA; s < issued_a; s++)
+        (void)mbar_wait(&afull[s % UM_NA], (s / UM_NA) & 1);
     }
   } else if (lane == 0) {
     // ------------------------------------------------------ MMA (one lane)
-    const uint32_t idesc = umma_idesc(UM_BM, UM_TN);
+    const uint32_t idesc = umma_idesc(UM_TN, NP);
     const uint32_t sA_u = smem_u32(sA), sX_u = smem_u32(sX);
-    const uint32_t a_sbo = (uint32_t)(KP / 8) * 128, a_lo = a_bytes / 2;
-    const uint32_t x_sbo = (UM_KC / 8) * 128;
-    int a_key = -1, a_phase = 0, d_phase = 0, s = 0;
-    bool issued = false;
+    const uint32_t sbo = (UM_KC / 8) * 128;  // 8-row groups, both operands
+    int s = 0;
     for (int j = 0, item = i0; item < i1; j++, item++) {
       if (*abort) break;
-      int e, mt, nt;
-      um_decode(w, item, e, mt, nt);
-      const int key = e * 1024 + mt;
-      if (key != a_key) {
-        if (issued) {  // every MMA reading the old tile has completed
-          umma_commit(dbar);
-          if (!mbar_wait_ab(dbar, d_phase & 1, abort)) { um_fail(abort, 3); break; }
-          d_phase++;
-          issued = false;
-        }
-        const unsigned char *src = (const unsigned char *)w.A[e] + (long)mt * a_bytes;
-        mbar_expect_tx(abar, a_bytes);
-        for (uint32_t off = 0; off < a_bytes; off += 32768u)
-          bulk_g2s(sA + off, src + off, min(32768u, a_bytes - off), abar);
-        // the copy must land before anything else happens in this CTA
-        if (!mbar_wait(abar, a_phase & 1)) { um_fail(abort, 4); break; }
-        a_phase++;
-        a_key = key;
-      }
       const int b = j & 1;
       if (j >= 2 && !mbar_wait_ab(&tempty[b], ((j - 2) >> 1) & 1, abort)) {
         um_fail(abort, 5);
         break;
       }
       tc_fence_after();
-      const uint32_t d = tmem + (uint32_t)(b * UM_TN);
+      const uint32_t d = tmem + (uint32_t)(b * NP);
       bool ok = true;
       for (int kc = 0; kc < nkc; kc++, s++) {
-        const int slot = s % UM_NS;
-        if (!mbar_wait_ab(&full[slot], (s / UM_NS) & 1, abort)) {
+        const int slot = s % UM_NS, a = s % UM_NA;
+        if (!mbar_wait_ab(&full[slot], (s / UM_NS) & 1, abort) ||
+            !mbar_wait_ab(&afull[a], (s / UM_NA) & 1, abort)) {
           um_fail(abort, 6);
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t xs = sX_u + slot * UM_SLOT;
+        const uint32_t xs = sX_u + slot * UM_SLOT, as = sA_u + a * ACH;
 #pragma unroll
         for (int ks = 0; ks < UM_KC / 16; ks++) {
-          const uint32_t ja = (uint32_t)(kc * (UM_KC / 8) + 2 * ks) * 128;
-          const uint64_t ahi = smem_desc(sA_u + ja, 128, a_sbo);
-          const uint64_t alo = smem_desc(sA_u + a_lo + ja, 128, a_sbo);
-          const uint64_t bhi = smem_desc(xs + (uint32_t)(2 * ks) * 128, 128, x_sbo);
-          const uint64_t blo = smem_desc(xs + UM_SLOT / 2 + (uint32_t)(2 * ks) * 128, 128, x_sbo);
-          umma_bf16(d, ahi, bhi, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
-          umma_bf16(d, ahi, blo, idesc, 1u);
-          umma_bf16(d, alo, bhi, idesc, 1u);
+          const uint32_t o = (uint32_t)(2 * ks) * 128;
+          const uint64_t xhi = smem_desc(xs + o, 128, sbo);
+          const uint64_t xlo = smem_desc(xs + UM_SLOT / 2 + o, 128, sbo);
+          const uint64_t ahi = smem_desc(as + o, 128, sbo);
+          const uint64_t alo = smem_desc(as + ACH / 2 + o, 128, sbo);
+          umma_bf16(d, xhi, ahi, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+          umma_bf16(d, xlo, ahi, idesc, 1u);
+          umma_bf16(d, xhi, alo, idesc, 1u);
         }
         umma_commit(&empty[slot]);
-        issued = true;
+        umma_commit(&aempty[a]);
       }
       if (!ok) break;
       umma_commit(&tfull[b]);
     }
     // drain: whatever was issued completes before TMEM is released
     umma_commit(dbar);
-    (void)mbar_wait(dbar, d_phase & 1);
+    (void)mbar_wait(dbar, 0);
   }
   __syncwarp();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS));
 }
 
-static size_t umma_smem(int kp) {
-  return 1024 + umma_tile_bytes(kp) + UM_NS * UM_SLOT + UM_NR * UM_RAW + 256;
+static size_t umma_smem(int np) {
+  return 1024 + UM_NA * umma_chunk_bytes(np) + UM_NS * UM_SLOT + UM_NR * UM_RAW + 256;
 }
 
 size_t umma_split_bytes(int m, int k) {
-  if (k > UM_MAXK) return 0;
-  int kp = umma_kpad(k);
-  long ntile = (m + UM_BM - 1) / UM_BM;
-  return (size_t)(ntile * umma_tile_bytes(kp));
+  if (k > UM_MAXK || m > UM_MAXK || m <= 0 || k <= 0) return 0;
+  const int nchunk = (k + UM_KC - 1) / UM_KC;
+  return (size_t)nchunk * umma_chunk_bytes(umma_np(m));
 }
 
 template <typename TA>
 int umma_split_a(const TA *A, int m, int k, void *out, size_t bytes, cudaStream_t s) {
-  CCL_REQUIRE(k > 0 && k <= UM_MAXK && m > 0, CCL_ERR_UNSUPPORTED,
-              "umma split: m=%d k=%d (k <= %d)", m, k, UM_MAXK);
+  CCL_REQUIRE(k > 0 && k <= UM_MAXK && m > 0 && m <= UM_MAXK, CCL_ERR_UNSUPPORTED,
+              "umma split: m=%d k=%d (m, k <= %d)", m, k, UM_MAXK);
   CCL_REQUIRE(bytes >= umma_split_bytes(m, k), CCL_ERR_WORKSPACE,
               "umma split: %zu < %zu bytes", bytes, umma_split_bytes(m, k));
   CCL_REQUIRE(((uintptr_t)out & 15) == 0, CCL_ERR_ARG, "umma split: output not 16-B aligned");
-  int kp = umma_kpad(k);
-  int ntile = (m + UM_BM - 1) / UM_BM;
-  long total = (long)ntile * 2 * UM_BM * kp / 8;
-  k_umma_split_a<TA><<<grid_for(total, 256), 256, 0, s>>>(A, m, k, kp, ntile, (uint4 *)out);
+  const int np = umma_np(m), nchunk = (k + UM_KC - 1) / UM_KC;
+  const long total = (long)nchunk * 2 * np * (UM_KC / 8);
+  k_umma_split_a<TA><<<grid_for(total, 256), 256, 0, s>>>(A, m, k, np, nchunk, (uint4 *)out);
   CCL_LAUNCH_CHECK("umma_split_a");
   return CCL_OK;
 }
@@ -596,12 +558,24 @@ static int device_sm_count() {
   return n;
 }
 
+template <bool C, bool A_, int NP>
+static void umma_launch(int grid, size_t smem, const UmmaArgs &args, int m, int k, float ar,
+                        float ai, cudaStream_t s) {
+  auto kern = k_umma_gemm<C, A_, NP>;
+  static size_t set_smem = 0;  // the attribute is set once per size, not per launch
+  if (set_smem < smem) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set_smem = smem;
+  }
+  kern<<<grid, UM_THREADS2, smem, s>>>(args, m, k, ar, ai);
+}
+
 int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const void *const *Ap,
                     const void *const *X, const long *ldx, void *const *Y, const long *ldy,
                     double are, double aim, double beta, cudaStream_t s) {
   CCL_REQUIRE(batch >= 0 && batch <= UM_MAXBATCH, CCL_ERR_ARG, "umma: batch %d", batch);
-  CCL_REQUIRE(m > 0 && k > 0 && k <= UM_MAXK, CCL_ERR_UNSUPPORTED,
-              "umma: m=%d k=%d (k <= %d)", m, k, UM_MAXK);
+  CCL_REQUIRE(m > 0 && k > 0 && k <= UM_MAXK && m <= UM_MAXK, CCL_ERR_UNSUPPORTED,
+              "umma: m=%d k=%d (m, k <= %d)", m, k, UM_MAXK);
   CCL_REQUIRE(beta == 0.0 || beta == 1.0, CCL_ERR_ARG, "umma: beta must be 0 or 1");
   if (batch == 0) return CCL_OK;
   static UmmaArgs args;  // host staging of the kernel parameters
@@ -610,8 +584,6 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
   UmmaWork &w = args.w;
   auto encode = encode_tiled();
   CCL_REQUIRE(encode, CCL_ERR_CUDA, "umma: cuTensorMapEncodeTiled unavailable");
-  const int mtiles = (m + UM_BM - 1) / UM_BM;
-  int vec_y = 1;
   long items = 0;
   for (int i = 0; i < batch; i++) {
     CCL_REQUIRE(Ap[i] && X[i] && Y[i], CCL_ERR_ARG, "umma: null operand %d", i);
@@ -635,41 +607,40 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
                   (int)r);
     }
     CCL_REQUIRE(((uintptr_t)Ap[i] & 15) == 0, CCL_ERR_ARG, "umma: entry %d A not aligned", i);
-    if (((uintptr_t)Y[i] & 15) != 0 || ldy[i] % 4 != 0) vec_y = 0;
     w.A[i] = Ap[i];
     w.Y[i] = (float *)Y[i];
     w.ncols[i] = ncols[i];
-    w.ntn[i] = (ncols[i] + UM_TN - 1) / UM_TN;
     w.base[i] = (int)items;
     w.ldy[i] = ldy[i];
-    items += (long)mtiles * w.ntn[i];
+    items += (ncols[i] + UM_TN - 1) / UM_TN;
   }
   CCL_REQUIRE(items < (1L << 30), CCL_ERR_ARG, "umma: %ld work items", items);
   w.batch = batch;
   w.items = (int)items;
-  w.mtiles = mtiles;
-  const int kp = umma_kpad(k);
-  const size_t smem = umma_smem(kp);
   static int sms = 0;
   if (!sms) sms = device_sm_count();
   const int grid = (int)(items < sms ? items : sms);
   const float ar = (float)are, ai = (float)aim;
-#define CCL_UMMA(C, A_)                                                              \
-  {                                                                                  \
-    auto kern = k_umma_gemm<C, A_>;                                                  \
-    static size_t set_smem = 0; /* the attribute is set once per size, not per launch */ \
-    if (set_smem < smem) {                                                           \
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-      set_smem = smem;                                                               \
-    }                                                                                \
-    kern<<<grid, UM_THREADS2, smem, s>>>(args, m, k, kp, vec_y, ar, ai);                \
-  }
-  if (cplx) {
-    if (beta == 1.0) CCL_UMMA(true, true) else CCL_UMMA(true, false)
+  const bool acc = beta == 1.0;
+  if (umma_np(m) == 128) {
+    const size_t smem = umma_smem(128);
+    if (cplx) {
+      if (acc) umma_launch<true, true, 128>(grid, smem, args, m, k, ar, ai, s);
+      else umma_launch<true, false, 128>(grid, smem, args, m, k, ar, ai, s);
+    } else {
+      if (acc) umma_launch<false, true, 128>(grid, smem, args, m, k, ar, ai, s);
+      else umma_launch<false, false, 128>(grid, smem, args, m, k, ar, ai, s);
+    }
   } else {
-    if (beta == 1.0) CCL_UMMA(false, true) else CCL_UMMA(false, false)
+    const size_t smem = umma_smem(256);
+    if (cplx) {
+      if (acc) umma_launch<true, true, 256>(grid, smem, args, m, k, ar, ai, s);
+      else umma_launch<true, false, 256>(grid, smem, args, m, k, ar, ai, s);
+    } else {
+      if (acc) umma_launch<false, true, 256>(grid, smem, args, m, k, ar, ai, s);
+      else umma_launch<false, false, 256>(grid, smem, args, m, k, ar, ai, s);
+    }
   }
-#undef CCL_UMMA
   CCL_LAUNCH_CHECK("umma_gemm");
   return CCL_OK;
 }

@@ -273,7 +273,7 @@ int ccl_dht_gemm_batch(int dtype, int batch, int m, int k, const int *ncols,
  * accumulation), for FP32 operands: A = A_hi + A_lo and X = X_hi + X_lo in
  * bf16, A X ~ A_hi X_hi + A_hi X_lo + A_lo X_hi (relative error ~1e-5).
  * The constant matrix is split once: ccl_dht_bf16x3_prepare writes the
- * split, tiled form of A (m x k, row-major, k <= 256, dtype CCL_F64 or
+ * split, tiled form of A (m x k, row-major, m, k <= 256, dtype CCL_F64 or
  * CCL_F32) into `out` (ccl_dht_bf16x3_prepare_bytes bytes, 16-byte aligned).
  * ccl_dht_bf16x3_gemm_batch then takes prepared matrices and the arguments
  * of ccl_dht_gemm_batch (X rows 16-byte aligned: ldx % 4 == 0).
