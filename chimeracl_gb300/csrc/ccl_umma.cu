@@ -181,12 +181,11 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int np, i
 constexpr int UM_EPI_WARPS = 4, UM_CVT_WARPS = 8;
 constexpr int UM_THREADS2 = (UM_EPI_WARPS + UM_CVT_WARPS + 2) * 32;  // 448
 constexpr int UM_TN = 128;        // X columns per work item (the MMA's M)
-constexpr int UM_NS = 2;          // bf16 X slots
+constexpr int UM_NS = 3;          // bf16 X slots
 constexpr int UM_NR = 4;          // raw FP32 X slots
 constexpr int UM_NA = 3;          // A chunk slots
 constexpr uint32_t UM_SLOT = 2u * UM_KC * UM_TN * 2;  // hi + lo bf16: 16 KB
 constexpr uint32_t UM_RAW = (uint32_t)UM_KC * UM_TN * 4;  // FP32: 16 KB
-constexpr int UM_CVT_THREADS = UM_CVT_WARPS * 32;
 
 struct UmmaWork {
   const void *A[UM_MAXBATCH];
@@ -320,12 +319,12 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
   }
   if (tid == 0) {
     for (int i = 0; i < UM_NS; i++) {
-      mbar_init(&full[i], UM_CVT_THREADS);
+      mbar_init(&full[i], UM_CVT_WARPS);  // one arrival per converter warp
       mbar_init(&empty[i], 1);
     }
     for (int i = 0; i < UM_NR; i++) {
       mbar_init(&rfull[i], 1);
-      mbar_init(&rempty[i], UM_CVT_THREADS);
+      mbar_init(&rempty[i], UM_CVT_WARPS);
     }
     for (int i = 0; i < UM_NA; i++) {
       mbar_init(&afull[i], 1);
@@ -365,13 +364,15 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       const long ldy = w.ldy[e];
       const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * NP);
       const int mrow = M < NP ? M : NP;
+      float *yp = ycol;  // row i of this lane's column
 #pragma unroll 1
-      for (int i0c = 0; i0c < mrow; i0c += 16) {
-        float v[16];
-        tmem_ld16(tb + i0c, v);
+      for (int i0c = 0; i0c < mrow; i0c += 32) {
+        float v[32];
+        tmem_ld16(tb + i0c, v);  // two loads in flight per wait
+        tmem_ld16(tb + i0c + 16, v + 16);
         tmem_wait_ld();
 #pragma unroll
-        for (int t = 0; t < 16; t++) {
+        for (int t = 0; t < 32; t++) {
           float r;
           if (CPLX) {  // (re, im) = columns (n even, n odd): partner via shuffle
             const float o = __shfl_xor_sync(0xffffffffu, v[t], 1);
@@ -379,12 +380,11 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
           } else {
             r = are * v[t];
           }
-          const int i = i0c + t;
-          if (nin && i < M) {
-            float *yp = ycol + (long)i * ldy;
+          if (nin && i0c + t < M) {
             if (ACC) r += *yp;
             *yp = r;
           }
+          yp += ldy;
         }
       }
       tc_fence_before();
@@ -398,16 +398,18 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
     const int ncol_local = 2 * ((cw & 1) * 32 + lane);   // 0..126
     const uint32_t o0 = (uint32_t)(((ncol_local >> 3) * (UM_KC / 8) + kb) * 128 +
                                    (ncol_local & 7) * 16);
+    // exit decisions are taken warp-wide (the loop holds a __syncwarp)
     for (int s = 0; s < S; s++) {
-      if (*abort) break;
+      if (__any_sync(0xffffffffu, *abort)) break;
       const int r = s % UM_NR, slot = s % UM_NS;
-      if (!mbar_wait_ab(&rfull[r], (s / UM_NR) & 1, abort)) {
+      if (!__all_sync(0xffffffffu, mbar_wait_ab(&rfull[r], (s / UM_NR) & 1, abort))) {
         um_fail(abort, 7);
         break;
       }
       uint4 o[4];
       cvt_stage((const float *)(sR + r * UM_RAW), kb, ncol_local, o);
-      if (s >= UM_NS && !mbar_wait_ab(&empty[slot], ((s / UM_NS) - 1) & 1, abort)) {
+      if (s >= UM_NS &&
+          !__all_sync(0xffffffffu, mbar_wait_ab(&empty[slot], ((s / UM_NS) - 1) & 1, abort))) {
         um_fail(abort, 1);
         break;
       }
@@ -419,10 +421,15 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       // one proxy fence orders both hand-offs against the async proxy: the
       // raw slot's generic-proxy reads before the next tensor copy into it
       // (the barrier's release alone does not order across proxies), and the
-      // bf16 stores before the MMAs that read them
+      // bf16 stores before the MMAs that read them.  The warp then arrives
+      // once (256 arrivals on one barrier serialise): __syncwarp orders the
+      // lanes' accesses before lane 0's release.
       fence_async_smem();
-      mbar_arrive(&rempty[r]);
-      mbar_arrive(&full[slot]);
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&rempty[r]);
+        mbar_arrive(&full[slot]);
+      }
     }
   } else if (warp == UM_EPI_WARPS + UM_CVT_WARPS) {
     // --------------------------------------------------- producer (one lane)
