@@ -21,6 +21,7 @@ namespace ccl {
 
 constexpr int DEP_TX = 32, DEP_TR = 8, DEP_THREADS = DEP_TX * DEP_TR;
 constexpr int DEP_NTX = DEP_TX - 1, DEP_NTR = DEP_TR - 1;
+constexpr int DEP_CARVEOUT = 10;  // percent of the unified L1 / shared memory
 
 // One particle's contribution to the 2x2 corner sums of its cell, in the
 // reference's operation order (grid_deposit_m1.cl:105-138 scalar,
@@ -239,6 +240,16 @@ int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
   dim3 grid((g.Nx + DEP_NTX - 1) / DEP_NTX, (g.Nr + DEP_NTR - 1) / DEP_NTR);
   // the reference passes the charge as a signed char (grid_methods_cl.py:259)
   T q = (T)(signed char)charge;
+  {
+    // the per-lane particle streams are re-read from L1 across a cell's
+    // particles: ask for the smallest shared-memory carve-out (largest L1)
+    static bool set = false;  // per instantiation, once
+    if (!set) {
+      cudaFuncSetAttribute(k_deposit<T, M, VEC>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           DEP_CARVEOUT);
+      set = true;
+    }
+  }
   k_deposit<T, M, VEC><<<grid, DEP_THREADS, 0, s>>>(sort_indx, cell_off, x, y, z, ux, uy, uz,
                                                     g_inv, w, q, g, f);
   CCL_LAUNCH_CHECK("deposit");
@@ -511,10 +522,16 @@ int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
   int nb = grid_for(np, 256, 16);
   T dt = (T)factor_push;
 #define CCL_GP(MM)                                                                     \
-  if constexpr (sizeof(T) == 4)                                                        \
+  if constexpr (sizeof(T) == 4) {                                                      \
+    static bool set = false; /* no shared memory: all of it as L1, set once */          \
+    if (!set) {                                                                        \
+      cudaFuncSetAttribute(k_gather_push_f32<MM>,                                      \
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 0);         \
+      set = true;                                                                      \
+    }                                                                                  \
     k_gather_push_f32<MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx, \
                                              np_stay, dt, g, f);                       \
-  else                                                                                 \
+  } else                                                                               \
     k_gather_push<T, MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx,  \
                                             np_stay, dt, g, f)
   switch (M) {
