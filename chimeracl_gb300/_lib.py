@@ -42,6 +42,8 @@ SIGNATURES = {
     "ccl_warp_axis": [_i, _i, _i, _pp, _i, _vp],
     "ccl_gather_push": [_i, _i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d,
                         _i, _d, _d, _i, _d, _d, _pp, _vp],
+    "ccl_gather_push_cells": [_i, _i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                              _d, _i, _d, _d, _i, _d, _d, _pp, _vp],
     "ccl_phase": [_i, _i, _vp, _vp, _d, _i, _vp],
     "ccl_fft_forward_rows": [_i, _i, _i, _vp, _l, _i, _vp, _vp, _vp, _vp],
     "ccl_fft_backward_rows": [_i, _i, _i, _vp, _vp, _l, _i, _vp, _vp],

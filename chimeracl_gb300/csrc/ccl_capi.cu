@@ -221,6 +221,26 @@ int ccl_gather_push(int dtype, int M, long np, const void *x, const void *y,
                                      S(stream)));
 }
 
+int ccl_gather_push_cells(int dtype, int M, long np, const void *x, const void *y,
+                          const void *z, void *px, void *py, void *pz, void *g_inv,
+                          const uint32_t *sort_indx, const uint32_t *cell_offset,
+                          const uint32_t *np_stay, double factor_push, int Nx,
+                          double xmin, double dx_inv, int Nr, double rmin,
+                          double dr_inv, const void *const *flds, void *stream) {
+  DTYPE_CHECK(dtype);
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "%s: M=%d", __func__, M);
+  NONNEG(np);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  if (np == 0) return CCL_OK;
+  NONNULL(x); NONNULL(y); NONNULL(z); NONNULL(px); NONNULL(py); NONNULL(pz);
+  NONNULL(g_inv); NONNULL(sort_indx); NONNULL(cell_offset); NONNULL(np_stay);
+  NONNULL(flds);
+  return DISPATCH(dtype, gather_push_cells(M, np, x, y, z, px, py, pz, g_inv, sort_indx,
+                                           cell_offset, np_stay, factor_push, Nx, xmin,
+                                           dx_inv, Nr, rmin, dr_inv, flds, S(stream)));
+}
+
 // ----------------------------------------------------------------- spectral
 int ccl_phase(int dtype, int nx, void *phs, const double *kx, double x0,
               int sign, void *stream) {

@@ -508,6 +508,154 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// FP32 form, cell tile by cell tile: one CTA per tile of 32 x 8 cells (the
+// deposit's tiling without its halo).  The 33 x 9 nodes' E and B over all
+// modes are staged in shared memory once (mode m >= 1 already doubled); the
+// tile's particles -- one contiguous range of sort_indx per tile row, from
+// cell_offset -- are then taken by consecutive threads (coalesced), and each
+// interpolates from shared memory.  The row comes from the sort; the column
+// from the particle's x with the sort's own formula, clamped to the tile.
+constexpr int GT_TX = 32, GT_TR = 8, GT_THREADS = 256;
+constexpr int GT_NX = GT_TX + 1, GT_NR = GT_TR + 1;
+__host__ __device__ constexpr int gt_stride(int M) {  // floats per staged node, 16-B multiple
+  return ((6 * (1 + 2 * M)) + 3) & ~3;
+}
+
+template <int M>
+__global__ void __launch_bounds__(GT_THREADS)
+    k_gather_push_tiled(const float *__restrict__ x, const float *__restrict__ y,
+                        const float *__restrict__ z, float *__restrict__ px,
+                        float *__restrict__ py, float *__restrict__ pz,
+                        float *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
+                        const u32 *__restrict__ cell_off, const u32 *__restrict__ np_stay_p,
+                        float dt, GridP<float> g, ptrs<24> f) {
+  constexpr int NS = gt_stride(M);
+  extern __shared__ __align__(16) float gsm[];  // [GT_NR][GT_NX][NS]
+  __shared__ u32 row_a[GT_TR], row_pre[GT_TR + 1];
+  const int Nx = g.Nx, Nr = g.Nr, nxc = Nx - 1;
+  const int nx0 = blockIdx.x * GT_TX, nr0 = blockIdx.y * GT_TR;
+  const u32 np_stay = *np_stay_p;
+  // 1. node tile: [ex ey ez bx by bz] (m = 0), then per mode m >= 1 the same
+  //    six as 2*(re, im)
+  for (int t = threadIdx.x; t < GT_NR * GT_NX; t += GT_THREADS) {
+    const int lr = t / GT_NX, lc = t - lr * GT_NX;
+    const int nr = nr0 + lr, nx = nx0 + lc;
+    float *d = gsm + t * NS;
+    const bool in = nr < Nr && nx < Nx;
+    const long node = (long)nr * Nx + nx;
+#pragma unroll
+    for (int k = 0; k < 6; k++) d[k] = in ? __ldg((const float *)f.p[k] + node) : 0.f;
+#pragma unroll
+    for (int m = 1; m <= M; m++)
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const float2 v = in ? __ldg((const float2 *)f.p[6 * m + k] + node) : make_float2(0.f, 0.f);
+        d[6 + 12 * (m - 1) + 2 * k] = 2.f * v.x;
+        d[6 + 12 * (m - 1) + 2 * k + 1] = 2.f * v.y;
+      }
+  }
+  // 2. the tile's valid cells per row: 0 < ix < Nx-2, 0 <= ir < Nr-2
+  const int ixl = nx0 > 1 ? nx0 : 1, ixh = nx0 + GT_TX - 1 < Nx - 3 ? nx0 + GT_TX - 1 : Nx - 3;
+  if (threadIdx.x < GT_TR) {
+    const int ir = nr0 + threadIdx.x;
+    u32 a = 0, b = 0;
+    if (ir < Nr - 2 && ixl <= ixh) {
+      a = cell_off[(long)ixl + (long)ir * nxc];
+      b = cell_off[(long)ixh + (long)ir * nxc + 1];
+    }
+    row_a[threadIdx.x] = a;
+    row_pre[threadIdx.x + 1] = b - a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    row_pre[0] = 0;
+    for (int r = 0; r < GT_TR; r++) row_pre[r + 1] += row_pre[r];
+  }
+  __syncthreads();
+  const u32 total = row_pre[GT_TR];
+  const float dt_2 = 0.5f * dt;
+  for (u32 idx = threadIdx.x; idx < total; idx += GT_THREADS) {
+    int r = 0;
+#pragma unroll
+    for (int q = 1; q < GT_TR; q++) r += idx >= row_pre[q];
+    const u32 pos = row_a[r] + (idx - row_pre[r]);
+    const u32 p = __ldg(sort_indx + pos);
+    if (p >= np_stay) continue;  // grid_deposit_m1.cl:367-368
+    const float xp = x[p], yp = y[p], zp = z[p];
+    const float r2 = yp * yp + zp * zp;
+    const float rp = sqrtf(r2);
+    const float rinv = r2 > 0.f ? 1.f / rp : __int_as_float(0x7f800000);
+    const float fx = (xp - g.xmin) * g.dx_inv, fr = (rp - g.rmin) * g.dr_inv;
+    int ix = (int)floorf(fx);
+    ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
+    const int ir = nr0 + r;
+    const float sX1 = fx - (float)ix, sX0 = 1.f - sX1;
+    const float sR1 = fr - (float)ir, sR0 = 1.f - sR1;
+    const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+    const int l0 = (r * GT_NX + (ix - nx0)) * NS;
+    const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};
+    float e[M + 1][2];
+    if (M >= 1) {
+      e[1][0] = yp * rinv;
+      e[1][1] = -zp * rinv;
+    }
+#pragma unroll
+    for (int m = 2; m <= M; m++) {
+      e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+      e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+    }
+    float fld[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      float a = 0.f;
+#pragma unroll
+      for (int c = 0; c < 4; c++) a = fmaf(C[c], gsm[loff[c] + k], a);
+#pragma unroll
+      for (int m = 1; m <= M; m++) {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          re = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k], re);
+          im = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k + 1], im);
+        }
+        a = fmaf(re, e[m][0], a);
+        a = fmaf(-im, e[m][1], a);
+      }
+      fld[k] = a;
+    }
+    // Boris push (grid_deposit_m1.cl:440-505)
+    float um[3];
+    um[0] = px[p] + dt_2 * fld[0];
+    um[1] = py[p] + dt_2 * fld[1];
+    um[2] = pz[p] + dt_2 * fld[2];
+    const float gi0 = rsqrtf(1.f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+    float t[3], sv[3], u0[3], up[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) t[k] = dt_2 * fld[3 + k] * gi0;
+    const float f2 = __fdividef(2.f, 1.f + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
+    u0[0] = um[0] + um[1] * t[2] - um[2] * t[1];
+    u0[1] = um[1] - um[0] * t[2] + um[2] * t[0];
+    u0[2] = um[2] + um[0] * t[1] - um[1] * t[0];
+    up[0] = um[0] + u0[1] * sv[2] - u0[2] * sv[1];
+    up[1] = um[1] - u0[0] * sv[2] + u0[2] * sv[0];
+    up[2] = um[2] + u0[0] * sv[1] - u0[1] * sv[0];
+    const float u[3] = {up[0] + dt_2 * fld[0], up[1] + dt_2 * fld[1], up[2] + dt_2 * fld[2]};
+    px[p] = u[0];
+    py[p] = u[1];
+    pz[p] = u[2];
+    g_inv[p] = rsqrtf(1.f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  }
+}
+
+// with the sort's cell offsets: the FP32 form runs tile by tile, the FP64
+// form is the exact kernel above
+template <typename T>
+int gather_push_cells(int M, long np, const T *x, const T *y, const T *z, T *px, T *py, T *pz,
+                      T *g_inv, const u32 *sort_indx, const u32 *cell_off, const u32 *np_stay,
+                      double factor_push, GridP<T> g, const void *const *flds, cudaStream_t s);
+
 template <typename T>
 int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
                 T *py, T *pz, T *g_inv, const u32 *sort_indx,
@@ -546,6 +694,48 @@ int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
 #undef CCL_GP
   CCL_LAUNCH_CHECK("gather_push");
   return CCL_OK;
+}
+
+template <typename T>
+int gather_push_cells(int M, long np, const T *x, const T *y, const T *z, T *px, T *py, T *pz,
+                      T *g_inv, const u32 *sort_indx, const u32 *cell_off, const u32 *np_stay,
+                      double factor_push, GridP<T> g, const void *const *flds, cudaStream_t s) {
+  if constexpr (sizeof(T) == 8) {
+    (void)cell_off;
+    return gather_push<T>(M, np, x, y, z, px, py, pz, g_inv, sort_indx, np_stay, factor_push, g,
+                          flds, s);
+  } else {
+    if (np == 0) return CCL_OK;
+    CCL_REQUIRE(M >= 0 && M <= 3, CCL_ERR_UNSUPPORTED, "gather: M=%d not supported (0..3)", M);
+    ptrs<24> f;
+    for (int i = 0; i < 6 * (M + 1); i++) {
+      CCL_REQUIRE(flds[i], CCL_ERR_ARG, "gather: null field pointer %d", i);
+      f.p[i] = (void *)flds[i];
+    }
+    dim3 grid((g.Nx + GT_TX - 1) / GT_TX, (g.Nr + GT_TR - 1) / GT_TR);
+    const float dt = (float)factor_push;
+#define CCL_GT(MM)                                                                         \
+  {                                                                                        \
+    const size_t smem = (size_t)GT_NR * GT_NX * gt_stride(MM) * sizeof(float);            \
+    auto kern = k_gather_push_tiled<MM>;                                                   \
+    static bool set = false; /* once per instantiation */                                  \
+    if (!set) {                                                                            \
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
+      set = true;                                                                          \
+    }                                                                                      \
+    kern<<<grid, GT_THREADS, smem, s>>>(x, y, z, px, py, pz, g_inv, sort_indx, cell_off,    \
+                                        np_stay, dt, g, f);                                \
+  }
+    switch (M) {
+      case 0: CCL_GT(0); break;
+      case 1: CCL_GT(1); break;
+      case 2: CCL_GT(2); break;
+      default: CCL_GT(3); break;
+    }
+#undef CCL_GT
+    CCL_LAUNCH_CHECK("gather_push_tiled");
+    return CCL_OK;
+  }
 }
 
 }  // namespace ccl

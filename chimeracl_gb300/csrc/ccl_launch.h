@@ -86,6 +86,13 @@ template <typename T> struct Ops {
                          double xmin, double dx_inv, int Nr, double rmin,
                          double dr_inv, const void *const *flds,
                          cudaStream_t s);
+  static int gather_push_cells(int M, long np, const void *x, const void *y,
+                               const void *z, void *px, void *py, void *pz,
+                               void *g_inv, const uint32_t *sort_indx,
+                               const uint32_t *cell_offset, const uint32_t *np_stay,
+                               double factor_push, int Nx, double xmin,
+                               double dx_inv, int Nr, double rmin, double dr_inv,
+                               const void *const *flds, cudaStream_t s);
   static int psatd(long n, double dt_inv, const void *c1, const void *c2,
                    const void *c3, void *const *flds, cudaStream_t s);
   static int phase(int nx, void *phs, const double *kx, double x0, int sign,

@@ -141,6 +141,20 @@ int Ops<T>::gather_push(int M, long np, const void *x, const void *y,
 }
 
 template <typename T>
+int Ops<T>::gather_push_cells(int M, long np, const void *x, const void *y,
+                              const void *z, void *px, void *py, void *pz,
+                              void *g_inv, const uint32_t *sort_indx,
+                              const uint32_t *cell_offset, const uint32_t *np_stay,
+                              double factor_push, int Nx, double xmin,
+                              double dx_inv, int Nr, double rmin, double dr_inv,
+                              const void *const *flds, cudaStream_t s) {
+  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
+  return ccl::gather_push_cells<T>(M, np, (const T *)x, (const T *)y, (const T *)z,
+                                   (T *)px, (T *)py, (T *)pz, (T *)g_inv, sort_indx,
+                                   cell_offset, np_stay, factor_push, g, flds, s);
+}
+
+template <typename T>
 int Ops<T>::psatd(long n, double dt_inv, const void *c1, const void *c2,
                   const void *c3, void *const *flds, cudaStream_t s) {
   ptrs<15> f;

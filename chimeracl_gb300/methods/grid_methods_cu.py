@@ -82,8 +82,9 @@ class GridMethodsCU(GenericMethodsCU):
         D, M = parts.DataDev, self.Args["M"]
         f = [self.DataDev[fl + c + "_m" + str(m)]
              for m in range(M + 1) for fl in flds for c in self.Args["vec_comps"]]
-        call("ccl_gather_push", self._dt, M, parts.Args["Np"], D["x"].data_ptr(),
+        # with the sort's cell offsets (the FP32 form runs tile by tile)
+        call("ccl_gather_push_cells", self._dt, M, parts.Args["Np"], D["x"].data_ptr(),
              D["y"].data_ptr(), D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(),
              D["pz"].data_ptr(), D["g_inv"].data_ptr(), D["sort_indx"].data_ptr(),
-             D["Np_stay_dev"].data_ptr(), float(parts.Args["FactorPush"]),
-             *self._grid_scalars(), PP(f), stream())
+             D["cell_offset"].data_ptr(), D["Np_stay_dev"].data_ptr(),
+             float(parts.Args["FactorPush"]), *self._grid_scalars(), PP(f), stream())

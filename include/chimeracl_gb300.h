@@ -182,6 +182,18 @@ int ccl_gather_push(int dtype, int M, long np, const void *x, const void *y,
                     int Nr, double rmin, double dr_inv,
                     const void *const *flds, void *stream);
 
+/* ccl_gather_push with the cell offsets of the sort (cell_offset from
+ * ccl_index_sort, which the reference's gather does not take): the FP32 form
+ * then runs tile by tile (32 x 8 cells per CTA, the tile's E and B staged in
+ * shared memory, the tile's particles taken in sort order); the FP64 form is
+ * ccl_gather_push.  Same outputs and skip rules. */
+int ccl_gather_push_cells(int dtype, int M, long np, const void *x, const void *y,
+                          const void *z, void *px, void *py, void *pz, void *g_inv,
+                          const uint32_t *sort_indx, const uint32_t *cell_offset,
+                          const uint32_t *np_stay, double factor_push, int Nx,
+                          double xmin, double dx_inv, int Nr, double rmin,
+                          double dr_inv, const void *const *flds, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Spectral transforms  (chimeraCL/methods/transformer_methods_cl.py)  */
 /* ------------------------------------------------------------------ */

@@ -374,11 +374,13 @@ def test_gather_push_bit_exact(cuda, port, M):
         np.testing.assert_array_equal(host(pd[k]), ref[k], err_msg=k)
 
 
-@pytest.mark.parametrize("M", [0, 1, 2])
-def test_gather_push_fp32(cuda, port, M):
+@pytest.mark.parametrize("cells", [False, True])
+@pytest.mark.parametrize("M", [0, 1, 2, 3])
+def test_gather_push_fp32(cuda, port, M, cells):
     """The FP32 gather + Boris kernel against the FP64 oracle on the same
     FP32-rounded inputs (no particles exactly on cell faces, where the two
-    precisions may pick different but equivalent cells)."""
+    precisions may pick different but equivalent cells); `cells` runs the
+    tiled form (ccl_gather_push_cells)."""
     rng = np.random.default_rng(50 + M)
     g = geom(128, 32)
     p = {k: to64(to32(v)) for k, v in particles(rng, 50000, g, boundaries=False).items()}
@@ -395,10 +397,17 @@ def test_gather_push_fp32(cuda, port, M):
     pd = {k: dev(to32(v)) for k, v in p.items()}
     fd = [dev(to32(f[k])) for k in order]
     nst = torch.tensor([np_stay], dtype=torch.int32, device="cuda")
-    call("ccl_gather_push", CCL_F32, M, p["x"].size, pd["x"].data_ptr(), pd["y"].data_ptr(),
-         pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(), pd["pz"].data_ptr(),
-         pd["g_inv"].data_ptr(), dev(srt).data_ptr(), nst.data_ptr(), fp, g["Nx"], g["Xmin"],
-         g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], PP(fd), S())
+    if cells:
+        call("ccl_gather_push_cells", CCL_F32, M, p["x"].size, pd["x"].data_ptr(),
+             pd["y"].data_ptr(), pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(),
+             pd["pz"].data_ptr(), pd["g_inv"].data_ptr(), dev(srt).data_ptr(),
+             dev(off).data_ptr(), nst.data_ptr(), fp, g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"],
+             g["Rmin"], g["dr_inv"], PP(fd), S())
+    else:
+        call("ccl_gather_push", CCL_F32, M, p["x"].size, pd["x"].data_ptr(), pd["y"].data_ptr(),
+             pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(), pd["pz"].data_ptr(),
+             pd["g_inv"].data_ptr(), dev(srt).data_ptr(), nst.data_ptr(), fp, g["Nx"],
+             g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"], PP(fd), S())
     for k in ref:
         got = to64(host(pd[k]))
         err = np.abs(got - ref[k]).max() / np.abs(ref[k]).max()
