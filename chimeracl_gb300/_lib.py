@@ -62,6 +62,7 @@ SIGNATURES = {
     "ccl_grad_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _vp],
     "ccl_rot_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _pp, _vp],
     "ccl_set": [_i, _i, _l, _vp, _d, _d, _vp],
+    "ccl_set_batch": [_i, _i, C.POINTER(C.c_int), C.POINTER(C.c_long), _pp, _d, _d, _vp],
     "ccl_append_c2c": [_i, _l, _vp, _vp, _vp],
     "ccl_zpaxz": [_i, _l, _vp, _d, _d, _vp, _vp],
     "ccl_axpbyz": [_i, _l, _d, _d, _vp, _d, _d, _vp, _vp, _vp],

@@ -446,6 +446,20 @@ int ccl_set(int dtype, int cplx, long n, void *a, double re, double im,
   return DISPATCH(dtype, set(cplx, n, a, re, im, S(stream)));
 }
 
+int ccl_set_batch(int dtype, int narr, const int *cplx, const long *n,
+                  void *const *a, double re, double im, void *stream) {
+  DTYPE_CHECK(dtype);
+  CCL_REQUIRE(narr >= 0 && narr <= 32, CCL_ERR_ARG, "%s: narr %d outside [0, 32]", __func__,
+              narr);
+  if (narr == 0) return CCL_OK;
+  NONNULL(cplx); NONNULL(n); NONNULL(a);
+  for (int i = 0; i < narr; i++) {
+    CCL_REQUIRE(n[i] >= 0, CCL_ERR_ARG, "%s: n[%d] = %ld", __func__, i, n[i]);
+    CCL_REQUIRE(n[i] == 0 || a[i], CCL_ERR_ARG, "%s: a[%d] is NULL", __func__, i);
+  }
+  return DISPATCH(dtype, set_batch(narr, cplx, n, a, re, im, S(stream)));
+}
+
 int ccl_append_c2c(int dtype, long n, void *base, const void *add,
                    void *stream) {
   DTYPE_CHECK(dtype);

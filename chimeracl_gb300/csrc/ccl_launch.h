@@ -101,6 +101,8 @@ template <typename T> struct Ops {
                     cudaStream_t s);
   static int set(int cplx, long n, void *a, double re, double im,
                  cudaStream_t s);
+  static int set_batch(int narr, const int *cplx, const long *n, void *const *a, double re,
+                       double im, cudaStream_t s);
   static int append(long n, void *base, const void *add, cudaStream_t s);
   static int zpaxz(long n, void *z, double are, double aim, const void *x,
                    cudaStream_t s);

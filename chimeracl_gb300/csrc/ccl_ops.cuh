@@ -197,6 +197,24 @@ int Ops<T>::set(int cplx, long n, void *a, double re, double im,
 }
 
 template <typename T>
+int Ops<T>::set_batch(int narr, const int *cplx, const long *n, void *const *a, double re,
+                      double im, cudaStream_t s) {
+  SetBatch b;
+  long nmax = 0;
+  for (int i = 0; i < narr; i++) {
+    b.a[i] = a[i];
+    b.n[i] = n[i];
+    b.cplx[i] = cplx[i];
+    if (n[i] > nmax) nmax = n[i];
+  }
+  if (nmax == 0) return CCL_OK;
+  dim3 grid((unsigned)((grid_for(nmax, 256) + narr - 1) / narr), (unsigned)narr);
+  k_set_batch<T><<<grid, 256, 0, s>>>(b, (T)re, (T)im);
+  CCL_LAUNCH_CHECK("set_batch");
+  return CCL_OK;
+}
+
+template <typename T>
 int Ops<T>::append(long n, void *base, const void *add, cudaStream_t s) {
   if (n == 0) return CCL_OK;
   k_append<T><<<grid_for(n, 256), 256, 0, s>>>(n, (T *)base, (const T *)add);

@@ -3,6 +3,7 @@
 // compiled with -fmad=false so that every expression rounds exactly as the
 // reference kernels written in strict IEEE arithmetic do.
 #pragma once
+#include <type_traits>
 #include "ccl_common.cuh"
 
 namespace ccl {
@@ -13,8 +14,32 @@ template <typename T>
 __global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
                          T *__restrict__ z, const T *__restrict__ px,
                          const T *__restrict__ py, const T *__restrict__ pz,
-                         const T *__restrict__ g_inv, T dt) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+                         const T *__restrict__ g_inv, T dt, int vec) {
+  // 16-byte vectors of VW particles when every array is 16-byte aligned, the
+  // per-particle arithmetic of push_xyz unchanged; the tail one by one
+  constexpr int VW = 16 / sizeof(T);
+  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const long nv = vec ? np / VW : 0;
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nv;
+       v += (long)gridDim.x * blockDim.x) {
+    V gx = ((const V *)g_inv)[v], ux = ((const V *)px)[v], uy = ((const V *)py)[v],
+      uz = ((const V *)pz)[v];
+    V xx = ((V *)x)[v], yy = ((V *)y)[v], zz = ((V *)z)[v];
+    T *g = (T *)&gx, *a = (T *)&ux, *b = (T *)&uy, *c = (T *)&uz;
+    T *xo = (T *)&xx, *yo = (T *)&yy, *zo = (T *)&zz;
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      T dt_g = dt * g[q];
+      T ddx = a[q] * dt_g, ddy = b[q] * dt_g, ddz = c[q] * dt_g;
+      xo[q] = xo[q] + ddx;
+      yo[q] = yo[q] + ddy;
+      zo[q] = zo[q] + ddz;
+    }
+    ((V *)x)[v] = xx;
+    ((V *)y)[v] = yy;
+    ((V *)z)[v] = zz;
+  }
+  for (long i = nv * VW + blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
        i += (long)gridDim.x * blockDim.x) {
     T dt_g = dt * g_inv[i];
     T ddx = px[i] * dt_g, ddy = py[i] * dt_g, ddz = pz[i] * dt_g;
@@ -27,16 +52,18 @@ __global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
 template <typename T>
 int push_x(long np, T *x, T *y, T *z, const T *px, const T *py, const T *pz,
            const T *g_inv, double dt, cudaStream_t s) {
+  // the vector path needs 16-byte aligned arrays (device allocations are)
+  const uintptr_t mis = ((uintptr_t)x | (uintptr_t)y | (uintptr_t)z | (uintptr_t)px |
+                         (uintptr_t)py | (uintptr_t)pz | (uintptr_t)g_inv) & 15;
   if (np == 0) return CCL_OK;
   k_push_x<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv,
-                                                 (T)dt);
+                                                 (T)dt, mis == 0);
   CCL_LAUNCH_CHECK("push_x");
   return CCL_OK;
 }
 
 // ---------------------------------------------------------------------
-// Cell key of a particle (particles_generic.cl:106-125).  Coordinates are
-// converted to double so that the FP32 form sorts with the same key rule.
+// Cell key of a particle (particles_generic.cl:106-125).
 // Grid geometry in the particles' own precision (converted once on the
 // host: the FP32 kernels then never touch the FP64 pipe)
 template <typename T>

@@ -107,6 +107,27 @@ __global__ void k_set(long n, int cplxf, T *a, T re, T im) {
   }
 }
 
+// set over a batch of arrays: blockIdx.y = array
+struct SetBatch {
+  void *a[32];
+  long n[32];
+  int cplx[32];
+};
+template <typename T>
+__global__ void k_set_batch(SetBatch b, T re, T im) {
+  const int e = blockIdx.y;
+  T *a = (T *)b.a[e];
+  const long n = b.n[e];
+  if (b.cplx[e]) {
+    CCL_GRID_STRIDE(i, n) {
+      a[2 * i] = re;
+      a[2 * i + 1] = im;
+    }
+  } else {
+    CCL_GRID_STRIDE(i, n) a[i] = re;
+  }
+}
+
 // append_c2c (generic.cl:18-29)
 template <typename T>
 __global__ void k_append(long n, T *base, const T *add) {

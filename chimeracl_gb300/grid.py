@@ -21,17 +21,15 @@ class Grid(GridMethodsCU):
     def depose_charge(self, species=()):
         """rho = sum over species of the charge deposit, then axis and 1/dV
         (grid.py:23-31)."""
-        for m in range(self.Args["M"] + 1):
-            self.set_to(self.DataDev["rho_m" + str(m)], 0)
+        self.set_many([self.DataDev["rho_m" + str(m)] for m in range(self.Args["M"] + 1)], 0)
         for parts in species:
             self.depose_scalar(parts, "w", "rho", charge=parts.Args["charge"])
         self.postproc_depose_scalar("rho")
 
     def depose_currents(self, species=()):
         """J from the mobile species (grid.py:33-54)."""
-        for m in range(self.Args["M"] + 1):
-            for c in self.Args["vec_comps"]:
-                self.set_to(self.DataDev["J" + c + "_m" + str(m)], 0)
+        self.set_many([self.DataDev["J" + c + "_m" + str(m)]
+                       for m in range(self.Args["M"] + 1) for c in self.Args["vec_comps"]], 0)
         mom = ["p" + c for c in self.Args["vec_comps"]]
         for parts in species:
             if "Immobile" in parts.Args:

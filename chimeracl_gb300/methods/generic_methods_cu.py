@@ -10,7 +10,7 @@ import numpy as np
 import torch
 
 from .. import _lib
-from .._lib import CCL_F32, CCL_F64, P, call, stream
+from .._lib import CCL_F32, CCL_F64, P, PP, call, ints, longs, stream
 
 _NP2TORCH = {
     np.dtype(np.float64): torch.float64,
@@ -188,6 +188,17 @@ class GenericMethodsCU:
             return
         c = complex(val)
         call("ccl_set", dt, int(arr.is_complex()), arr.numel(), P(arr), c.real, c.imag, stream())
+
+    def set_many(self, arrs, val):
+        """set_to on several arrays of one dtype in one launch."""
+        dt = self._ccl_of(arrs[0])
+        if dt is None or len(arrs) > 32:
+            for a in arrs:
+                self.set_to(a, val)
+            return
+        c = complex(val)
+        call("ccl_set_batch", dt, len(arrs), ints([int(a.is_complex()) for a in arrs]),
+             longs([a.numel() for a in arrs]), PP(arrs), c.real, c.imag, stream())
 
     def cast_array_c2d(self, arr_in, arr_out):
         call("ccl_cast_c2d", self._ccl_of(arr_in), arr_in.numel(), P(arr_in), P(arr_out), stream())

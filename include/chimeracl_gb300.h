@@ -346,6 +346,11 @@ int ccl_rot_combine(int dtype, int M, int nrows, int nx, const void *kx,
  * Replaces set_to (generic_methods_cl.py:96-105). */
 int ccl_set(int dtype, int cplx, long n, void *a, double re, double im,
             void *stream);
+/* ccl_set over `narr` arrays (narr <= 32) in one launch: array i has n[i]
+ * elements at a[i], complex when cplx[i].  For the zeroing of the deposit
+ * targets (grid.py:23-54), one launch instead of one per array and mode. */
+int ccl_set_batch(int dtype, int narr, const int *cplx, const long *n,
+                  void *const *a, double re, double im, void *stream);
 /* base += add (complex n).  append_c2c, generic.cl:18-29. */
 int ccl_append_c2c(int dtype, long n, void *base, const void *add,
                    void *stream);
