@@ -334,9 +334,20 @@ __device__ __forceinline__ void fft_reg(cplx<T> (&v)[8], cplx<T> *sm,
   for (int p = 0; p < F::P8; p++) {
     const int k = j & (Ns - 1);
     if (p > 0) {
+      // W^(r k) for r = 1..7 from one table entry: the powers by a product
+      // tree at most three multiplications deep (one table read instead of
+      // seven; the table reads were the kernel's L1 bottleneck)
       const int ts = N / (8 * Ns);
+      cplx<T> w[8];
+      w[1] = twid(tw, (long)k * ts, INV);
+      w[2] = cmul(w[1], w[1]);
+      w[3] = cmul(w[2], w[1]);
+      w[4] = cmul(w[2], w[2]);
+      w[5] = cmul(w[4], w[1]);
+      w[6] = cmul(w[4], w[2]);
+      w[7] = cmul(w[4], w[3]);
 #pragma unroll
-      for (int r = 1; r < 8; r++) v[r] = cmul(v[r], twid(tw, (long)(r * k) * ts, INV));
+      for (int r = 1; r < 8; r++) v[r] = cmul(v[r], w[r]);
     }
     dft8<T, INV>(v);
     const bool last = (p == F::P8 - 1) && F::TAIL == 1;
@@ -361,8 +372,10 @@ __device__ __forceinline__ void fft_reg(cplx<T> (&v)[8], cplx<T> *sm,
       cplx<T> a[4];
 #pragma unroll
       for (int r = 0; r < 4; r++) a[r] = sm[fpad(jj + r * (N / 4))];
-#pragma unroll
-      for (int r = 1; r < 4; r++) a[r] = cmul(a[r], twid(tw, (long)(r * jj), INV));
+      const cplx<T> w1 = twid(tw, (long)jj, INV), w2 = cmul(w1, w1), w3 = cmul(w2, w1);
+      a[1] = cmul(a[1], w1);
+      a[2] = cmul(a[2], w2);
+      a[3] = cmul(a[3], w3);
       dft4<T, INV>(a[0], a[1], a[2], a[3]);
 #pragma unroll
       for (int r = 0; r < 4; r++) v[t + 2 * r] = a[r];  // X[j + (t + 2r) N/8]
