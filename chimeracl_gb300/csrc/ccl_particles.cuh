@@ -143,11 +143,28 @@ static __global__ void k_scan_reduce(const u32 *__restrict__ in, long L,
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
-// exclusive scan of one tile per block, plus part[blockIdx] (scanned)
+// exclusive scan of one tile per block, offset by the tile's prefix: with
+// sum_parts the block adds up the raw tile sums part[0 .. blockIdx) itself
+// (few tiles), else part holds them scanned.  Optionally copies out[tap_i]
+// to *tap (the in-window count of the cell sort).
 static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
-                            const u32 *__restrict__ part, u32 *__restrict__ out,
-                            u32 *__restrict__ total_out) {
+                            const u32 *__restrict__ part, int sum_parts,
+                            u32 *__restrict__ out, u32 *__restrict__ total_out,
+                            u32 *__restrict__ tap, long tap_i) {
   __shared__ u32 sh[32];
+  __shared__ u32 tile_pre;
+  if (threadIdx.x == 0) tile_pre = 0;
+  if (part && sum_parts) {
+    u32 ps = 0;
+    for (long t = threadIdx.x; t < blockIdx.x; t += blockDim.x) ps += part[t];
+    u32 ptot;
+    __syncthreads();
+    block_exclusive_scan(ps, sh, &ptot);
+    if (threadIdx.x == 0) tile_pre = ptot;
+  } else if (part && threadIdx.x == 0) {
+    tile_pre = part[blockIdx.x];
+  }
+  __syncthreads();
   long base = (long)blockIdx.x * SCAN_TILE + (long)threadIdx.x * SCAN_ITEMS;
   u32 v[SCAN_ITEMS];
   u32 s = 0;
@@ -158,15 +175,16 @@ static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
     s += v[it];
   }
   u32 tot;
-  u32 pre = block_exclusive_scan(s, sh, &tot) + (part ? part[blockIdx.x] : 0);
+  const u32 tp = tile_pre;
+  u32 pre = block_exclusive_scan(s, sh, &tot) + tp;
 #pragma unroll
   for (int it = 0; it < SCAN_ITEMS; it++) {
     long i = base + it;
     if (i < L) out[i] = pre;
+    if (tap && i == tap_i) *tap = pre;
     pre += v[it];
   }
-  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
-    *total_out = (part ? part[blockIdx.x] : 0) + tot;
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = tp + tot;
 }
 
 // Keys + per-cell counts over tiles of ST_TILE consecutive particles; cell
@@ -215,24 +233,30 @@ static inline long scan_ws_words(long L) {
   return w + 1;
 }
 
-// out[0..L-1] = exclusive scan of in; *total_out = sum (if non-null).
-// Works in place (out == in).  ws: scan_ws_words(L) words.
+// out[0..L-1] = exclusive scan of in; *total_out = sum (if non-null);
+// *tap = out[tap_i] (if tap).  Works in place (out == in).  ws:
+// scan_ws_words(L) words.  Up to SCAN_FUSE tiles: two launches (tile sums,
+// then the tile scans, each adding up its own prefix).
+constexpr long SCAN_FUSE = 4096;
 static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
-                          u32 *ws, cudaStream_t s) {
+                          u32 *ws, cudaStream_t s, u32 *tap = nullptr, long tap_i = -1) {
   if (L <= 0) return CCL_OK;
   long nb = (L + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 1) {
-    k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, L, nullptr, out, total_out);
+    k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, L, nullptr, 0, out, total_out, tap, tap_i);
     CCL_LAUNCH_CHECK("scan_tile");
     return CCL_OK;
   }
   u32 *part = ws;
   k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part);
   CCL_LAUNCH_CHECK("scan_reduce");
-  int rc = scan_exclusive(part, nb, part, nullptr, ws + nb, s);
-  if (rc) return rc;
-  k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part, out,
-                                                     total_out);
+  int fused = nb <= SCAN_FUSE;
+  if (!fused) {
+    int rc = scan_exclusive(part, nb, part, nullptr, ws + nb, s);
+    if (rc) return rc;
+  }
+  k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part, fused, out, total_out, tap,
+                                                     tap_i);
   CCL_LAUNCH_CHECK("scan_tile");
   return CCL_OK;
 }
@@ -242,25 +266,36 @@ static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
 // cell's segment through a per-cell cursor (one atomic per distinct cell per
 // warp; lanes of a warp keep index order); out-of-window particles take
 // cell_offset[C] + (overflow particles in earlier tiles) + (rank in this
-// tile), so that segment is in index order.  k_cell_fixup then sorts each
-// cell's segment by particle number (insertion sort: linear on the nearly
-// sorted segments this produces), which makes the result that of a stable
-// sort: within a cell, ascending particle number -- the order of the
-// reference's sort kernel run serially.
+// tile), so that segment is in index order.  A cell claimed more than once
+// is flagged, and k_cell_fixup sorts just those cells' segments by particle
+// number, which makes the result that of a stable sort: within a cell,
+// ascending particle number -- the order of the reference's sort kernel run
+// serially.
 static __global__ void __launch_bounds__(ST_THREADS)
     k_scatter(long np, const u32 *__restrict__ keys, u32 C,
               const u32 *__restrict__ cell_offset, u32 *__restrict__ cursor,
-              const u32 *__restrict__ ovf_off, u32 *__restrict__ sort_indx) {
+              u32 *__restrict__ multi, const u32 *__restrict__ ovf_off, int ovf_scanned,
+              u32 *__restrict__ sort_indx) {
   __shared__ u32 sh[32];
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const long base = (long)blockIdx.x * ST_TILE;
-  u32 tile_run = ovf_off[blockIdx.x] + cell_offset[C];
-  // overflow items of this tile (block-uniform): the exclusive tile offsets
-  // end at np - (in-window total)
-  const u32 ovf_next =
-      blockIdx.x + 1 < gridDim.x ? ovf_off[blockIdx.x + 1] : (u32)np - cell_offset[C];
-  const bool tile_has_ovf = ovf_next != ovf_off[blockIdx.x];
+  // overflow items before this tile: the block adds up the per-tile counts
+  // itself (ovf_scanned == 0) or reads their exclusive scan
+  u32 ovf_before;
+  if (!ovf_scanned) {
+    u32 ps = 0;
+    for (long t = threadIdx.x; t < blockIdx.x; t += blockDim.x) ps += ovf_off[t];
+    block_exclusive_scan(ps, sh, &ovf_before);
+  } else {
+    ovf_before = ovf_off[blockIdx.x];
+  }
+  u32 tile_run = ovf_before + cell_offset[C];
+  // overflow items of this tile (block-uniform)
+  const u32 ovf_next = ovf_scanned ? (blockIdx.x + 1 < gridDim.x ? ovf_off[blockIdx.x + 1]
+                                                                 : (u32)np - cell_offset[C])
+                                   : ovf_before + ovf_off[blockIdx.x];
+  const bool tile_has_ovf = ovf_next != ovf_before;
 #pragma unroll
   for (int it = 0; it < ST_ITEMS; it++) {
     const long i = base + it * ST_THREADS + threadIdx.x;
@@ -278,72 +313,78 @@ static __global__ void __launch_bounds__(ST_THREADS)
     const unsigned peers = __match_any_sync(0xffffffffu, (valid && !ovf) ? k : 0xffffffffu);
     const int leader = __ffs(peers) - 1;
     u32 b0 = 0;
-    if (valid && !ovf && lane == leader) b0 = atomicAdd(&cursor[k], __popc(peers));
+    if (valid && !ovf && lane == leader) {
+      b0 = atomicAdd(&cursor[k], __popc(peers));
+      // a second claim on the cell: its order may need the fix-up
+      if (b0 != 0) atomicOr(&multi[k >> 5], 1u << (k & 31));
+    }
     b0 = __shfl_sync(0xffffffffu, b0, leader);
     if (valid && !ovf) sort_indx[cell_offset[k] + b0 + __popc(peers & lt)] = (u32)i;
   }
 }
 
-// One block per FX_CELLS consecutive cells: their segments are contiguous
-// in sort_indx, so the block stages them in shared memory with coalesced
-// loads, each thread insertion-sorts its cell there, and the block writes
-// the range back (only if some cell changed).  A range larger than the
-// staging buffer (cells far denser than the mean) is sorted in place.
-constexpr int FX_CELLS = 256, FX_CAP = 8192;
-static __global__ void __launch_bounds__(FX_CELLS)
-    k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, u32 *__restrict__ sort_indx) {
-  __shared__ u32 sh[FX_CAP];
-  __shared__ int changed;
-  const long c0 = (long)blockIdx.x * FX_CELLS;
-  const long c1 = c0 + FX_CELLS < (long)C ? c0 + FX_CELLS : (long)C;
-  const long c = c0 + threadIdx.x;
-  const u32 lo = cell_offset[c0], n = cell_offset[c1] - lo;
-  if (n <= (u32)FX_CAP) {
-    if (threadIdx.x == 0) changed = 0;
-    for (u32 i = threadIdx.x; i < n; i += FX_CELLS) sh[i] = sort_indx[lo + i];
-    __syncthreads();
-    if (c < c1) {
-      const u32 p0 = cell_offset[c] - lo, p1 = cell_offset[c + 1] - lo;
-      bool moved = false;
+// Fix-up of the cells the scatter flagged (claimed by more than one warp
+// group; a single group writes its items in ascending order): one thread per
+// cell, segments of up to FX_REG items sorted in registers by Batcher's
+// odd-even merge network, longer ones by insertion sort in place.  Every
+// other cell is left untouched without reading it.
+constexpr int FX_REG = 16;
+
+__device__ __forceinline__ void cswap(u32 &a, u32 &b) {
+  const u32 lo = a < b ? a : b, hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+static __global__ void __launch_bounds__(256)
+    k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, const u32 *__restrict__ multi,
+                 u32 *__restrict__ sort_indx) {
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < (long)C;
+       c += (long)gridDim.x * blockDim.x) {
+    if (!(multi[c >> 5] & (1u << (c & 31)))) continue;
+    const u32 p0 = cell_offset[c], p1 = cell_offset[c + 1], n = p1 - p0;
+    if (n <= (u32)FX_REG) {
+      u32 v[FX_REG];
+#pragma unroll
+      for (int i = 0; i < FX_REG; i++) v[i] = (u32)i < n ? sort_indx[p0 + i] : 0xffffffffu;
+#pragma unroll
+      for (int p = 1; p < FX_REG; p <<= 1)
+#pragma unroll
+        for (int k = p; k >= 1; k >>= 1)
+#pragma unroll
+          for (int j = k % p; j <= FX_REG - 1 - k; j += 2 * k)
+#pragma unroll
+            for (int i = 0; i <= k - 1 && i + j + k <= FX_REG - 1; i++)
+              if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) cswap(v[i + j], v[i + j + k]);
+#pragma unroll
+      for (int i = 0; i < FX_REG; i++)
+        if ((u32)i < n) sort_indx[p0 + i] = v[i];
+    } else {
       for (u32 a = p0 + 1; a < p1; a++) {
-        const u32 v = sh[a];
+        const u32 v = sort_indx[a];
         u32 b = a;
-        while (b > p0 && sh[b - 1] > v) {
-          sh[b] = sh[b - 1];
+        while (b > p0 && sort_indx[b - 1] > v) {
+          sort_indx[b] = sort_indx[b - 1];
           b--;
         }
-        if (b != a) {
-          sh[b] = v;
-          moved = true;
-        }
+        sort_indx[b] = v;
       }
-      if (moved) changed = 1;
-    }
-    __syncthreads();
-    if (changed)
-      for (u32 i = threadIdx.x; i < n; i += FX_CELLS) sort_indx[lo + i] = sh[i];
-  } else if (c < c1) {
-    const u32 p0 = cell_offset[c], p1 = cell_offset[c + 1];
-    for (u32 a = p0 + 1; a < p1; a++) {
-      const u32 v = sort_indx[a];
-      u32 b = a;
-      while (b > p0 && sort_indx[b - 1] > v) {
-        sort_indx[b] = sort_indx[b - 1];
-        b--;
-      }
-      sort_indx[b] = v;
     }
   }
 }
 
+// workspace: scatter cursors (C + 1 words), multi-claim bits (one per cell),
+// per-tile overflow counts, scan partials
 struct SortWs {
-  u32 *cursor, *tile_ovf, *scan;
+  u32 *cursor, *multi, *tile_ovf, *scan;
 };
+
+static inline long sort_multi_words(long ncells) { return (ncells + 31) / 32; }
 
 static inline size_t sort_ws_bytes(long np, long ncells) {
   long ntiles = (np + ST_TILE - 1) / ST_TILE;
   long scanw = scan_ws_words(ncells + 1 > ntiles ? ncells + 1 : ntiles);
-  long words = ncells + 1 + ntiles + 1 + scanw + 64;
+  long words = ncells + 1 + sort_multi_words(ncells) + ntiles + 1 + scanw + 64;
   return (size_t)words * 4 + 256;
 }
 
@@ -353,12 +394,11 @@ static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
   u32 *w = (u32 *)p;
   SortWs s;
   s.cursor = w;
-  s.tile_ovf = w + ncells + 1;
+  s.multi = w + ncells + 1;
+  s.tile_ovf = s.multi + sort_multi_words(ncells);
   s.scan = s.tile_ovf + ntiles + 1;
   return s;
 }
-
-static __global__ void k_copy_u32(const u32 *src, u32 *dst) { *dst = *src; }
 
 template <typename T>
 int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
@@ -376,21 +416,26 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
                                                       w.tile_ovf);
     CCL_LAUNCH_CHECK("keys");
   }
-  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1,
-                          w.scan, s);
+  // offsets, total, and np_stay = cell_offset[C] from the scan's own tap
+  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1, w.scan, s, np_stay,
+                          C);
   if (rc) return rc;
-  k_copy_u32<<<1, 1, 0, s>>>(cell_offset + C, np_stay);
-  CCL_LAUNCH_CHECK("np_stay");
   if (np == 0) return CCL_OK;
-  rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
-  if (rc) return rc;
-  cudaMemsetAsync(w.cursor, 0, C * sizeof(u32), s);
+  // few tiles: each scatter block adds up the overflow counts before it
+  const int ovf_scanned = ntiles > SCAN_FUSE;
+  if (ovf_scanned) {
+    rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
+    if (rc) return rc;
+  }
+  // cursors and multi-claim bits are adjacent: one memset clears both
+  cudaMemsetAsync(w.cursor, 0, (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32),
+                  s);
   k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
-                                                    w.cursor, w.tile_ovf, sort_indx);
+                                                    w.cursor, w.multi, w.tile_ovf, ovf_scanned,
+                                                    sort_indx);
   CCL_LAUNCH_CHECK("scatter");
   if (C > 0)
-    k_cell_fixup<<<(unsigned)((C + FX_CELLS - 1) / FX_CELLS), FX_CELLS, 0, s>>>(
-        (u32)C, cell_offset, sort_indx);
+    k_cell_fixup<<<grid_for(C, 256), 256, 0, s>>>((u32)C, cell_offset, w.multi, sort_indx);
   CCL_LAUNCH_CHECK("cell_fixup");
   return CCL_OK;
 }
