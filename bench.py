@@ -377,6 +377,13 @@ def load_peaks():
         return dict(FALLBACK_PEAKS), "fallback"
 
 
+# DRAM bytes (read + write) per call of the 2048 x 256, M = 1 workload, summed
+# over the call's kernels in one ncu capture:
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       --clock-control none --nvtx --nvtx-include "prof/" <one sort of the workload>
+MEASURED_TRAFFIC = {"ccl_index_sort": 86.7e6}
+
+
 def roofline(probe_summary, peaks, src):
     """Roofline line of the kernel with the largest share of the probed
     time: achieved = algorithmic bytes (or flops) per launch / mean launch
@@ -388,7 +395,7 @@ def roofline(probe_summary, peaks, src):
     per_s = s["ms_total"] / s["launches"] * 1e-3
     gbs = s["bytes"] / s["launches"] / per_s / 1e9
     line = {"kernel": name, "launches": s["launches"], "ms_per_launch": round(per_s * 1e3, 5),
-            "traffic": None, "peak_source": src}
+            "traffic": MEASURED_TRAFFIC.get(name), "peak_source": src}
     hbm = {"bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
            "frac": round(gbs / peaks["hbm_gbs"], 4)}
     if name == "ccl_dht_bf16x3_gemm_batch":
