@@ -68,7 +68,7 @@ def config_line(cfg):
 
 
 # ---------------------------------------------------------------------------
-def build_run(cfg, precision, device_index=0):
+def build_run(cfg, precision, device_index=0, particles_cls=None, **comm_kw):
     """Set the run up through the public API, as the reference's example
     scripts do (examples/lpa_script_small.py:51-95)."""
     from chimeracl_gb300 import Communicator
@@ -78,7 +78,7 @@ def build_run(cfg, precision, device_index=0):
     from chimeracl_gb300.pic_loop import PIC_loop
     from chimeracl_gb300.solver import Solver
 
-    comm = Communicator(precision=precision, device=device_index, seed=cfg["seed"])
+    comm = Communicator(precision=precision, device=device_index, seed=cfg["seed"], **comm_kw)
     solver = Solver(copy.deepcopy(cfg["grid_in"]), comm)
     add_gausian_pulse(solver, dict(cfg["laser_in"]))
     e_in = copy.deepcopy(cfg["eons_in"])
@@ -86,7 +86,7 @@ def build_run(cfg, precision, device_index=0):
     i_in = copy.deepcopy(e_in)
     i_in["charge"] = 1
     i_in["Immobile"] = True
-    eons = Particles(e_in, comm, seed=cfg["seed"])
+    eons = (particles_cls or Particles)(e_in, comm, seed=cfg["seed"])
     ions = Particles(i_in, comm, seed=cfg["seed"] + 1)
     ions.Args["InjectorSource"] = eons
     eons.make_new_domain(dict(cfg["prefill"]), density_profiles=cfg["profiles"])
@@ -101,8 +101,9 @@ def build_run(cfg, precision, device_index=0):
 def diagnostics_dev(solver, eons):
     """Integrated diagnostics on the device (float64 reductions): field
     energy sum_m w_m sum (|E|^2 + |B|^2) 2 pi r dr dx over rows r > 0
-    (w_0 = 1, w_m = 2), on-axis Ez wake amplitude max |Ez_m0[1, ix]| behind
-    the laser (x < x_laser - 2 Lx), kinetic energy sum w (gamma - 1)."""
+    (w_0 = 1, w_m = 2); the on-axis longitudinal field |Ex_m0[1, ix]| (x is
+    the propagation axis: behind the laser this is the wake); kinetic
+    energy sum w (gamma - 1)."""
     import torch
     A, D = solver.Args, solver.DataDev
     r = torch.as_tensor(A["Rgrid"][1:, None], device=D["Ez_m0"].device)
@@ -114,10 +115,48 @@ def diagnostics_dev(solver, eons):
             for c in "xyz":
                 a = D[f + c + "_m" + str(m)][1:].to(torch.complex128 if m else torch.float64)
                 We = We + wm * ((a.abs() ** 2) * vol).sum()
-    ez = D["Ez_m0"][1].to(torch.float64).abs()
-    kin = (eons.DataDev["w"].to(torch.float64)
-           * (1.0 / eons.DataDev["g_inv"].to(torch.float64) - 1.0)).sum()
-    return We, ez, kin
+    ex = D["Ex_m0"][1].to(torch.float64).abs()
+    # gamma - 1 = p^2 / (1 + gamma) from the momenta, in float64 (1/g_inv - 1
+    # cancels: an FP32 g_inv holds nothing of gamma - 1 below 6e-8)
+    D = eons.DataDev
+    p2 = sum(D[k].to(torch.float64) ** 2 for k in ("px", "py", "pz"))
+    kin = (D["w"].to(torch.float64) * p2 / (1.0 + torch.sqrt(1.0 + p2))).sum()
+    return We, ex, kin
+
+
+def field_l2_rel(sol, ref):
+    """Pointwise relative L2 difference of all real-space E, B modes (rows
+    r > 0) of `sol` against `ref`, in float64 on the device."""
+    import torch
+    A = ref.Args
+    num = den = 0.0
+    for m in range(A["M"] + 1):
+        for f in ("E", "B"):
+            for c in "xyz":
+                k = f + c + "_m" + str(m)
+                dt = torch.complex128 if m else torch.float64
+                a, b = sol.DataDev[k][1:].to(dt), ref.DataDev[k][1:].to(dt)
+                num += float(((a - b).abs() ** 2).sum())
+                den += float((b.abs() ** 2).sum())
+    return float(np.sqrt(num / den))
+
+
+def compare_runs(cfg, run, ref):
+    """Relative differences of `run` against `ref` at the same step: field
+    energy, wake amplitude (max on-axis |Ex_m0| behind the laser,
+    x < x_laser - 2 Lx), kinetic energy, pointwise field L2."""
+    vals = []
+    for r in (run, ref):
+        We, ex, kin = diagnostics_dev(r["solver"], r["eons"])
+        A = r["solver"].Args
+        x_las = cfg["laser_in"]["x0"] + r["loop"].it * A["dt"]
+        vals.append((float(We), wake_amplitude(ex.cpu().numpy(), A["Xgrid"], x_las,
+                                               cfg["laser_in"]["Lx"]), float(kin)))
+    (We, wk, kin), (We0, wk0, kin0) = vals
+    return {"field_energy_rel_err": abs(We / We0 - 1), "wake_ex_rel_err": abs(wk / wk0 - 1),
+            "kinetic_rel_err": abs(kin / kin0 - 1),
+            "field_l2_rel_err": field_l2_rel(run["solver"], ref["solver"]),
+            "at_step": ref["loop"].it}
 
 
 def wake_amplitude(ez_row, xgrid, x_laser, Lx):
@@ -500,19 +539,8 @@ def run_ours(args):
         r64["loop"].step()
     torch.cuda.synchronize()
     acc = {}
-    vals = {}
-    for tag, r in (("mixed", r32), ("fp64", r64)):
-        We, ez, kin = diagnostics_dev(r["solver"], r["eons"])
-        A = r["solver"].Args
-        x_las = cfg["laser_in"]["x0"] + r["loop"].it * A["dt"]
-        vals[tag] = (float(We), wake_amplitude(ez.cpu().numpy(), A["Xgrid"], x_las,
-                                               cfg["laser_in"]["Lx"]), float(kin),
-                     r["loop"].it)
-    if vals["mixed"][3] == vals["fp64"][3]:
-        acc = {"field_energy_rel_err": abs(vals["mixed"][0] / vals["fp64"][0] - 1),
-               "ez_wake_rel_err": abs(vals["mixed"][1] / vals["fp64"][1] - 1),
-               "kinetic_rel_err": abs(vals["mixed"][2] / vals["fp64"][2] - 1),
-               "at_step": vals["mixed"][3]}
+    if r32["loop"].it == r64["loop"].it:
+        acc = compare_runs(cfg, r32, r64)
     ms32 = reduce_max(dist, r32["ms"], dev)
     ms64 = reduce_max(dist, r64["ms"], dev)
     np32 = reduce_sum(dist, r32["np_sum"], dev)
@@ -554,6 +582,57 @@ def run_ours(args):
     return 0
 
 
+def fp32_injected_particles():
+    """Particles (FP64) whose injector output -- coordinates and weights of
+    every prefilled or injected particle -- is rounded through FP32: the
+    particles an FP32 run starts from, stepped in FP64.  The reference for
+    the step error of the FP32 forms on the same initial particles."""
+    from chimeracl_gb300.particles import Particles
+
+    class Fp32InjectedParticles(Particles):
+        def make_new_domain(self, parts_in, density_profiles=None):
+            super().make_new_domain(parts_in, density_profiles)
+            for k in ("x_new", "y_new", "z_new", "w_new"):
+                t = self.DataDev[k]
+                t.copy_(t.float().double())
+
+    return Fp32InjectedParticles
+
+
+def run_accuracy(args):
+    """The mixed form against FP64 after `acc_steps` steps, on the bench
+    workload (2x1x4 particles per cell: every radial position on a grid
+    node) and with 2x2x4 per cell (none on a node): against the FP64 run on
+    the same seed, and against the FP64 run on the same FP32-rounded
+    particles (the step error alone)."""
+    import torch
+    out = {}
+    for name, nppc in (("2x1x4", None), ("2x2x4", (2, 2, 4))):
+        cfg = workload()
+        if nppc:
+            cfg["eons_in"]["Nppc"] = nppc
+        runs = {}
+        for tag, prec, cls in (("fp64", "fp64", None),
+                               ("fp64_fp32_particles", "fp64", fp32_injected_particles()),
+                               ("mixed", "mixed", None)):
+            solver, eons, ions, loop = build_run(cfg, prec, particles_cls=cls)
+            for _ in range(args.acc_steps):
+                loop.step()
+            torch.cuda.synchronize()
+            runs[tag] = dict(solver=solver, eons=eons, ions=ions, loop=loop)
+        out[name] = {
+            "mixed_vs_fp64": compare_runs(cfg, runs["mixed"], runs["fp64"]),
+            "mixed_vs_fp64_same_particles": compare_runs(cfg, runs["mixed"],
+                                                         runs["fp64_fp32_particles"]),
+            "fp64_same_particles_vs_fp64": compare_runs(cfg, runs["fp64_fp32_particles"],
+                                                        runs["fp64"]),
+            "electrons": {k: int(r["eons"].Args["Np"]) for k, r in runs.items()}}
+        del runs
+        torch.cuda.empty_cache()
+    print(json.dumps({"accuracy": out, "steps": args.acc_steps, "workload": WORKLOAD}))
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -562,11 +641,16 @@ def main(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="run the mixed-vs-FP64 accuracy study instead of the benchmark")
+    ap.add_argument("--acc-steps", type=int, default=608)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         return run_reference(args)
+    if args.accuracy:
+        return run_accuracy(args)
     return run_ours(args)
 
 

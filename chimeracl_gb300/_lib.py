@@ -25,6 +25,7 @@ _pp = C.POINTER(C.c_void_p)
 # name -> argtypes (all return int status)
 SIGNATURES = {
     "ccl_push_x": [_i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _vp],
+    "ccl_push_x_compensated": [_i, _l] + [_vp] * 10 + [_d, _vp],
     "ccl_index_sort_workspace": [_l, _l, C.POINTER(_sz)],
     "ccl_index_sort": [_i, _l, _vp, _vp, _vp, _i, _d, _d, _i, _d, _d,
                        _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp],
@@ -54,6 +55,7 @@ SIGNATURES = {
     "ccl_damp_batch": [_i, _i, _i, _i, _pp, _pp, _vp, _vp, _vp, _vp, _i, _vp],
     "ccl_dht_gemm_batch": [_i, _i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],
     "ccl_psatd_advance": [_i, _l, _d, _vp, _vp, _vp, _pp, _vp],
+    "ccl_psatd_advance_split": [_i, _l, _vp, _pp, _vp],
     "ccl_dht_bf16x3_prepare_bytes": [_i, _i, C.POINTER(_sz)],
     "ccl_dht_bf16x3_prepare": [_i, _vp, _i, _i, _vp, _sz, _vp],
     "ccl_dht_bf16x3_gemm_batch": [_i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],

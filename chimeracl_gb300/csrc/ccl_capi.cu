@@ -65,6 +65,18 @@ int ccl_push_x(int dtype, long np, void *x, void *y, void *z, const void *px,
   return DISPATCH(dtype, push_x(np, x, y, z, px, py, pz, g_inv, dt, S(stream)));
 }
 
+int ccl_push_x_compensated(int dtype, long np, void *x, void *y, void *z, void *x_lo,
+                           void *y_lo, void *z_lo, const void *px, const void *py,
+                           const void *pz, const void *g_inv, double dt, void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNEG(np);
+  if (np == 0) return CCL_OK;
+  NONNULL(x); NONNULL(y); NONNULL(z); NONNULL(x_lo); NONNULL(y_lo); NONNULL(z_lo);
+  NONNULL(px); NONNULL(py); NONNULL(pz); NONNULL(g_inv);
+  return DISPATCH(dtype, push_x_comp(np, x, y, z, x_lo, y_lo, z_lo, px, py, pz, g_inv, dt,
+                                     S(stream)));
+}
+
 int ccl_index_sort_workspace(long np, long ncells, size_t *bytes) {
   NONNEG(np);
   CCL_REQUIRE(ncells > 0, CCL_ERR_ARG, "%s: ncells %ld", __func__, ncells);
@@ -407,6 +419,14 @@ int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
   NONNEG(ncells);
   NONNULL(c1); NONNULL(c2); NONNULL(c3); NONNULL(flds);
   return DISPATCH(dtype, psatd(ncells, dt_inv, c1, c2, c3, flds, S(stream)));
+}
+
+int ccl_psatd_advance_split(int dtype, long ncells, const void *coef, void *const *flds,
+                            void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNEG(ncells);
+  NONNULL(coef); NONNULL(flds);
+  return DISPATCH(dtype, psatd_split(ncells, coef, flds, S(stream)));
 }
 
 int ccl_get_m1(int dtype, int nrows, int nx, void *out, const void *in,

@@ -97,7 +97,7 @@ __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (
   const float wp = VEC ? wraw * gi * q : wraw * q;
   const float r2 = yp * yp + zp * zp;
   const float rinv = r2 > 0.f ? rsqrtf(r2) : (VEC ? 0.f : __int_as_float(0x7f800000));
-  const float rp = r2 > 0.f ? r2 * rinv : 0.f;
+  const float rp = sqrtf(r2);
   float e[M + 1][2];
   e[0][0] = 1.f;
   e[0][1] = 0.f;
@@ -110,8 +110,8 @@ __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (
     e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
     e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
   }
-  const float sX1 = (xp - g.xmin) * g.dx_inv - fix, sX0 = 1.f - sX1;
-  const float sR1 = (rp - g.rmin) * g.dr_inv - fir, sR0 = 1.f - sR1;
+  const float sX1 = frac_x(xp, (int)fix, g), sX0 = 1.f - sX1;
+  const float sR1 = frac_r(rp, (int)fir, g), sR0 = 1.f - sR1;
   const float wX0 = sX0 * wp, wX1 = sX1 * wp;
   const float C[4] = {sR0 * wX0, sR0 * wX1, sR1 * wX0, sR1 * wX1};
   const float jp[3] = {VEC ? ux : 1.f, uy, uz};
@@ -440,14 +440,14 @@ __global__ void __launch_bounds__(256)
     const float xp = x[p], yp = y[p], zp = z[p];
     const float r2 = yp * yp + zp * zp;
     const float rinv = r2 > 0.f ? rsqrtf(r2) : __int_as_float(0x7f800000);
-    const float rp = r2 > 0.f ? r2 * rinv : 0.f;
+    const float rp = sqrtf(r2);
     const float fx = (xp - g.xmin) * g.dx_inv, fr = (rp - g.rmin) * g.dr_inv;
     const int ix = floor_to_int<float>(floorf(fx), -1);
     const int ir = floor_to_int<float>(floorf(fr), 1 << 30);
     if (!(ix > 0 && ix < nxc - 1 && ir < nrc - 1)) continue;
     const unsigned ig = (unsigned)ix + (unsigned)ir * (unsigned)Nx;
-    const float sX1 = fx - (float)ix, sX0 = 1.f - sX1;
-    const float sR1 = fr - (float)ir, sR0 = 1.f - sR1;
+    const float sX1 = frac_x(xp, ix, g), sX0 = 1.f - sX1;
+    const float sR1 = frac_r(rp, ir, g), sR0 = 1.f - sR1;
     const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
     const unsigned nodes[4] = {ig, ig + 1, ig + (unsigned)Nx, ig + (unsigned)Nx + 1};
     float e[M + 1][2];
@@ -589,8 +589,8 @@ __global__ void __launch_bounds__(GT_THREADS)
     int ix = (int)floorf(fx);
     ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
     const int ir = nr0 + r;
-    const float sX1 = fx - (float)ix, sX0 = 1.f - sX1;
-    const float sR1 = fr - (float)ir, sR0 = 1.f - sR1;
+    const float sX1 = frac_x(xp, ix, g), sX0 = 1.f - sX1;
+    const float sR1 = frac_r(rp, ir, g), sR0 = 1.f - sR1;
     const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
     const int l0 = (r * GT_NX + (ix - nx0)) * NS;
     const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};

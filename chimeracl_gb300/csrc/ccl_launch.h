@@ -51,6 +51,9 @@ template <typename T> struct Ops {
   static int push_x(long np, void *x, void *y, void *z, const void *px,
                     const void *py, const void *pz, const void *g_inv,
                     double dt, cudaStream_t s);
+  static int push_x_comp(long np, void *x, void *y, void *z, void *xl, void *yl, void *zl,
+                         const void *px, const void *py, const void *pz,
+                         const void *g_inv, double dt, cudaStream_t s);
   static int index_sort(long np, const void *x, const void *y, const void *z,
                         int Nx, double xmin, double dx_inv, int Nr,
                         double rmin, double dr_inv, uint32_t *indx,
@@ -95,6 +98,7 @@ template <typename T> struct Ops {
                                const void *const *flds, cudaStream_t s);
   static int psatd(long n, double dt_inv, const void *c1, const void *c2,
                    const void *c3, void *const *flds, cudaStream_t s);
+  static int psatd_split(long n, const void *coef, void *const *flds, cudaStream_t s);
   static int phase(int nx, void *phs, const double *kx, double x0, int sign,
                    cudaStream_t s);
   static int get_m1(int nrows, int nx, void *out, const void *in,

@@ -19,13 +19,22 @@ int Ops<T>::push_x(long np, void *x, void *y, void *z, const void *px,
 }
 
 template <typename T>
+int Ops<T>::push_x_comp(long np, void *x, void *y, void *z, void *xl, void *yl, void *zl,
+                        const void *px, const void *py, const void *pz, const void *g_inv,
+                        double dt, cudaStream_t s) {
+  return ccl::push_x_comp<T>(np, (T *)x, (T *)y, (T *)z, (T *)xl, (T *)yl, (T *)zl,
+                             (const T *)px, (const T *)py, (const T *)pz, (const T *)g_inv,
+                             dt, s);
+}
+
+template <typename T>
 int Ops<T>::index_sort(long np, const void *x, const void *y, const void *z,
                        int Nx, double xmin, double dx_inv, int Nr, double rmin,
                        double dr_inv, uint32_t *indx, uint32_t *counts,
                        uint32_t *cell_offset, uint32_t *sort_indx,
                        uint32_t *np_stay, void *ws, size_t ws_bytes,
                        cudaStream_t s) {
-  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
+  const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
   return ccl::index_sort<T>(np, (const T *)x, (const T *)y, (const T *)z, g,
                             indx, counts, cell_offset, sort_indx, np_stay, ws,
                             ws_bytes, s);
@@ -80,7 +89,7 @@ int Ops<T>::deposit(int vec, int M, const uint32_t *sort_indx,
                     int charge, int Nx, double xmin, double dx_inv, int Nr,
                     double rmin, double dr_inv, void *const *flds,
                     cudaStream_t s) {
-  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
+  const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
   if (vec)
     return ccl::deposit<T, true>(M, sort_indx, cell_off, (const T *)x,
                                  (const T *)y, (const T *)z, (const T *)ux,
@@ -134,7 +143,7 @@ int Ops<T>::gather_push(int M, long np, const void *x, const void *y,
                         double xmin, double dx_inv, int Nr, double rmin,
                         double dr_inv, const void *const *flds,
                         cudaStream_t s) {
-  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
+  const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
   return ccl::gather_push<T>(M, np, (const T *)x, (const T *)y, (const T *)z,
                              (T *)px, (T *)py, (T *)pz, (T *)g_inv, sort_indx,
                              np_stay, factor_push, g, flds, s);
@@ -148,7 +157,7 @@ int Ops<T>::gather_push_cells(int M, long np, const void *x, const void *y,
                               double factor_push, int Nx, double xmin,
                               double dx_inv, int Nr, double rmin, double dr_inv,
                               const void *const *flds, cudaStream_t s) {
-  GridP<T> g = {Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv};
+  const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
   return ccl::gather_push_cells<T>(M, np, (const T *)x, (const T *)y, (const T *)z,
                                    (T *)px, (T *)py, (T *)pz, (T *)g_inv, sort_indx,
                                    cell_offset, np_stay, factor_push, g, flds, s);
@@ -166,6 +175,19 @@ int Ops<T>::psatd(long n, double dt_inv, const void *c1, const void *c2,
   k_psatd<T><<<grid_for(n, 256), 256, 0, s>>>(n, (T)dt_inv, (const T *)c1,
                                                (const T *)c2, (const T *)c3, f);
   CCL_LAUNCH_CHECK("psatd");
+  return CCL_OK;
+}
+
+template <typename T>
+int Ops<T>::psatd_split(long n, const void *coef, void *const *flds, cudaStream_t s) {
+  ptrs<15> f;
+  for (int i = 0; i < 15; i++) {
+    CCL_REQUIRE(flds[i], CCL_ERR_ARG, "psatd_split: null field %d", i);
+    f.p[i] = flds[i];
+  }
+  if (n == 0) return CCL_OK;
+  k_psatd_split<T><<<grid_for(n, 256), 256, 0, s>>>(n, (const T *)coef, f);
+  CCL_LAUNCH_CHECK("psatd_split");
   return CCL_OK;
 }
 

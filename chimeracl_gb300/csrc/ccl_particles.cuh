@@ -63,6 +63,97 @@ int push_x(long np, T *x, T *y, T *z, const T *px, const T *py, const T *pz,
 }
 
 // ---------------------------------------------------------------------
+// Compensated form of push_xyz: each coordinate is the unevaluated sum
+// hi + lo of two values of the particles' type, hi the nearest value to the
+// sum (what the sort, deposits and gather read).  The displacement is the
+// one push_xyz forms; it is added by Knuth's two-sum (the rounding error of
+// hi + d, exactly) into lo, and the pair renormalised by Dekker's fast
+// two-sum.  A coordinate then drifts by no more than a few units in the last
+// place of lo over a run, where a plain FP32 sum loses up to half a unit of
+// hi per push (and a displacement below that is lost whole).
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b) {
+  if constexpr (sizeof(T) == 4) return __fadd_rn(a, b);
+  else return __dadd_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T sub_rn(T a, T b) {
+  if constexpr (sizeof(T) == 4) return __fsub_rn(a, b);
+  else return __dsub_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ void comp_add(T &hi, T &lo, T d) {
+  const T s = add_rn(hi, d);
+  const T bp = sub_rn(s, hi);
+  const T e = add_rn(sub_rn(hi, sub_rn(s, bp)), sub_rn(d, bp));  // hi + d - s, exact
+  const T l = add_rn(lo, e);
+  const T h2 = add_rn(s, l);
+  lo = sub_rn(l, sub_rn(h2, s));
+  hi = h2;
+}
+
+template <typename T>
+__global__ void k_push_x_comp(long np, T *__restrict__ x, T *__restrict__ y,
+                              T *__restrict__ z, T *__restrict__ xl, T *__restrict__ yl,
+                              T *__restrict__ zl, const T *__restrict__ px,
+                              const T *__restrict__ py, const T *__restrict__ pz,
+                              const T *__restrict__ g_inv, T dt, int vec) {
+  constexpr int VW = 16 / sizeof(T);
+  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const long nv = vec ? np / VW : 0;
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nv;
+       v += (long)gridDim.x * blockDim.x) {
+    V gx = ((const V *)g_inv)[v], ux = ((const V *)px)[v], uy = ((const V *)py)[v],
+      uz = ((const V *)pz)[v];
+    V xx = ((V *)x)[v], yy = ((V *)y)[v], zz = ((V *)z)[v];
+    V xe = ((V *)xl)[v], ye = ((V *)yl)[v], ze = ((V *)zl)[v];
+    T *g = (T *)&gx, *a = (T *)&ux, *b = (T *)&uy, *c = (T *)&uz;
+    T *xo = (T *)&xx, *yo = (T *)&yy, *zo = (T *)&zz;
+    T *xs = (T *)&xe, *ys = (T *)&ye, *zs = (T *)&ze;
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      T dt_g = dt * g[q];
+      comp_add(xo[q], xs[q], a[q] * dt_g);
+      comp_add(yo[q], ys[q], b[q] * dt_g);
+      comp_add(zo[q], zs[q], c[q] * dt_g);
+    }
+    ((V *)x)[v] = xx;
+    ((V *)y)[v] = yy;
+    ((V *)z)[v] = zz;
+    ((V *)xl)[v] = xe;
+    ((V *)yl)[v] = ye;
+    ((V *)zl)[v] = ze;
+  }
+  for (long i = nv * VW + blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
+       i += (long)gridDim.x * blockDim.x) {
+    T dt_g = dt * g_inv[i];
+    T xo = x[i], yo = y[i], zo = z[i], xs = xl[i], ys = yl[i], zs = zl[i];
+    comp_add(xo, xs, px[i] * dt_g);
+    comp_add(yo, ys, py[i] * dt_g);
+    comp_add(zo, zs, pz[i] * dt_g);
+    x[i] = xo;
+    y[i] = yo;
+    z[i] = zo;
+    xl[i] = xs;
+    yl[i] = ys;
+    zl[i] = zs;
+  }
+}
+
+template <typename T>
+int push_x_comp(long np, T *x, T *y, T *z, T *xl, T *yl, T *zl, const T *px, const T *py,
+                const T *pz, const T *g_inv, double dt, cudaStream_t s) {
+  const uintptr_t mis = ((uintptr_t)x | (uintptr_t)y | (uintptr_t)z | (uintptr_t)xl |
+                         (uintptr_t)yl | (uintptr_t)zl | (uintptr_t)px | (uintptr_t)py |
+                         (uintptr_t)pz | (uintptr_t)g_inv) & 15;
+  if (np == 0) return CCL_OK;
+  k_push_x_comp<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, xl, yl, zl, px, py, pz,
+                                                      g_inv, (T)dt, mis == 0);
+  CCL_LAUNCH_CHECK("push_x_compensated");
+  return CCL_OK;
+}
+
+// ---------------------------------------------------------------------
 // Cell key of a particle (particles_generic.cl:106-125).
 // Grid geometry in the particles' own precision (converted once on the
 // host: the FP32 kernels then never touch the FP64 pipe)
@@ -70,7 +161,43 @@ template <typename T>
 struct GridP {
   int Nx, Nr;
   T xmin, dx_inv, rmin, dr_inv;
+  // the FP32 kernels' cell edges xmin + i dx, rmin + i dr: origin and step as
+  // unevaluated pairs hi + lo of the double values (dx = 1/dx_inv)
+  T xmin_lo, dx, dx_lo, rmin_lo, dr, dr_lo;
 };
+
+template <typename T>
+inline GridP<T> make_gridp(int Nx, int Nr, double xmin, double dx_inv, double rmin,
+                           double dr_inv) {
+  auto lo = [](double v) { return (T)(v - (double)(T)v); };
+  const double dx = 1.0 / dx_inv, dr = 1.0 / dr_inv;
+  return GridP<T>{Nx, Nr, (T)xmin, (T)dx_inv, (T)rmin, (T)dr_inv,
+                  lo(xmin), (T)dx, lo(dx), lo(rmin), (T)dr, lo(dr)};
+}
+
+// Fraction of coordinate v in cell i of an FP32 axis with edges o + i h
+// (o = o_hi + o_lo, h = h_hi + h_lo): the edge is formed as a float pair
+// (two-product of i h, two-sum with o) and v - edge is exact, so the
+// fraction keeps v's own precision.  The plain (v - o) / h - i rounds at
+// the magnitude of the cell count: at ~2000 cells an FP32 unit in the last
+// place is 1.2e-4 of a cell, which every shape-function weight then carries.
+__device__ __forceinline__ float cell_frac(float v, int i, float o_hi, float o_lo, float h_hi,
+                                           float h_lo, float h_inv) {
+  const float fi = (float)i;
+  const float p = __fmul_rn(fi, h_hi);
+  const float pe = __fmaf_rn(fi, h_hi, -p);  // fi h_hi - p, exactly
+  const float c = __fadd_rn(o_hi, p);
+  const float bp = __fsub_rn(c, o_hi);
+  const float ce = __fadd_rn(__fsub_rn(o_hi, __fsub_rn(c, bp)), __fsub_rn(p, bp));  // o_hi + p - c
+  const float c_lo = __fadd_rn(__fadd_rn(ce, pe), __fmaf_rn(fi, h_lo, o_lo));
+  return __fmul_rn(__fsub_rn(__fsub_rn(v, c), c_lo), h_inv);
+}
+__device__ __forceinline__ float frac_x(float xp, int ix, const GridP<float> &g) {
+  return cell_frac(xp, ix, g.xmin, g.xmin_lo, g.dx, g.dx_lo, g.dx_inv);
+}
+__device__ __forceinline__ float frac_r(float rp, int ir, const GridP<float> &g) {
+  return cell_frac(rp, ir, g.rmin, g.rmin_lo, g.dr, g.dr_lo, g.dr_inv);
+}
 
 template <typename T>
 __device__ __forceinline__ int floor_to_int(T f, int bad) {

@@ -45,6 +45,47 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The same update written with coefficients that carry no cancellation
+// (formed in double on the host, x = w dt, 2 pi folded in):
+//   e1 = c1 e0 + s g0 - s2 j0 + a2 n0 + b2 n1
+//   g1 = -c2 e0 + c1 g0 + q2 j0 + d2 (n0 - n1) - s2 n0
+// with c1 = cos x, c2 = w sin x, s = sin x / w, s2 = 2 pi s,
+// q2 = 2 pi (1 - cos x), a2 = 2 pi (cos x - sin x / x) / w^2,
+// b2 = 2 pi (sin x / x - 1) / w^2, d2 = 2 pi (1 - cos x) / (w^2 dt).
+// Algebraically the reference's expressions; but where those form the small
+// terms of the long-wavelength modes (x ~ 1e-3: O(x^2) results from O(1)
+// differences, c1 (g0 - j0) + j0 for (1 - cos x) j0) they lose
+// log10(1/x^2) digits, which FP32 cannot spare: at a plasma wake's x the
+// charge and current terms would keep 1 to 2 digits.  coef holds the eight
+// values per element, in that order.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_psatd_split(long n, const T *__restrict__ coef, ptrs<15> f) {
+  CCL_GRID_STRIDE(i, n) {
+    T c[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) c[k] = coef[8 * i + k];
+    const T c1 = c[0], c2 = c[1], s = c[2], s2 = c[3], q2 = c[4], a2 = c[5], b2 = c[6],
+            d2 = c[7];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const cplx<T> E0 = ld_c((const T *)f.p[k], i), G0 = ld_c((const T *)f.p[3 + k], i);
+      const cplx<T> J0 = ld_c((const T *)f.p[6 + k], i);
+      const cplx<T> N0 = ld_c((const T *)f.p[9 + k], i), N1 = ld_c((const T *)f.p[12 + k], i);
+      const T e0[2] = {E0.re, E0.im}, g0[2] = {G0.re, G0.im}, j0[2] = {J0.re, J0.im};
+      const T n0[2] = {N0.re, N0.im}, n1[2] = {N1.re, N1.im};
+      T e1[2], g1[2];
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        e1[q] = c1 * e0[q] + s * g0[q] - s2 * j0[q] + a2 * n0[q] + b2 * n1[q];
+        g1[q] = -c2 * e0[q] + c1 * g0[q] + q2 * j0[q] + d2 * (n0[q] - n1[q]) - s2 * n0[q];
+      }
+      st_c((T *)f.p[k], i, cplx<T>{e1[0], e1[1]});
+      st_c((T *)f.p[3 + k], i, cplx<T>{g1[0], g1[1]});
+    }
+  }
+}
+
 // get_phase_plus / get_phase_minus (transformer_generic.cl:28-55); computed
 // in double whatever T is.
 template <typename T>

@@ -72,10 +72,16 @@ class Communicator:
     precision.  ``precision='mixed'`` is FP32 with the radial Hankel and
     derivative GEMMs as BF16x3 split-precision products on the tensor cores
     (FP32 accumulation).  ``seed`` seeds the host generator of the plasma injector's
-    random draws.  Keyword arguments of the reference's OpenCL context choice
+    random draws.  ``compensated_positions=True`` holds each coordinate of a
+    mobile species as the sum of its value and a low part of the same type
+    (``x_lo``, ``y_lo``, ``z_lo`` in ``DataDev``), so that FP32 coordinates
+    keep displacements below their last place over long runs; the sort,
+    deposits and gather read the coordinate itself.  It costs 24 bytes per
+    particle per push and is off by default.  Keyword arguments of the reference's OpenCL context choice
     (``answers``, ``interactive``) are accepted and ignored."""
 
-    def __init__(self, precision="fp64", device=0, seed=0, verbose=False, **ctx_kw_args):
+    def __init__(self, precision="fp64", device=0, seed=0, verbose=False,
+                 compensated_positions=False, **ctx_kw_args):
         _lib.require_cuda()
         _lib.load()
         if precision not in ("fp64", "fp32", "mixed"):
@@ -97,6 +103,7 @@ class Communicator:
         self.cplx = torch.complex128 if precision == "fp64" else torch.complex64
         self.ccl = CCL_F64 if precision == "fp64" else CCL_F32
         self.dht_impl = "bf16x3" if precision == "mixed" else "simt"
+        self.compensated = bool(compensated_positions)
         # host<->device traffic issued by the methods (injector draws,
         # profile knots, lazy scalar reads), for end-to-end accounting
         self.h2d_bytes = 0

@@ -22,7 +22,18 @@ class ParticleMethodsCU(GenericMethodsCU):
     def _comps(self):
         if "Immobile" in self.Args:
             return ["x", "y", "z", "w"]
-        return ["x", "y", "z", "px", "py", "pz", "w", "g_inv"]
+        comps = ["x", "y", "z", "px", "py", "pz", "w", "g_inv"]
+        if self.comm.compensated:
+            comps += ["x_lo", "y_lo", "z_lo"]
+        return comps
+
+    def _new_low_parts(self, Np):
+        """Zero low parts of the coordinates of Np new particles (the
+        coordinates themselves are then exact)."""
+        if "x_lo" in self._comps():
+            for arg in ("x_lo", "y_lo", "z_lo"):
+                self.DataDev[arg + "_new"] = torch.zeros(Np, dtype=self.comm.real,
+                                                         device=self.comm.device)
 
     def add_new_particles(self, source=None):
         """particles_methods_cl.py:40-64"""
@@ -46,6 +57,7 @@ class ParticleMethodsCU(GenericMethodsCU):
         real = self.comm.real
         for arg in ("x", "y", "z", "w"):
             D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+        self._new_low_parts(Np)
         theta = self.dev_arr(shape=ncells, dtype=np.double)
         self._fill_arr_rand(theta, xmin=0, xmax=2 * np.pi)
         Xg_d, Rg_d = self.dev_arr(val=Xg), self.dev_arr(val=Rg)
@@ -90,6 +102,7 @@ class ParticleMethodsCU(GenericMethodsCU):
         real = self.comm.real
         for arg in ("x", "y", "z", "px", "py", "pz", "w"):
             D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
+        self._new_low_parts(Np)
         for arg in ("x", "y", "z"):
             self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"], sigma=parts_in["L" + arg])
         for arg in ("px", "py", "pz"):
@@ -125,6 +138,12 @@ class ParticleMethodsCU(GenericMethodsCU):
             return
         D = self.DataDev
         dt = self.Args["dt_2"] if mode == "half" else self.Args["dt"]
+        if "x_lo" in D:
+            call("ccl_push_x_compensated", self._dt, self.Args["Np"],
+                 *[D[k].data_ptr() for k in ("x", "y", "z", "x_lo", "y_lo", "z_lo", "px", "py",
+                                             "pz", "g_inv")], float(dt), stream())
+            self.flag_sorted = False
+            return
         call("ccl_push_x", self._dt, self.Args["Np"], D["x"].data_ptr(), D["y"].data_ptr(),
              D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(), D["pz"].data_ptr(),
              D["g_inv"].data_ptr(), float(dt), stream())

@@ -1,10 +1,11 @@
 """Solver wrapper (the reference's chimeraCL/solver.py): grid + transformer
 + PSATD coefficients; push, damp and B-restore entry points."""
 import numpy as np
+import torch
 
 from ._lib import PP, call, ints, stream
 from .grid import Grid
-from .methods.solver_methods_cu import SolverMethodsCU
+from .methods.solver_methods_cu import SolverMethodsCU, psatd_split_coefficients
 from .transformer import Transformer
 
 
@@ -50,7 +51,8 @@ class Solver(Grid, Transformer, SolverMethodsCU):
 
     def _make_ms_coefficients(self):
         """cos(w dt), sin(w dt) w and 1/w^2 per mode (solver.py:41-52), in
-        float64 on the host."""
+        float64 on the host; with FP32 fields also the eight coefficients of
+        the cancellation-free form of the update."""
         for m in range(self.Args["M"] + 1):
             w = self.Args["w_m" + str(m)]
             dt = self.Args["dt"]
@@ -59,3 +61,9 @@ class Solver(Grid, Transformer, SolverMethodsCU):
             self.Args["MxSlv_1/w**2_m" + str(m)] = 1.0 / w ** 2
             for k in ("MxSlv_cos(wdt)_m", "MxSlv_sin(wdt)*w_m", "MxSlv_1/w**2_m"):
                 self.Args["dont_keep"].append(k + str(m))
+            comm = getattr(self, "comm", None)
+            if comm is not None and comm.real != torch.float64:
+                # FP32 fields: the cancellation-free form of the same update
+                self.Args["MxSlv_split_m" + str(m)] = psatd_split_coefficients(w, dt).astype(
+                    np.float32)
+                self.Args["dont_keep"].append("MxSlv_split_m" + str(m))

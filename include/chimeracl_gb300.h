@@ -56,6 +56,18 @@ int ccl_push_x(int dtype, long np, void *x, void *y, void *z, const void *px,
                const void *py, const void *pz, const void *g_inv, double dt,
                void *stream);
 
+/* The same push with each coordinate held as the unevaluated sum hi + lo
+ * (x + x_lo, ...): the displacement of push_xyz is added by a two-sum into
+ * the low part and the pair renormalised, so x stays the nearest value to
+ * the compensated coordinate.  No counterpart in the reference (its
+ * coordinates are FP64); it keeps FP32 coordinates from losing the
+ * displacements below half a unit in the last place (a slow particle stops,
+ * and its charge and current then disagree).  x_lo, y_lo, z_lo start at 0
+ * for new particles. */
+int ccl_push_x_compensated(int dtype, long np, void *x, void *y, void *z, void *x_lo,
+                           void *y_lo, void *z_lo, const void *px, const void *py,
+                           const void *pz, const void *g_inv, double dt, void *stream);
+
 /* Bytes of device workspace ccl_index_sort needs for np particles on a grid
  * of ncells = (Nx-1)*(Nr-1) cells. */
 int ccl_index_sort_workspace(long np, long ncells, size_t *bytes);
@@ -310,6 +322,21 @@ int ccl_dht_bf16x3_status(int reset);
 int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
                       const void *c2, const void *c3, void *const *flds,
                       void *stream);
+
+/* The same update with cancellation-free coefficients, for FP32 fields
+ * (the FP32 form's advance_fields).  coef[8*i .. 8*i+7] per spectral cell,
+ * formed in double with x = w dt:
+ *   cos x, w sin x, s = sin x / w, 2 pi s, 2 pi (1 - cos x),
+ *   2 pi (cos x - sin x / x) / w^2, 2 pi (sin x / x - 1) / w^2,
+ *   2 pi (1 - cos x) / (w^2 dt)
+ * (the last three by their Taylor series for small x); then
+ *   E1 = c1 E0 + s G0 - 2 pi s J + a N0 + b N1,
+ *   G1 = -c2 E0 + c1 G0 + q J + d (N0 - N1) - 2 pi s N0.
+ * Algebraically ccl_psatd_advance; the reference's grouping forms the
+ * small charge and current terms of long-wavelength modes (w dt ~ 1e-3)
+ * as differences of O(1) terms, which keep only 1-2 digits in FP32. */
+int ccl_psatd_advance_split(int dtype, long ncells, const void *coef, void *const *flds,
+                            void *stream);
 
 /* out[ir, ix] = (-Re, +Im) of in[ir, (nx-ix) mod nx]: the m=-1 mirror.
  * Replaces _get_mm1_vec/_scl -> get_m1 (transformer_methods_cl.py:265-288,

@@ -21,7 +21,7 @@ def small_lpa(Nx=64, Nr=16, M=1, Xmin=-40.0, Xmax=0.0, Rmax=20.0, nppc=(2, 2, 4)
         profiles=profiles, seed=seed)
 
 
-def build_product(cfg, precision="fp64"):
+def build_product(cfg, precision="fp64", **comm_kw):
     from chimeracl_gb300 import Communicator
     from chimeracl_gb300.frame import Frame
     from chimeracl_gb300.laser import add_gausian_pulse
@@ -30,7 +30,7 @@ def build_product(cfg, precision="fp64"):
     from chimeracl_gb300.solver import Solver
 
     seed = cfg["seed"]
-    comm = Communicator(precision=precision, seed=seed)
+    comm = Communicator(precision=precision, seed=seed, **comm_kw)
     solver = Solver(copy.deepcopy(cfg["grid_in"]), comm)
     if cfg["laser_in"] is not None:
         add_gausian_pulse(solver, dict(cfg["laser_in"]))

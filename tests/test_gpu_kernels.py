@@ -176,6 +176,77 @@ def test_push_x_bit_exact(cuda, port):
         np.testing.assert_array_equal(host(d[k]), p[k])
 
 
+def compensated_push_np(hi, lo, p, g_inv, dt):
+    """numpy restatement of ccl_push_x_compensated for one coordinate, in
+    the arrays' own type (IEEE round-to-nearest, like the kernel's _rn adds):
+    d as push_xyz forms it, Knuth's two-sum of hi + d, the error added to
+    lo, Dekker's fast two-sum renormalisation."""
+    t = hi.dtype.type
+    d = p * (t(dt) * g_inv)
+    s = hi + d
+    bp = s - hi
+    e = (hi - (s - bp)) + (d - bp)
+    l = lo + e
+    h2 = s + l
+    return h2, l - (h2 - s)
+
+
+@pytest.mark.parametrize("dtype", [CCL_F32, CCL_F64])
+def test_push_x_compensated_bit_exact(cuda, dtype):
+    rng = np.random.default_rng(11)
+    npt = np.float32 if dtype == CCL_F32 else np.float64
+    p = {k: v.astype(npt) for k, v in particles(rng, 100003, geom(Xmin=-90.0, Xmax=-10.0)).items()}
+    for k in ("x", "y", "z"):  # some low parts already carried
+        p[k + "_lo"] = (rng.uniform(-0.5, 0.5, p[k].size) * np.spacing(p[k])).astype(npt)
+    names = ("x", "y", "z", "x_lo", "y_lo", "z_lo", "px", "py", "pz", "g_inv")
+    d = {k: dev(p[k]) for k in names}
+    for _ in range(3):
+        call("ccl_push_x_compensated", dtype, p["x"].size, *[d[k].data_ptr() for k in names],
+             0.0195, S())
+        for c in ("x", "y", "z"):
+            p[c], p[c + "_lo"] = compensated_push_np(p[c], p[c + "_lo"], p["p" + c], p["g_inv"],
+                                                     0.0195)
+    for k in ("x", "y", "z", "x_lo", "y_lo", "z_lo"):
+        np.testing.assert_array_equal(host(d[k]), p[k], err_msg=k)
+    # the renormalised pair: hi is the nearest value to hi + lo
+    for c in ("x", "y", "z"):
+        assert np.all(np.abs(p[c + "_lo"]) <= 0.5 * np.spacing(np.abs(p[c])))
+
+
+def test_push_x_compensated_tracks_exact_sum(cuda):
+    """1000 pushes of slow and fast particles at |x| ~ 60: the compensated
+    FP32 coordinate hi + lo stays within 1e-2 FP32 units in the last place of
+    the exact sum of its FP32 displacements, where the plain FP32 push loses
+    up to half a unit per push (and a displacement below that is lost
+    whole: a slow particle does not move)."""
+    rng = np.random.default_rng(12)
+    n, steps, dt = 65536, 1000, 0.0195
+    x = rng.uniform(-70.0, -50.0, n)
+    y, z = rng.uniform(-30.0, 30.0, (2, n))
+    u = rng.normal(0, 1.0, (3, n)) * np.repeat([1e-5, 1e-3, 1e-1, 1.0], n // 4)
+    g_inv = 1.0 / np.sqrt(1 + (u ** 2).sum(0))
+    f32 = {k: v.astype(np.float32) for k, v in dict(x=x, y=y, z=z, px=u[0], py=u[1], pz=u[2],
+                                                      g_inv=g_inv).items()}
+    comp = {k: dev(v) for k, v in f32.items()}
+    plain = {k: dev(v) for k, v in f32.items()}
+    for c in ("x", "y", "z"):
+        comp[c + "_lo"] = dev(np.zeros(n, np.float32))
+    cn = ("x", "y", "z", "x_lo", "y_lo", "z_lo", "px", "py", "pz", "g_inv")
+    pn = ("x", "y", "z", "px", "py", "pz", "g_inv")
+    for _ in range(steps):
+        call("ccl_push_x_compensated", CCL_F32, n, *[comp[k].data_ptr() for k in cn], dt, S())
+        call("ccl_push_x", CCL_F32, n, *[plain[k].data_ptr() for k in pn], dt, S())
+    dt_g = np.float32(dt) * f32["g_inv"]
+    for c in ("x", "y", "z"):
+        d = (f32["p" + c] * dt_g).astype(np.float64)  # the kernel's displacement
+        exact = f32[c].astype(np.float64) + steps * d
+        ulp = np.spacing(np.maximum(np.abs(exact), np.abs(f32[c])).astype(np.float32))
+        ec = np.abs(host(comp[c]).astype(np.float64) + host(comp[c + "_lo"]) - exact) / ulp
+        ep = np.abs(host(plain[c]).astype(np.float64) - exact) / ulp
+        assert ec.max() < 1e-2, (c, ec.max())
+        assert ep.max() > 10.0, (c, ep.max())
+
+
 def test_align_bit_exact(cuda, port):
     rng = np.random.default_rng(2)
     g = geom()
@@ -431,6 +502,31 @@ def test_psatd_bit_exact(cuda, port):
          dev(c3).data_ptr(), PP(d), S())
     for i in range(6):
         np.testing.assert_array_equal(host(d[i]), ref[i])
+
+
+@pytest.mark.parametrize("sources_only", [False, True])
+def test_psatd_split_fp32(cuda, port, sources_only):
+    """The FP32 form's update (cancellation-free coefficients) against the
+    oracle's FP64 advance_e_g_m on the same FP32-representable inputs, over
+    w dt from 1e-3 (long waves) to 3: within 1e-6 of each output's norm,
+    also for the source response alone (E = G = 0), whose long-wave part
+    the reference's grouping would keep to 1-2 digits in FP32."""
+    from chimeracl_gb300.methods.solver_methods_cu import psatd_split_coefficients
+    rng = np.random.default_rng(42)
+    n, dt = 63 * 512, 0.039
+    w = np.exp(rng.uniform(np.log(1e-3), np.log(3.0), n)) / dt
+    f = [cplx(rng, n).astype(np.complex64).astype(np.complex128) for _ in range(15)]
+    if sources_only:
+        for k in range(6):
+            f[k][:] = 0
+    ref = [a.copy() for a in f]
+    port.advance_e_g_m(1 / dt, np.cos(w * dt), np.sin(w * dt) * w, 1 / w ** 2, ref)
+    coef = dev(psatd_split_coefficients(w, dt).astype(np.float32))
+    d = [dev(a.astype(np.complex64)) for a in f]
+    call("ccl_psatd_advance_split", CCL_F32, n, coef.data_ptr(), PP(d), S())
+    for i in range(6):
+        got = host(d[i]).astype(np.complex128)
+        assert np.linalg.norm(got - ref[i]) <= 1e-6 * np.linalg.norm(ref[i]), i
 
 
 def test_elementwise_bit_exact(cuda, port):
