@@ -92,12 +92,12 @@ template <int M, bool VEC>
 __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (1 + 2 * M)],
                                              float xp, float yp, float zp, float wraw, float ux,
                                              float uy, float uz, float gi, float q,
-                                             const GridP<float> &g, float fix, float fir) {
+                                             const GridP<float> &g, CellEdge ex, CellEdge er) {
   constexpr int NK = VEC ? 3 : 1, B = 1 + 2 * M;
   const float wp = VEC ? wraw * gi * q : wraw * q;
   const float r2 = yp * yp + zp * zp;
   const float rinv = r2 > 0.f ? rsqrtf(r2) : (VEC ? 0.f : __int_as_float(0x7f800000));
-  const float rp = sqrtf(r2);
+  const float rp = radius_from_rsqrt(r2, rinv);
   float e[M + 1][2];
   e[0][0] = 1.f;
   e[0][1] = 0.f;
@@ -110,8 +110,8 @@ __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (
     e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
     e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
   }
-  const float sX1 = frac_x(xp, (int)fix, g), sX0 = 1.f - sX1;
-  const float sR1 = frac_r(rp, (int)fir, g), sR0 = 1.f - sR1;
+  const float sX1 = edge_frac(xp, ex, g.dx_inv), sX0 = 1.f - sX1;
+  const float sR1 = edge_frac(rp, er, g.dr_inv), sR0 = 1.f - sR1;
   const float wX0 = sX0 * wp, wX1 = sX1 * wp;
   const float C[4] = {sR0 * wX0, sR0 * wX1, sR1 * wX0, sR1 * wX1};
   const float jp[3] = {VEC ? ux : 1.f, uy, uz};
@@ -178,12 +178,17 @@ __global__ void __launch_bounds__(DEP_THREADS)
     const long cg = (long)ix + (long)ir * (Nx - 1);
     const u32 p0 = cell_off[cg], p1 = cell_off[cg + 1];
     const T fix = (T)ix, fir = (T)ir;
+    CellEdge ex{}, er{};  // FP32: this thread's cell edges, formed once
+    if constexpr (sizeof(T) == 4) {
+      ex = x_edge(g, ix);
+      er = r_edge(g, ir);
+    }
     for (u32 ip = p0; ip < p1; ip++) {
       const u32 p = sort_indx[ip];
       const T a = VEC ? ux[p] : T(0), b = VEC ? uy[p] : T(0), c = VEC ? uz[p] : T(0),
               d = VEC ? g_inv[p] : T(0);
       if constexpr (sizeof(T) == 4)
-        dep_particle_f32<M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, fix, fir);
+        dep_particle_f32<M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, ex, er);
       else
         dep_particle<T, M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, fix, fir);
     }
@@ -440,7 +445,7 @@ __global__ void __launch_bounds__(256)
     const float xp = x[p], yp = y[p], zp = z[p];
     const float r2 = yp * yp + zp * zp;
     const float rinv = r2 > 0.f ? rsqrtf(r2) : __int_as_float(0x7f800000);
-    const float rp = sqrtf(r2);
+    const float rp = radius_from_rsqrt(r2, rinv);
     const float fx = (xp - g.xmin) * g.dx_inv, fr = (rp - g.rmin) * g.dr_inv;
     const int ix = floor_to_int<float>(floorf(fx), -1);
     const int ir = floor_to_int<float>(floorf(fr), 1 << 30);
@@ -532,9 +537,12 @@ __global__ void __launch_bounds__(GT_THREADS)
   constexpr int NS = gt_stride(M);
   extern __shared__ __align__(16) float gsm[];  // [GT_NR][GT_NX][NS]
   __shared__ u32 row_a[GT_TR], row_pre[GT_TR + 1];
+  __shared__ CellEdge xedge[GT_TX], redge[GT_TR];  // the tile's cell edges
   const int Nx = g.Nx, Nr = g.Nr, nxc = Nx - 1;
   const int nx0 = blockIdx.x * GT_TX, nr0 = blockIdx.y * GT_TR;
   const u32 np_stay = *np_stay_p;
+  if (threadIdx.x < GT_TX) xedge[threadIdx.x] = x_edge(g, nx0 + threadIdx.x);
+  else if (threadIdx.x < GT_TX + GT_TR) redge[threadIdx.x - GT_TX] = r_edge(g, nr0 + threadIdx.x - GT_TX);
   // 1. node tile: [ex ey ez bx by bz] (m = 0), then per mode m >= 1 the same
   //    six as 2*(re, im)
   for (int t = threadIdx.x; t < GT_NR * GT_NX; t += GT_THREADS) {
@@ -585,12 +593,11 @@ __global__ void __launch_bounds__(GT_THREADS)
     const float r2 = yp * yp + zp * zp;
     const float rp = sqrtf(r2);
     const float rinv = r2 > 0.f ? 1.f / rp : __int_as_float(0x7f800000);
-    const float fx = (xp - g.xmin) * g.dx_inv, fr = (rp - g.rmin) * g.dr_inv;
+    const float fx = (xp - g.xmin) * g.dx_inv;
     int ix = (int)floorf(fx);
     ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
-    const int ir = nr0 + r;
-    const float sX1 = frac_x(xp, ix, g), sX0 = 1.f - sX1;
-    const float sR1 = frac_r(rp, ir, g), sR0 = 1.f - sR1;
+    const float sX1 = edge_frac(xp, xedge[ix - nx0], g.dx_inv), sX0 = 1.f - sX1;
+    const float sR1 = edge_frac(rp, redge[r], g.dr_inv), sR0 = 1.f - sR1;
     const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
     const int l0 = (r * GT_NX + (ix - nx0)) * NS;
     const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};

@@ -185,6 +185,8 @@ int Ops<T>::psatd_split(long n, const void *coef, void *const *flds, cudaStream_
     CCL_REQUIRE(flds[i], CCL_ERR_ARG, "psatd_split: null field %d", i);
     f.p[i] = flds[i];
   }
+  CCL_REQUIRE(((uintptr_t)coef & 15) == 0, CCL_ERR_ARG,
+              "psatd_split: coefficient array not 16-byte aligned");
   if (n == 0) return CCL_OK;
   k_psatd_split<T><<<grid_for(n, 256), 256, 0, s>>>(n, (const T *)coef, f);
   CCL_LAUNCH_CHECK("psatd_split");

@@ -181,22 +181,42 @@ inline GridP<T> make_gridp(int Nx, int Nr, double xmin, double dx_inv, double rm
 // fraction keeps v's own precision.  The plain (v - o) / h - i rounds at
 // the magnitude of the cell count: at ~2000 cells an FP32 unit in the last
 // place is 1.2e-4 of a cell, which every shape-function weight then carries.
-__device__ __forceinline__ float cell_frac(float v, int i, float o_hi, float o_lo, float h_hi,
-                                           float h_lo, float h_inv) {
+// (A kernel whose cell is fixed per thread or per tile forms the edge once.)
+struct CellEdge {
+  float hi, lo;
+};
+__device__ __forceinline__ CellEdge cell_edge(int i, float o_hi, float o_lo, float h_hi,
+                                              float h_lo) {
   const float fi = (float)i;
   const float p = __fmul_rn(fi, h_hi);
   const float pe = __fmaf_rn(fi, h_hi, -p);  // fi h_hi - p, exactly
   const float c = __fadd_rn(o_hi, p);
   const float bp = __fsub_rn(c, o_hi);
   const float ce = __fadd_rn(__fsub_rn(o_hi, __fsub_rn(c, bp)), __fsub_rn(p, bp));  // o_hi + p - c
-  const float c_lo = __fadd_rn(__fadd_rn(ce, pe), __fmaf_rn(fi, h_lo, o_lo));
-  return __fmul_rn(__fsub_rn(__fsub_rn(v, c), c_lo), h_inv);
+  return CellEdge{c, __fadd_rn(__fadd_rn(ce, pe), __fmaf_rn(fi, h_lo, o_lo))};
+}
+__device__ __forceinline__ float edge_frac(float v, CellEdge e, float h_inv) {
+  return __fmul_rn(__fsub_rn(__fsub_rn(v, e.hi), e.lo), h_inv);
+}
+__device__ __forceinline__ CellEdge x_edge(const GridP<float> &g, int ix) {
+  return cell_edge(ix, g.xmin, g.xmin_lo, g.dx, g.dx_lo);
+}
+__device__ __forceinline__ CellEdge r_edge(const GridP<float> &g, int ir) {
+  return cell_edge(ir, g.rmin, g.rmin_lo, g.dr, g.dr_lo);
+}
+// r = sqrt(r2) from rinv = rsqrt(r2) (which the kernels need for e^{i m phi}
+// anyway) with one Newton correction: within a unit in the last place, where
+// r2 * rinv alone carries rsqrt's approximation error.  0 for r2 = 0.
+__device__ __forceinline__ float radius_from_rsqrt(float r2, float rinv) {
+  if (!(r2 > 0.f)) return 0.f;
+  const float r = r2 * rinv;
+  return fmaf(fmaf(-r, r, r2), 0.5f * rinv, r);
 }
 __device__ __forceinline__ float frac_x(float xp, int ix, const GridP<float> &g) {
-  return cell_frac(xp, ix, g.xmin, g.xmin_lo, g.dx, g.dx_lo, g.dx_inv);
+  return edge_frac(xp, x_edge(g, ix), g.dx_inv);
 }
 __device__ __forceinline__ float frac_r(float rp, int ir, const GridP<float> &g) {
-  return cell_frac(rp, ir, g.rmin, g.rmin_lo, g.dr, g.dr_lo, g.dr_inv);
+  return edge_frac(rp, r_edge(g, ir), g.dr_inv);
 }
 
 template <typename T>

@@ -63,8 +63,14 @@ __global__ void __launch_bounds__(256)
     k_psatd_split(long n, const T *__restrict__ coef, ptrs<15> f) {
   CCL_GRID_STRIDE(i, n) {
     T c[8];
+    if constexpr (sizeof(T) == 4) {  // two 16-byte loads (the array is 32-byte aligned)
+      const float4 a = ((const float4 *)coef)[2 * i], b = ((const float4 *)coef)[2 * i + 1];
+      c[0] = a.x, c[1] = a.y, c[2] = a.z, c[3] = a.w, c[4] = b.x, c[5] = b.y, c[6] = b.z,
+      c[7] = b.w;
+    } else {
 #pragma unroll
-    for (int k = 0; k < 8; k++) c[k] = coef[8 * i + k];
+      for (int k = 0; k < 8; k++) c[k] = coef[8 * i + k];
+    }
     const T c1 = c[0], c2 = c[1], s = c[2], s2 = c[3], q2 = c[4], a2 = c[5], b2 = c[6],
             d2 = c[7];
 #pragma unroll

@@ -329,7 +329,8 @@ int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
  *   cos x, w sin x, s = sin x / w, 2 pi s, 2 pi (1 - cos x),
  *   2 pi (cos x - sin x / x) / w^2, 2 pi (sin x / x - 1) / w^2,
  *   2 pi (1 - cos x) / (w^2 dt)
- * (the last three by their Taylor series for small x); then
+ * (the last three by their Taylor series for small x; the array 16-byte
+ * aligned); then
  *   E1 = c1 E0 + s G0 - 2 pi s J + a N0 + b N1,
  *   G1 = -c2 E0 + c1 G0 + q J + d (N0 - N1) - 2 pi s N0.
  * Algebraically ccl_psatd_advance; the reference's grouping forms the
