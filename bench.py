@@ -124,20 +124,23 @@ def diagnostics_dev(solver, eons):
     return We, ex, kin
 
 
-def field_l2_rel(sol, ref):
+def field_l2_rel(sol, ref, per_field=None):
     """Pointwise relative L2 difference of all real-space E, B modes (rows
-    r > 0) of `sol` against `ref`, in float64 on the device."""
+    r > 0) of `sol` against `ref`, in float64 on the device; each field's
+    own (E, B and rho per mode) into `per_field` if given."""
     import torch
     A = ref.Args
     num = den = 0.0
     for m in range(A["M"] + 1):
-        for f in ("E", "B"):
-            for c in "xyz":
-                k = f + c + "_m" + str(m)
-                dt = torch.complex128 if m else torch.float64
-                a, b = sol.DataDev[k][1:].to(dt), ref.DataDev[k][1:].to(dt)
-                num += float(((a - b).abs() ** 2).sum())
-                den += float((b.abs() ** 2).sum())
+        for k in [f + c + "_m" + str(m) for f in ("E", "B") for c in "xyz"] + ["rho_m" + str(m)]:
+            dt = torch.complex128 if m else torch.float64
+            a, b = sol.DataDev[k][1:].to(dt), ref.DataDev[k][1:].to(dt)
+            dn, dd = float(((a - b).abs() ** 2).sum()), float((b.abs() ** 2).sum())
+            if per_field is not None:
+                per_field[k] = float(np.sqrt(dn / dd)) if dd > 0 else None
+            if k[0] in "EB":
+                num += dn
+                den += dd
     return float(np.sqrt(num / den))
 
 
@@ -153,9 +156,12 @@ def compare_runs(cfg, run, ref):
         vals.append((float(We), wake_amplitude(ex.cpu().numpy(), A["Xgrid"], x_las,
                                                cfg["laser_in"]["Lx"]), float(kin)))
     (We, wk, kin), (We0, wk0, kin0) = vals
+    per = {}
+    l2 = field_l2_rel(run["solver"], ref["solver"], per)
     return {"field_energy_rel_err": abs(We / We0 - 1), "wake_ex_rel_err": abs(wk / wk0 - 1),
-            "kinetic_rel_err": abs(kin / kin0 - 1),
-            "field_l2_rel_err": field_l2_rel(run["solver"], ref["solver"]),
+            "kinetic_rel_err": abs(kin / kin0 - 1), "field_l2_rel_err": l2,
+            "field_l2_rel_err_per_field": {k: (None if v is None else float("%.3g" % v))
+                                           for k, v in per.items()},
             "at_step": ref["loop"].it}
 
 
