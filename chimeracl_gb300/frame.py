@@ -1,6 +1,9 @@
 """Moving window (the reference's chimeraCL/frame.py): grid shift and
 plasma injection into the uncovered slab."""
 import numpy as np
+import torch
+
+from .methods.generic_methods_cu import LazyScalar
 
 
 class Frame:
@@ -47,7 +50,11 @@ class Frame:
             sp.free_added()
             sp.sort_parts(grid=grid)
             sp.align_parts()
-            nppc = np.int32(np.prod(sp.Args["Nppc"]) + 1)
-            x_max = float(sp.DataDev["x"][-nppc:].max().item())
-            sp.comm.d2h_bytes += sp.DataDev["x"].element_size()
-            sp.Args["right_lim"] = x_max + 0.5 * sp.Args["ddx"]
+            # right_lim = max x of the last Nppc+1 particles + ddx/2, kept on
+            # the device until the next shift reads it (the value is the
+            # same double sum; the read no longer stalls this step)
+            if sp.Args["Np"] > 0:
+                nppc = int(np.prod(sp.Args["Nppc"]) + 1)
+                x_max = sp.DataDev["x"][-nppc:].max().to(torch.float64)
+                dict.__setitem__(sp.Args, "right_lim",
+                                 LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))

@@ -35,22 +35,25 @@ def torch_dtype(dtype):
 
 
 class LazyScalar:
-    """A device scalar read back only when the host asks for its value."""
+    """A device scalar read back only when the host asks for its value
+    (as an int, or through ``cast``)."""
 
-    def __init__(self, tensor, comm=None):
+    def __init__(self, tensor, comm=None, cast=int):
         self.tensor = tensor
         self.comm = comm
+        self.cast = cast
 
     def resolve(self):
         if self.comm is not None:
             self.comm.d2h_bytes += self.tensor.element_size()
-        return int(self.tensor.item())
+        return self.cast(self.tensor.item())
 
 
 class ArgsDict(dict):
     """``Args`` container: a plain dict, except that values held as
-    ``LazyScalar`` (the in-window particle count after a sort) are read from
-    the device the first time they are looked up."""
+    ``LazyScalar`` (the in-window particle count after a sort, the injector's
+    right limit after a window shift) are read from the device the first
+    time they are looked up."""
 
     def __getitem__(self, k):
         v = dict.__getitem__(self, k)

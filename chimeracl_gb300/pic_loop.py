@@ -10,11 +10,17 @@ With ``timit=True`` each phase is timed on the device with CUDA events under
 the reference's twelve phase names (device time, no host synchronisation
 inside the step; ``Timer`` is filled when read through ``timings()``).
 
-With ``graphs=True`` the steps between window shifts -- which change no
-particle count and allocate nothing -- run as a CUDA graph: the first such
-step after a shift is captured, later ones replay it (the launch sequence of
-a step is ~150 kernels).  A signature of every device buffer and particle
-count guards the replay; anything that changes it is captured anew."""
+With ``graphs=True`` the step runs as three CUDA graphs replayed in order:
+the particle work before the field solve (pushes, sorts, deposits), the
+field solve (transforms, gradient, PSATD push, damping, B, backward
+transforms) and the gather + push.  Each is captured on first use and
+replayed while a signature of what its launches depend on is unchanged:
+device buffers, particle counts and the grid origin for the particle
+pieces; the solver's buffers alone for the field piece.  A window shift
+(host-driven injection, new particle counts and origin) therefore runs only
+the particle pieces eagerly and captures them again -- the field solve,
+~65 of the step's library calls, is replayed through the shift (its phase
+factors are refreshed in place first)."""
 import numpy as np
 import torch
 
@@ -49,14 +55,13 @@ class PIC_loop:
         self.Timer = {k: 0.0 for k in loop_steps}
         self._events = []
         self.graphs = graphs
-        self._graph = None
-        self._graph_sig = None
-        self.graph_replays = 0
-        self.graph_captures = 0
+        # piece name -> [graph, signature, library kernels in it]
+        self._graphs = {}
+        self.graph_replays = 0  # steps served by graph replays
+        self.graph_captures = 0  # pieces captured
         self._cap_stream = None
-        # library kernels per captured step, and totals captured / replayed
-        # (a replay runs the captured kernels without launching them again)
-        self._graph_kernels = 0
+        # library kernels captured / replayed in total (a replay runs the
+        # captured kernels without launching them again)
         self.graph_kernels_captured = 0
         self.graph_kernels_replayed = 0
 
@@ -83,47 +88,77 @@ class PIC_loop:
     def _frame_due(self):
         return any(np.mod(self.it, fr.Args["Steps"]) == 0 for fr in self.frames)
 
-    def _signature(self):
-        sig = []
-        for obj in list(self.solvers) + list(self.species):
-            for k, v in obj.DataDev.items():
-                if isinstance(v, torch.Tensor):
-                    sig.append((k, v.data_ptr(), v.numel()))
-            sig.append(obj.Args.get("Np", None) if hasattr(obj.Args, "get") else None)
-        for sol in self.solvers:
-            sig.append(float(sol.Args["Xmin"]))
-        return tuple(sig)
+    def _signature(self, piece):
+        """What a piece's launches depend on: the identity of every device
+        buffer (DataDev entries are rebound, never resized in place), the
+        particle counts and the grid origin (the field piece: the solvers'
+        buffers alone).  Returns (key, refs): comparing keys is a tuple of
+        ints; the graph keeps refs, so that no id is reused while it lives."""
+        objs = list(self.solvers) + ([] if piece == "f" else list(self.species))
+        # (phs_shft names whichever phase buffer was used last)
+        refs = tuple(v for obj in objs for k, v in obj.DataDev.items() if k != "phs_shft")
+        key = [tuple(map(id, refs))]
+        if piece != "f":
+            key += [obj.Args.get("Np", None) if hasattr(obj.Args, "get") else None
+                    for obj in objs]
+            key += [float(sol.Args["Xmin"]) for sol in self.solvers]
+        return tuple(key), refs
+
+    def _piece_fn(self, piece):
+        return {"pa": self._particles_before, "f": self._fields,
+                "pb": self._particles_after}[piece]
 
     def step(self):
         for diag in self.diags:
             diag.make_record(self.it)
         use_graph = self.graphs and not self.timit and not self.diags and self.it > 0
         if not use_graph:
-            self._graph = None
+            self._graphs = {}
             self._body(graph_mode=False)
         elif self._frame_due():
-            # a window shift (host-driven injection, new array sizes) runs
-            # eagerly; the graph for the steps that follow is captured right
-            # after it, while the device still executes this step
-            self._graph = None
-            self._body(graph_mode=False)
-            self._capture()
-        else:
-            if self._graph is None or self._signature() != self._graph_sig:
-                self._capture()
-            self._graph.replay()
+            # a window shift: host-driven injection, new particle counts and
+            # origin.  The particle pieces run eagerly and are captured again
+            # right after, while the device still executes this step; the
+            # field solve replays (its phase factors are moved first)
+            self._frame_part()
+            for sol in self.solvers:
+                sol._phase(0)
+                sol._phase(1)
+            self._particles_before(graph_mode=True)
+            self._run_piece("f")
+            self._particles_after(graph_mode=True)
+            for piece in ("pa", "pb"):
+                self._capture(piece)
             self.graph_replays += 1
-            self.graph_kernels_replayed += self._graph_kernels
+        else:
+            full = self._signature("pa")  # the same for both particle pieces
+            for piece in ("pa", "f", "pb"):
+                self._run_piece(piece, full if piece != "f" else None)
+            self.graph_replays += 1
         self.it += 1
         return self.it
 
-    def _capture(self):
-        """Capture the step without its window shift (what every step between
-        shifts runs) into a CUDA graph, on a persistent side stream with the
-        graph's own memory pool; unlike torch.cuda.graph() this neither
-        synchronises the device nor empties the allocator's cache."""
+    def _run_piece(self, piece, sig=None):
+        g = self._graphs.get(piece)
+        if g is None or (sig or self._signature(piece))[0] != g[1][0]:
+            self._capture(piece)
+            g = self._graphs[piece]
+        g[0].replay()
+        self.graph_kernels_replayed += g[2]
+
+    def _capture(self, piece):
+        """Capture one piece of the step into a CUDA graph, on a persistent
+        side stream with the graph's own memory pool; unlike
+        torch.cuda.graph() this neither synchronises the device nor empties
+        the allocator's cache."""
         from . import _lib
-        self._graph = None
+        self._graphs.pop(piece, None)
+        if piece == "f":
+            # phase factors for the current origin, outside the graph: a
+            # captured recomputation would replay the capture's origin
+            for sol in self.solvers:
+                sol._phase(0)
+                sol._phase(1)
         n0 = _lib.launch_count()
         g = torch.cuda.CUDAGraph()
         if self._cap_stream is None:
@@ -133,15 +168,14 @@ class PIC_loop:
         with torch.cuda.stream(self._cap_stream):
             g.capture_begin()
             try:
-                self._step_part(graph_mode=True)
+                self._piece_fn(piece)(graph_mode=True)
             finally:
                 g.capture_end()
         cur.wait_stream(self._cap_stream)
-        self._graph_kernels = _lib.launch_count() - n0
-        self._graph = g
-        self._graph_sig = self._signature()
+        nk = _lib.launch_count() - n0
+        self._graphs[piece] = [g, self._signature(piece), nk]
         self.graph_captures += 1
-        self.graph_kernels_captured += self._graph_kernels
+        self.graph_kernels_captured += nk
 
     def _body(self, graph_mode):
         self._frame_part()
@@ -156,6 +190,13 @@ class PIC_loop:
         self.timer_record("frame")
 
     def _step_part(self, graph_mode):
+        self._particles_before(graph_mode)
+        self._fields(graph_mode)
+        self._particles_after(graph_mode)
+
+    def _particles_before(self, graph_mode):
+        """Half push + sort, current deposit, half push + sort, charge
+        deposit (pic_loop.py:73-98)."""
         for parts in self.species:
             self.timer_start()
             parts.push_coords(mode="half")
@@ -182,6 +223,11 @@ class PIC_loop:
             solver.depose_charge(species=self.species)
             self.timer_record("depose")
 
+    def _fields(self, graph_mode):
+        """Forward transforms with smoothing, dN0 <- dN1, gradient, PSATD
+        push, damping, B, backward transforms (pic_loop.py:100-135): reads
+        and writes the solver's buffers only."""
+        for solver in self.solvers:
             self.timer_start()
             M = solver.Args["M"]
             if self.fuse_smooth:
@@ -225,9 +271,12 @@ class PIC_loop:
             self.timer_start()
             solver.fb_transform(vects=["E", "B"], dir=1)
             self.timer_record("transform")
+
+    def _particles_after(self, graph_mode):
+        """Ghost rows of E, B, gather + Boris push (pic_loop.py:137-142)."""
+        for solver in self.solvers:
             self.timer_start()
             solver.gather_and_push(species=self.species)
             self.timer_record("gather + push-p")
-
         for parts in self.species:
             parts.free_mp()
