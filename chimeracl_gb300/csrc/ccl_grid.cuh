@@ -183,6 +183,9 @@ __global__ void __launch_bounds__(DEP_THREADS)
       ex = x_edge(g, ix);
       er = r_edge(g, ir);
     }
+    // two particles in flight (their dependent loads overlap); the
+    // accumulation order is unchanged
+#pragma unroll 2
     for (u32 ip = p0; ip < p1; ip++) {
       const u32 p = sort_indx[ip];
       const T a = VEC ? ux[p] : T(0), b = VEC ? uy[p] : T(0), c = VEC ? uz[p] : T(0),
