@@ -631,10 +631,11 @@ def diagnostics(solver, species):
 
 
 def build_lpa(grid_in, eons_in, frame_in=None, laser_in=None, prefill=None, K=None, seed=0,
-              density_profiles=None):
+              density_profiles=None, ion_mass=None):
     """Set up solver + electrons + immobile ions (+ frame, laser, prefilled
     window) the way the reference's example scripts do
-    (examples/lpa_script_small.py:51-95)."""
+    (examples/lpa_script_small.py:51-95); with ion_mass the ions are a
+    second mobile species of that mass."""
     K = K or get_kernels("port")
     solver = OGrid(copy.deepcopy(grid_in), K)
     if laser_in is not None:
@@ -643,7 +644,10 @@ def build_lpa(grid_in, eons_in, frame_in=None, laser_in=None, prefill=None, K=No
     e_in.update(dx=solver.Args["dx"], dr=solver.Args["dr"], dt=solver.Args["dt"])
     i_in = copy.deepcopy(e_in)
     i_in["charge"] = 1
-    i_in["Immobile"] = True
+    if ion_mass is None:
+        i_in["Immobile"] = True
+    else:
+        i_in["mass"] = ion_mass
     eons = OSpecies(e_in, K, seed=seed)
     ions = OSpecies(i_in, K, seed=seed + 1)
     ions.Args["InjectorSource"] = eons

@@ -21,7 +21,8 @@ def small_lpa(Nx=64, Nr=16, M=1, Xmin=-40.0, Xmax=0.0, Rmax=20.0, nppc=(2, 2, 4)
         profiles=profiles, seed=seed)
 
 
-def build_product(cfg, precision="fp64", **comm_kw):
+def build_product(cfg, precision="fp64", ion_mass=None, **comm_kw):
+    """ion_mass: the ions move, with that mass (else they are immobile)."""
     from chimeracl_gb300 import Communicator
     from chimeracl_gb300.frame import Frame
     from chimeracl_gb300.laser import add_gausian_pulse
@@ -38,7 +39,10 @@ def build_product(cfg, precision="fp64", **comm_kw):
     e_in.update(dx=solver.Args["dx"], dr=solver.Args["dr"], dt=solver.Args["dt"])
     i_in = copy.deepcopy(e_in)
     i_in["charge"] = 1
-    i_in["Immobile"] = True
+    if ion_mass is None:
+        i_in["Immobile"] = True
+    else:
+        i_in["mass"] = ion_mass
     eons = Particles(e_in, comm, seed=seed)
     ions = Particles(i_in, comm, seed=seed + 1)
     ions.Args["InjectorSource"] = eons
@@ -57,14 +61,14 @@ def build_product(cfg, precision="fp64", **comm_kw):
     return solver, eons, ions, loop
 
 
-def build_oracle(cfg, kind="port"):
+def build_oracle(cfg, kind="port", ion_mass=None):
     from oracle import pic_oracle as po
     from oracle.kernels import get_kernels
 
     K = get_kernels(kind)
     return po.build_lpa(cfg["grid_in"], cfg["eons_in"], cfg["frame_in"], cfg["laser_in"],
                         prefill=cfg["prefill"], K=K, seed=cfg["seed"],
-                        density_profiles=cfg["profiles"])
+                        density_profiles=cfg["profiles"], ion_mass=ion_mass)
 
 
 def to_np(t):

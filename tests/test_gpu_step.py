@@ -66,6 +66,32 @@ def test_25_steps_fp64_window(cuda):
     assert sol.Args["Xmin"] == osol.Args["Xmin"]
 
 
+def test_two_mobile_species_fp64(cuda):
+    """Electrons and mobile ions (charge +1, mass 100, injected on the
+    electrons) through 25 steps and two window shifts: both species' pushes
+    (their own charge-to-mass factor), sorts, current and charge deposits and
+    gathers against the oracle's loop over the same two species
+    (pic_loop.py:73-142).  Bar 1e-8 of each array's magnitude: the
+    injector's y, z differ from the oracle's by ulps (CUDA's sin/cos vs the
+    host libm), and the a0 = 3 pulse grows that to ~1.4e-9 in the momenta
+    over 25 steps; a wrong charge-to-mass factor or a species left out of a
+    deposit or gather would differ at 1e-2 or more."""
+    cfg = small_lpa(Nx=128, Nr=32, M=1, seed=31, a0=3.0)
+    sol, e, i, loop = build_product(cfg, ion_mass=100.0)
+    osol, oe, oi, oloop = build_oracle(cfg, ion_mass=100.0)
+    for _ in range(25):
+        loop.step()
+        oloop.step()
+    torch.cuda.synchronize()
+    for p, op in ((e, oe), (i, oi)):
+        assert p.Args["Np"] == op.Args["Np"]
+        _sort_equal(p, op)
+        _particles_equal(p, op, tol=1e-8)
+    assert float(np.abs(to_np(i.DataDev["px"])).max()) > 1e-4  # the ions did move
+    worst = compare_fields(sol, osol, dens=cfg["eons_in"]["dens"])
+    assert worst < 1e-8, worst
+
+
 def test_density_profile_injection(cuda):
     prof = [{"coord": "x", "points": [-1e4, -40.0, -25.0, 1e6], "values": [0.0, 0.0, 1.0, 1.0]}]
     cfg = small_lpa(Nx=96, Nr=24, M=1, seed=9, profiles=prof, steps=5)
