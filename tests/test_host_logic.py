@@ -45,6 +45,37 @@ def test_dht_matrices_invert():
         assert np.abs(I - np.eye(I.shape[0])).max() < 1e-12
 
 
+@pytest.mark.parametrize("real", ["float64", "float32"])
+def test_psatd_coefficients_per_precision(real):
+    """FP64 fields keep the reference's three coefficient arrays alone; FP32
+    fields also get the eight cancellation-free ones, in float32."""
+    import torch
+
+    from chimeracl_gb300.grid import Grid
+    from chimeracl_gb300.methods.solver_methods_cu import psatd_split_coefficients
+    from chimeracl_gb300.solver import Solver
+    from chimeracl_gb300.transformer import Transformer
+    s = _Stub()
+    s.comm = _Stub()
+    s.comm.real = getattr(torch, real)
+    Grid._process_configs(s, dict(Xmin=-20.0, Xmax=0.0, Nx=64, Rmin=0.0, Rmax=10.0, Nr=17,
+                                  M=1))
+    Transformer._make_spectral_axes(s)
+    Transformer._make_DHT(s)
+    Solver._make_ms_coefficients(s)
+    A = s.Args
+    for m in (0, 1):
+        w, dt = A["w_m%d" % m], A["dt"]
+        np.testing.assert_array_equal(A["MxSlv_cos(wdt)_m%d" % m], np.cos(w * dt))
+        key = "MxSlv_split_m%d" % m
+        if real == "float64":
+            assert key not in A
+        else:
+            assert A[key].dtype == np.float32 and A[key].shape == w.shape + (8,)
+            np.testing.assert_array_equal(A[key], psatd_split_coefficients(w, dt).astype(np.float32))
+            assert key in A["dont_keep"]
+
+
 def test_lazy_args():
     from chimeracl_gb300.methods.generic_methods_cu import ArgsDict, LazyScalar
 
@@ -56,6 +87,9 @@ def test_lazy_args():
     dict.__setitem__(a, "Np_stay", LazyScalar(T()))
     assert a["Np_stay"] == 41 and a.get("Np_stay") == 41 and a["Np"] == 3
     assert type(dict.__getitem__(a, "Np_stay")) is int
+    # a float read back lazily (the injector's right limit)
+    dict.__setitem__(a, "right_lim", LazyScalar(T(), cast=float))
+    assert a["right_lim"] == 41.0 and type(dict.__getitem__(a, "right_lim")) is float
 
 
 def test_injector_draws_match_oracle():
