@@ -39,12 +39,18 @@ SIGNATURES = {
     "ccl_deposit_scalar": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _d, _d, _i, _d, _d, _pp, _vp],
     "ccl_deposit_vector": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                            _i, _d, _d, _i, _d, _d, _pp, _vp],
+    "ccl_deposit_scalar_lo": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _d, _d, _i, _d, _d,
+                              _pp, _vp, _vp, _vp, _vp],
+    "ccl_deposit_vector_lo": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
+                              _i, _d, _d, _i, _d, _d, _pp, _vp, _vp, _vp, _vp],
     "ccl_deposit_postproc": [_i, _i, _i, _pp, _i, _i, _vp, _vp],
     "ccl_warp_axis": [_i, _i, _i, _pp, _i, _vp],
     "ccl_gather_push": [_i, _i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d,
                         _i, _d, _d, _i, _d, _d, _pp, _vp],
     "ccl_gather_push_cells": [_i, _i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                               _d, _i, _d, _d, _i, _d, _d, _pp, _vp],
+    "ccl_gather_push_cells_lo": [_i, _i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                 _d, _i, _d, _d, _i, _d, _d, _pp, _vp, _vp, _vp, _vp],
     "ccl_phase": [_i, _i, _vp, _vp, _d, _i, _vp],
     "ccl_fft_forward_rows": [_i, _i, _i, _vp, _l, _i, _vp, _vp, _vp, _vp],
     "ccl_fft_backward_rows": [_i, _i, _i, _vp, _vp, _l, _i, _vp, _vp],

@@ -195,6 +195,47 @@ int ccl_deposit_vector(int dtype, int M, const uint32_t *sort_indx,
                                  rmin, dr_inv, J, S(stream)));
 }
 
+#define LO_CHECK()                                                              \
+  CCL_REQUIRE(dtype == CCL_F32, CCL_ERR_UNSUPPORTED,                             \
+              "%s: low coordinate parts are for FP32 particles", __func__);      \
+  NONNULL(x_lo); NONNULL(y_lo); NONNULL(z_lo)
+
+int ccl_deposit_scalar_lo(int dtype, int M, const uint32_t *sort_indx,
+                          const uint32_t *cell_offset, const void *x, const void *y,
+                          const void *z, const void *w, int charge, int Nx, double xmin,
+                          double dx_inv, int Nr, double rmin, double dr_inv, void *const *rho,
+                          const void *x_lo, const void *y_lo, const void *z_lo, void *stream) {
+  DTYPE_CHECK(dtype);
+  LO_CHECK();
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "%s: M=%d", __func__, M);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  NONNULL(sort_indx); NONNULL(cell_offset); NONNULL(x); NONNULL(y); NONNULL(z);
+  NONNULL(w); NONNULL(rho);
+  const void *lo[3] = {x_lo, y_lo, z_lo};
+  return DISPATCH(dtype, deposit(0, M, sort_indx, cell_offset, x, y, z, nullptr, nullptr,
+                                 nullptr, nullptr, w, charge, Nx, xmin, dx_inv, Nr, rmin,
+                                 dr_inv, rho, S(stream), lo));
+}
+
+int ccl_deposit_vector_lo(int dtype, int M, const uint32_t *sort_indx,
+                          const uint32_t *cell_offset, const void *x, const void *y,
+                          const void *z, const void *ux, const void *uy, const void *uz,
+                          const void *g_inv, const void *w, int charge, int Nx, double xmin,
+                          double dx_inv, int Nr, double rmin, double dr_inv, void *const *J,
+                          const void *x_lo, const void *y_lo, const void *z_lo, void *stream) {
+  DTYPE_CHECK(dtype);
+  LO_CHECK();
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "%s: M=%d", __func__, M);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  NONNULL(sort_indx); NONNULL(cell_offset); NONNULL(x); NONNULL(y); NONNULL(z);
+  NONNULL(ux); NONNULL(uy); NONNULL(uz); NONNULL(g_inv); NONNULL(w); NONNULL(J);
+  const void *lo[3] = {x_lo, y_lo, z_lo};
+  return DISPATCH(dtype, deposit(1, M, sort_indx, cell_offset, x, y, z, ux, uy, uz, g_inv, w,
+                                 charge, Nx, xmin, dx_inv, Nr, rmin, dr_inv, J, S(stream), lo));
+}
+
 int ccl_deposit_postproc(int dtype, int M, int nfld, void *const *flds,
                          int Nx, int Nr, const void *dV_inv, void *stream) {
   DTYPE_CHECK(dtype);
@@ -251,6 +292,29 @@ int ccl_gather_push_cells(int dtype, int M, long np, const void *x, const void *
   return DISPATCH(dtype, gather_push_cells(M, np, x, y, z, px, py, pz, g_inv, sort_indx,
                                            cell_offset, np_stay, factor_push, Nx, xmin,
                                            dx_inv, Nr, rmin, dr_inv, flds, S(stream)));
+}
+
+int ccl_gather_push_cells_lo(int dtype, int M, long np, const void *x, const void *y,
+                             const void *z, void *px, void *py, void *pz, void *g_inv,
+                             const uint32_t *sort_indx, const uint32_t *cell_offset,
+                             const uint32_t *np_stay, double factor_push, int Nx, double xmin,
+                             double dx_inv, int Nr, double rmin, double dr_inv,
+                             const void *const *flds, const void *x_lo, const void *y_lo,
+                             const void *z_lo, void *stream) {
+  DTYPE_CHECK(dtype);
+  CCL_REQUIRE(M >= 0 && M < kMaxModes, CCL_ERR_UNSUPPORTED, "%s: M=%d", __func__, M);
+  NONNEG(np);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  if (np == 0) return CCL_OK;
+  LO_CHECK();
+  NONNULL(x); NONNULL(y); NONNULL(z); NONNULL(px); NONNULL(py); NONNULL(pz);
+  NONNULL(g_inv); NONNULL(sort_indx); NONNULL(cell_offset); NONNULL(np_stay);
+  NONNULL(flds);
+  const void *lo[3] = {x_lo, y_lo, z_lo};
+  return DISPATCH(dtype, gather_push_cells(M, np, x, y, z, px, py, pz, g_inv, sort_indx,
+                                           cell_offset, np_stay, factor_push, Nx, xmin,
+                                           dx_inv, Nr, rmin, dr_inv, flds, S(stream), lo));
 }
 
 // ----------------------------------------------------------------- spectral

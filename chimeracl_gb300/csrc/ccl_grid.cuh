@@ -87,12 +87,15 @@ __device__ __forceinline__ void dep_particle(T (&s)[4][(VEC ? 3 : 1) * (1 + 2 * 
 
 // FP32 form (the mixed-precision step; no bit-exact counterpart): the same
 // corner sums with 1/r from rsqrt and the per-particle moments (1, e^{im phi}
-// per component) formed once, then one FMA per (corner, moment).
-template <int M, bool VEC>
+// per component) formed once, then one FMA per (corner, moment).  LO: the
+// coordinates are hi + lo (compensated), and the shape fractions take the
+// low parts in.
+template <int M, bool VEC, bool LO = false>
 __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (1 + 2 * M)],
                                              float xp, float yp, float zp, float wraw, float ux,
                                              float uy, float uz, float gi, float q,
-                                             const GridP<float> &g, CellEdge ex, CellEdge er) {
+                                             const GridP<float> &g, CellEdge ex, CellEdge er,
+                                             float xl = 0.f, float yl = 0.f, float zl = 0.f) {
   constexpr int NK = VEC ? 3 : 1, B = 1 + 2 * M;
   const float wp = VEC ? wraw * gi * q : wraw * q;
   const float r2 = yp * yp + zp * zp;
@@ -110,8 +113,17 @@ __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (
     e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
     e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
   }
-  const float sX1 = edge_frac(xp, ex, g.dx_inv), sX0 = 1.f - sX1;
-  const float sR1 = edge_frac(rp, er, g.dr_inv), sR0 = 1.f - sR1;
+  float sX1, sR1;
+  if constexpr (LO) {
+    float rr, rrl;
+    radius_pair(yp, zp, yl, zl, rinv, rr, rrl);
+    sX1 = edge_frac_lo(xp, xl, ex, g.dx_inv);
+    sR1 = edge_frac_lo(rr, rrl, er, g.dr_inv);
+  } else {
+    sX1 = edge_frac(xp, ex, g.dx_inv);
+    sR1 = edge_frac(rp, er, g.dr_inv);
+  }
+  const float sX0 = 1.f - sX1, sR0 = 1.f - sR1;
   const float wX0 = sX0 * wp, wX1 = sX1 * wp;
   const float C[4] = {sR0 * wX0, sR0 * wX1, sR1 * wX0, sR1 * wX1};
   const float jp[3] = {VEC ? ux : 1.f, uy, uz};
@@ -133,14 +145,16 @@ __device__ __forceinline__ void dep_particle_f32(float (&s)[4][(VEC ? 3 : 1) * (
 
 // Field pointer bundle: for a scalar deposit f[m] (m = 0..M); for a vector
 // deposit f[3m + k].  Mode 0 is real, modes >= 1 complex.
-template <typename T, int M, bool VEC>
+template <typename T, int M, bool VEC, bool LO = false>
 __global__ void __launch_bounds__(DEP_THREADS)
     k_deposit(const u32 *__restrict__ sort_indx,
               const u32 *__restrict__ cell_off, const T *__restrict__ x,
               const T *__restrict__ y, const T *__restrict__ z,
               const T *__restrict__ ux, const T *__restrict__ uy,
               const T *__restrict__ uz, const T *__restrict__ g_inv,
-              const T *__restrict__ w, T q, GridP<T> g, ptrs<12> f) {
+              const T *__restrict__ w, T q, GridP<T> g, ptrs<12> f,
+              const T *__restrict__ xl = nullptr, const T *__restrict__ yl = nullptr,
+              const T *__restrict__ zl = nullptr) {
   constexpr int NK = VEC ? 3 : 1;       // vector components
   constexpr int NQ = NK * (1 + 2 * M);  // reals per node
   __shared__ T acc[NQ][DEP_NTR][DEP_NTX];
@@ -190,7 +204,10 @@ __global__ void __launch_bounds__(DEP_THREADS)
       const u32 p = sort_indx[ip];
       const T a = VEC ? ux[p] : T(0), b = VEC ? uy[p] : T(0), c = VEC ? uz[p] : T(0),
               d = VEC ? g_inv[p] : T(0);
-      if constexpr (sizeof(T) == 4)
+      if constexpr (sizeof(T) == 4 && LO)
+        dep_particle_f32<M, VEC, true>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, ex, er,
+                                       xl[p], yl[p], zl[p]);
+      else if constexpr (sizeof(T) == 4)
         dep_particle_f32<M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, ex, er);
       else
         dep_particle<T, M, VEC>(s, x[p], y[p], z[p], w[p], a, b, c, d, q, g, fix, fir);
@@ -234,11 +251,31 @@ __global__ void __launch_bounds__(DEP_THREADS)
   }
 }
 
+template <typename T, int M, bool VEC, bool LO>
+void deposit_launch(dim3 grid, const u32 *sort_indx, const u32 *cell_off, const T *x,
+                    const T *y, const T *z, const T *ux, const T *uy, const T *uz,
+                    const T *g_inv, const T *w, T q, GridP<T> g, ptrs<12> f,
+                    const T *const *lo, cudaStream_t s) {
+  // the per-lane particle streams are re-read from L1 across a cell's
+  // particles: ask for the smallest shared-memory carve-out (largest L1)
+  static bool set = false;  // per instantiation, once
+  if (!set) {
+    cudaFuncSetAttribute(k_deposit<T, M, VEC, LO>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, DEP_CARVEOUT);
+    set = true;
+  }
+  k_deposit<T, M, VEC, LO><<<grid, DEP_THREADS, 0, s>>>(
+      sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w, q, g, f, LO ? lo[0] : nullptr,
+      LO ? lo[1] : nullptr, LO ? lo[2] : nullptr);
+}
+
+// lo: nullptr, or the low parts {x_lo, y_lo, z_lo} of compensated FP32
+// coordinates
 template <typename T, int M, bool VEC>
 int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
               const T *y, const T *z, const T *ux, const T *uy, const T *uz,
               const T *g_inv, const T *w, int charge, GridP<T> g,
-              void *const *flds, cudaStream_t s) {
+              void *const *flds, cudaStream_t s, const T *const *lo = nullptr) {
   ptrs<12> f;
   const int nptr = (VEC ? 3 : 1) * (M + 1);
   for (int i = 0; i < nptr; i++) {
@@ -248,18 +285,16 @@ int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
   dim3 grid((g.Nx + DEP_NTX - 1) / DEP_NTX, (g.Nr + DEP_NTR - 1) / DEP_NTR);
   // the reference passes the charge as a signed char (grid_methods_cl.py:259)
   T q = (T)(signed char)charge;
-  {
-    // the per-lane particle streams are re-read from L1 across a cell's
-    // particles: ask for the smallest shared-memory carve-out (largest L1)
-    static bool set = false;  // per instantiation, once
-    if (!set) {
-      cudaFuncSetAttribute(k_deposit<T, M, VEC>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           DEP_CARVEOUT);
-      set = true;
+  if constexpr (sizeof(T) == 4) {
+    if (lo) {
+      deposit_launch<T, M, VEC, true>(grid, sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w,
+                                      q, g, f, lo, s);
+      CCL_LAUNCH_CHECK("deposit");
+      return CCL_OK;
     }
   }
-  k_deposit<T, M, VEC><<<grid, DEP_THREADS, 0, s>>>(sort_indx, cell_off, x, y, z, ux, uy, uz,
-                                                    g_inv, w, q, g, f);
+  deposit_launch<T, M, VEC, false>(grid, sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w, q,
+                                   g, f, lo, s);
   CCL_LAUNCH_CHECK("deposit");
   return CCL_OK;
 }
@@ -268,20 +303,20 @@ template <typename T, bool VEC>
 int deposit(int M, const u32 *sort_indx, const u32 *cell_off, const T *x,
             const T *y, const T *z, const T *ux, const T *uy, const T *uz,
             const T *g_inv, const T *w, int charge, GridP<T> g,
-            void *const *flds, cudaStream_t s) {
+            void *const *flds, cudaStream_t s, const T *const *lo = nullptr) {
   switch (M) {
     case 0:
       return deposit_m<T, 0, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
-                                  g_inv, w, charge, g, flds, s);
+                                  g_inv, w, charge, g, flds, s, lo);
     case 1:
       return deposit_m<T, 1, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
-                                  g_inv, w, charge, g, flds, s);
+                                  g_inv, w, charge, g, flds, s, lo);
     case 2:
       return deposit_m<T, 2, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
-                                  g_inv, w, charge, g, flds, s);
+                                  g_inv, w, charge, g, flds, s, lo);
     case 3:
       return deposit_m<T, 3, VEC>(sort_indx, cell_off, x, y, z, ux, uy, uz,
-                                  g_inv, w, charge, g, flds, s);
+                                  g_inv, w, charge, g, flds, s, lo);
   }
   set_error("deposit: M=%d not supported (0..3)", M);
   return CCL_ERR_UNSUPPORTED;
@@ -529,14 +564,19 @@ __host__ __device__ constexpr int gt_stride(int M) {  // floats per staged node,
   return ((6 * (1 + 2 * M)) + 3) & ~3;
 }
 
-template <int M>
+// LO: coordinates held as hi + lo (compensated); the shape fractions take
+// the low parts in (xl, yl, zl), the cell and angle come from hi.
+template <int M, bool LO = false>
 __global__ void __launch_bounds__(GT_THREADS)
     k_gather_push_tiled(const float *__restrict__ x, const float *__restrict__ y,
                         const float *__restrict__ z, float *__restrict__ px,
                         float *__restrict__ py, float *__restrict__ pz,
                         float *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
                         const u32 *__restrict__ cell_off, const u32 *__restrict__ np_stay_p,
-                        float dt, GridP<float> g, ptrs<24> f) {
+                        float dt, GridP<float> g, ptrs<24> f,
+                        const float *__restrict__ xl = nullptr,
+                        const float *__restrict__ yl = nullptr,
+                        const float *__restrict__ zl = nullptr) {
   constexpr int NS = gt_stride(M);
   extern __shared__ __align__(16) float gsm[];  // [GT_NR][GT_NX][NS]
   __shared__ u32 row_a[GT_TR], row_pre[GT_TR + 1];
@@ -599,8 +639,27 @@ __global__ void __launch_bounds__(GT_THREADS)
     const float fx = (xp - g.xmin) * g.dx_inv;
     int ix = (int)floorf(fx);
     ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
-    const float sX1 = edge_frac(xp, xedge[ix - nx0], g.dx_inv), sX0 = 1.f - sX1;
-    const float sR1 = edge_frac(rp, redge[r], g.dr_inv), sR0 = 1.f - sR1;
+    float sX1, sR1;
+    if constexpr (LO) {
+      float rr, rrl;
+      radius_pair(yp, zp, yl[p], zl[p], rinv, rr, rrl);
+      const float xlp = xl[p];
+      sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+      // the index from hi can be one off within an FP32 spacing of a face:
+      // the cell of the full coordinate (within the tile's cells)
+      if (sX1 < 0.f && ix > ixl) {
+        ix--;
+        sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+      } else if (sX1 >= 1.f && ix < ixh) {
+        ix++;
+        sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+      }
+      sR1 = edge_frac_lo(rr, rrl, redge[r], g.dr_inv);
+    } else {
+      sX1 = edge_frac(xp, xedge[ix - nx0], g.dx_inv);
+      sR1 = edge_frac(rp, redge[r], g.dr_inv);
+    }
+    const float sX0 = 1.f - sX1, sR0 = 1.f - sR1;
     const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
     const int l0 = (r * GT_NX + (ix - nx0)) * NS;
     const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};
@@ -706,10 +765,13 @@ int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
   return CCL_OK;
 }
 
+// lo: nullptr, or the low parts {x_lo, y_lo, z_lo} of compensated FP32
+// coordinates
 template <typename T>
 int gather_push_cells(int M, long np, const T *x, const T *y, const T *z, T *px, T *py, T *pz,
                       T *g_inv, const u32 *sort_indx, const u32 *cell_off, const u32 *np_stay,
-                      double factor_push, GridP<T> g, const void *const *flds, cudaStream_t s) {
+                      double factor_push, GridP<T> g, const void *const *flds, cudaStream_t s,
+                      const T *const *lo = nullptr) {
   if constexpr (sizeof(T) == 8) {
     (void)cell_off;
     return gather_push<T>(M, np, x, y, z, px, py, pz, g_inv, sort_indx, np_stay, factor_push, g,
@@ -727,14 +789,15 @@ int gather_push_cells(int M, long np, const T *x, const T *y, const T *z, T *px,
 #define CCL_GT(MM)                                                                         \
   {                                                                                        \
     const size_t smem = (size_t)GT_NR * GT_NX * gt_stride(MM) * sizeof(float);            \
-    auto kern = k_gather_push_tiled<MM>;                                                   \
-    static bool set = false; /* once per instantiation */                                  \
-    if (!set) {                                                                            \
+    auto kern = lo ? k_gather_push_tiled<MM, true> : k_gather_push_tiled<MM, false>;     \
+    static bool set[2] = {false, false}; /* once per instantiation */                     \
+    if (!set[lo != nullptr]) {                                                             \
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
-      set = true;                                                                          \
+      set[lo != nullptr] = true;                                                           \
     }                                                                                      \
     kern<<<grid, GT_THREADS, smem, s>>>(x, y, z, px, py, pz, g_inv, sort_indx, cell_off,    \
-                                        np_stay, dt, g, f);                                \
+                                        np_stay, dt, g, f, lo ? lo[0] : nullptr,           \
+                                        lo ? lo[1] : nullptr, lo ? lo[2] : nullptr);       \
   }
     switch (M) {
       case 0: CCL_GT(0); break;

@@ -77,7 +77,7 @@ template <typename T> struct Ops {
                      const void *uz, const void *g_inv, const void *w,
                      int charge, int Nx, double xmin, double dx_inv, int Nr,
                      double rmin, double dr_inv, void *const *flds,
-                     cudaStream_t s);
+                     cudaStream_t s, const void *const *lo = nullptr);
   static int postproc(int M, int nfld, void *const *flds, int Nx, int Nr,
                       const void *dv, cudaStream_t s);
   static int warp_axis(int M, int nfld, void *const *flds, int Nx,
@@ -95,7 +95,8 @@ template <typename T> struct Ops {
                                const uint32_t *cell_offset, const uint32_t *np_stay,
                                double factor_push, int Nx, double xmin,
                                double dx_inv, int Nr, double rmin, double dr_inv,
-                               const void *const *flds, cudaStream_t s);
+                               const void *const *flds, cudaStream_t s,
+                               const void *const *lo = nullptr);
   static int psatd(long n, double dt_inv, const void *c1, const void *c2,
                    const void *c3, void *const *flds, cudaStream_t s);
   static int psatd_split(long n, const void *coef, void *const *flds, cudaStream_t s);

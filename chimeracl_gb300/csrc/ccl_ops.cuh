@@ -88,18 +88,19 @@ int Ops<T>::deposit(int vec, int M, const uint32_t *sort_indx,
                     const void *uz, const void *g_inv, const void *w,
                     int charge, int Nx, double xmin, double dx_inv, int Nr,
                     double rmin, double dr_inv, void *const *flds,
-                    cudaStream_t s) {
+                    cudaStream_t s, const void *const *lo) {
   const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
+  const T *const *lt = (const T *const *)lo;
   if (vec)
     return ccl::deposit<T, true>(M, sort_indx, cell_off, (const T *)x,
                                  (const T *)y, (const T *)z, (const T *)ux,
                                  (const T *)uy, (const T *)uz,
                                  (const T *)g_inv, (const T *)w, charge, g,
-                                 flds, s);
+                                 flds, s, lt);
   return ccl::deposit<T, false>(M, sort_indx, cell_off, (const T *)x,
                                 (const T *)y, (const T *)z, nullptr, nullptr,
                                 nullptr, nullptr, (const T *)w, charge, g,
-                                flds, s);
+                                flds, s, lt);
 }
 
 template <typename T>
@@ -156,11 +157,13 @@ int Ops<T>::gather_push_cells(int M, long np, const void *x, const void *y,
                               const uint32_t *cell_offset, const uint32_t *np_stay,
                               double factor_push, int Nx, double xmin,
                               double dx_inv, int Nr, double rmin, double dr_inv,
-                              const void *const *flds, cudaStream_t s) {
+                              const void *const *flds, cudaStream_t s,
+                              const void *const *lo) {
   const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
   return ccl::gather_push_cells<T>(M, np, (const T *)x, (const T *)y, (const T *)z,
                                    (T *)px, (T *)py, (T *)pz, (T *)g_inv, sort_indx,
-                                   cell_offset, np_stay, factor_push, g, flds, s);
+                                   cell_offset, np_stay, factor_push, g, flds, s,
+                                   (const T *const *)lo);
 }
 
 template <typename T>

@@ -212,6 +212,30 @@ __device__ __forceinline__ float radius_from_rsqrt(float r2, float rinv) {
   const float r = r2 * rinv;
   return fmaf(fmaf(-r, r, r2), 0.5f * rinv, r);
 }
+// Coordinates held as hi + lo (compensated): the in-cell fraction of v + vl
+// from the edge pair, (v - e.hi) exact, the low parts added after it.
+__device__ __forceinline__ float edge_frac_lo(float v, float vl, CellEdge e, float h_inv) {
+  return __fmul_rn(__fadd_rn(__fsub_rn(v, e.hi), __fsub_rn(vl, e.lo)), h_inv);
+}
+// |(y + yl, z + zl)| as r + rl: y^2 + z^2 with its rounding errors kept
+// (two-products by fma, a two-sum), the low parts to first order, then the
+// Newton residual of r (exact by fma) carried into rl.  rinv ~ 1/r.
+__device__ __forceinline__ void radius_pair(float y, float z, float yl, float zl, float rinv,
+                                            float &r, float &rl) {
+  const float p1 = __fmul_rn(y, y), p2 = __fmul_rn(z, z);
+  const float e1 = __fmaf_rn(y, y, -p1), e2 = __fmaf_rn(z, z, -p2);
+  const float s = __fadd_rn(p1, p2);
+  const float bp = __fsub_rn(s, p1);
+  const float es = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, bp)), __fsub_rn(p2, bp));
+  if (!(s > 0.f)) {
+    r = 0.f;
+    rl = 0.f;
+    return;
+  }
+  const float slo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(es, 2.f * (y * yl + z * zl)));
+  r = radius_from_rsqrt(s, rinv);
+  rl = __fmul_rn(__fadd_rn(__fmaf_rn(-r, r, s), slo), 0.5f * rinv);
+}
 __device__ __forceinline__ float frac_x(float xp, int ix, const GridP<float> &g) {
   return edge_frac(xp, x_edge(g, ix), g.dx_inv);
 }

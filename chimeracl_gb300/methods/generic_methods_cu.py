@@ -75,12 +75,15 @@ class Communicator:
     precision.  ``precision='mixed'`` is FP32 with the radial Hankel and
     derivative GEMMs as BF16x3 split-precision products on the tensor cores
     (FP32 accumulation).  ``seed`` seeds the host generator of the plasma injector's
-    random draws.  ``compensated_positions=True`` holds each coordinate of a
-    mobile species as the sum of its value and a low part of the same type
-    (``x_lo``, ``y_lo``, ``z_lo`` in ``DataDev``), so that FP32 coordinates
-    keep displacements below their last place over long runs; the sort,
-    deposits and gather read the coordinate itself.  It costs 24 bytes per
-    particle per push and is off by default.  Keyword arguments of the reference's OpenCL context choice
+    random draws.  ``compensated_positions=True`` (FP32 forms) holds each
+    coordinate as the sum of its FP32 value and an FP32 low part (``x_lo``,
+    ``y_lo``, ``z_lo`` in ``DataDev``): the injector stores the rounding
+    residual of its double-precision positions there, the push adds its
+    displacements by a two-sum, and the deposits and gather take the shape
+    fractions from the full coordinate (a 2^-24 fraction of a cell wherever
+    the particle is); the cell sort reads the FP32 value.  It costs 12 bytes
+    per particle in each deposit and the gather and 24 per push, and is off
+    by default.  The FP64 form ignores it.  Keyword arguments of the reference's OpenCL context choice
     (``answers``, ``interactive``) are accepted and ignored."""
 
     def __init__(self, precision="fp64", device=0, seed=0, verbose=False,
@@ -106,7 +109,7 @@ class Communicator:
         self.cplx = torch.complex128 if precision == "fp64" else torch.complex64
         self.ccl = CCL_F64 if precision == "fp64" else CCL_F32
         self.dht_impl = "bf16x3" if precision == "mixed" else "simt"
-        self.compensated = bool(compensated_positions)
+        self.compensated = bool(compensated_positions) and precision != "fp64"
         # host<->device traffic issued by the methods (injector draws,
         # profile knots, lazy scalar reads), for end-to-end accounting
         self.h2d_bytes = 0

@@ -36,10 +36,17 @@ class GridMethodsCU(GenericMethodsCU):
             return
         D, M = parts.DataDev, self.Args["M"]
         flds = [self.DataDev[dest_fld + "_m" + str(m)] for m in range(M + 1)]
-        call("ccl_deposit_scalar", self._dt, M, D["sort_indx"].data_ptr(),
-             D["cell_offset"].data_ptr(), D["x"].data_ptr(), D["y"].data_ptr(),
-             D["z"].data_ptr(), D[src_scalar].data_ptr(), int(np.int8(charge)),
-             *self._grid_scalars(), PP(flds), stream())
+        args = [self._dt, M, D["sort_indx"].data_ptr(), D["cell_offset"].data_ptr(),
+                D["x"].data_ptr(), D["y"].data_ptr(), D["z"].data_ptr(),
+                D[src_scalar].data_ptr(), int(np.int8(charge)), *self._grid_scalars(), PP(flds)]
+        if "x_lo" in D:  # compensated coordinates: fractions from hi + lo
+            call("ccl_deposit_scalar_lo", *args, *self._low_parts(D), stream())
+        else:
+            call("ccl_deposit_scalar", *args, stream())
+
+    @staticmethod
+    def _low_parts(D):
+        return [D[k].data_ptr() for k in ("x_lo", "y_lo", "z_lo")]
 
     def depose_vector(self, parts, vec, factors, vec_fld, charge):
         """grid_methods_cl.py:266-290; factors = [g_inv, w]."""
@@ -48,11 +55,14 @@ class GridMethodsCU(GenericMethodsCU):
         D, M = parts.DataDev, self.Args["M"]
         flds = [self.DataDev[vec_fld + c + "_m" + str(m)]
                 for m in range(M + 1) for c in self.Args["vec_comps"]]
-        call("ccl_deposit_vector", self._dt, M, D["sort_indx"].data_ptr(),
-             D["cell_offset"].data_ptr(), D["x"].data_ptr(), D["y"].data_ptr(),
-             D["z"].data_ptr(), D[vec[0]].data_ptr(), D[vec[1]].data_ptr(),
-             D[vec[2]].data_ptr(), D[factors[0]].data_ptr(), D[factors[1]].data_ptr(),
-             int(np.int8(charge)), *self._grid_scalars(), PP(flds), stream())
+        args = [self._dt, M, D["sort_indx"].data_ptr(), D["cell_offset"].data_ptr(),
+                D["x"].data_ptr(), D["y"].data_ptr(), D["z"].data_ptr(), D[vec[0]].data_ptr(),
+                D[vec[1]].data_ptr(), D[vec[2]].data_ptr(), D[factors[0]].data_ptr(),
+                D[factors[1]].data_ptr(), int(np.int8(charge)), *self._grid_scalars(), PP(flds)]
+        if "x_lo" in D:
+            call("ccl_deposit_vector_lo", *args, *self._low_parts(D), stream())
+        else:
+            call("ccl_deposit_vector", *args, stream())
 
     def _postproc(self, names):
         M = self.Args["M"]
@@ -83,8 +93,12 @@ class GridMethodsCU(GenericMethodsCU):
         f = [self.DataDev[fl + c + "_m" + str(m)]
              for m in range(M + 1) for fl in flds for c in self.Args["vec_comps"]]
         # with the sort's cell offsets (the FP32 form runs tile by tile)
-        call("ccl_gather_push_cells", self._dt, M, parts.Args["Np"], D["x"].data_ptr(),
-             D["y"].data_ptr(), D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(),
-             D["pz"].data_ptr(), D["g_inv"].data_ptr(), D["sort_indx"].data_ptr(),
-             D["cell_offset"].data_ptr(), D["Np_stay_dev"].data_ptr(),
-             float(parts.Args["FactorPush"]), *self._grid_scalars(), PP(f), stream())
+        args = [self._dt, M, parts.Args["Np"], D["x"].data_ptr(), D["y"].data_ptr(),
+                D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(), D["pz"].data_ptr(),
+                D["g_inv"].data_ptr(), D["sort_indx"].data_ptr(), D["cell_offset"].data_ptr(),
+                D["Np_stay_dev"].data_ptr(), float(parts.Args["FactorPush"]),
+                *self._grid_scalars(), PP(f)]
+        if "x_lo" in D:
+            call("ccl_gather_push_cells_lo", *args, *self._low_parts(D), stream())
+        else:
+            call("ccl_gather_push_cells", *args, stream())

@@ -4,7 +4,7 @@ align, plasma/beam injection."""
 import numpy as np
 import torch
 
-from .._lib import PP, call, sort_workspace_bytes, stream
+from .._lib import CCL_F64, PP, call, sort_workspace_bytes, stream
 from .generic_methods_cu import GenericMethodsCU, LazyScalar
 
 
@@ -21,15 +21,18 @@ class ParticleMethodsCU(GenericMethodsCU):
 
     def _comps(self):
         if "Immobile" in self.Args:
-            return ["x", "y", "z", "w"]
-        comps = ["x", "y", "z", "px", "py", "pz", "w", "g_inv"]
+            comps = ["x", "y", "z", "w"]
+        else:
+            comps = ["x", "y", "z", "px", "py", "pz", "w", "g_inv"]
         if self.comm.compensated:
+            # immobile species too: their charge must sit where the mobile
+            # species' charge sits (ions are injected on the electrons)
             comps += ["x_lo", "y_lo", "z_lo"]
         return comps
 
     def _new_low_parts(self, Np):
-        """Zero low parts of the coordinates of Np new particles (the
-        coordinates themselves are then exact)."""
+        """Zero low parts of the coordinates of Np new particles (filled in
+        by the injector where its positions are not FP32 values)."""
         if "x_lo" in self._comps():
             for arg in ("x_lo", "y_lo", "z_lo"):
                 self.DataDev[arg + "_new"] = torch.zeros(Np, dtype=self.comm.real,
@@ -62,9 +65,23 @@ class ParticleMethodsCU(GenericMethodsCU):
         self._fill_arr_rand(theta, xmin=0, xmax=2 * np.pi)
         Xg_d, Rg_d = self.dev_arr(val=Xg), self.dev_arr(val=Rg)
         npx, npr, npth = (int(v) for v in A["Nppc"])
-        call("ccl_fill_grid", self._dt, ncells, D["x_new"].data_ptr(), D["y_new"].data_ptr(),
-             D["z_new"].data_ptr(), D["w_new"].data_ptr(), theta.data_ptr(), Xg_d.data_ptr(),
-             Rg_d.data_ptr(), Nx_loc, npx, npr, npth, stream())
+        if "x_lo_new" in D:
+            # compensated FP32 coordinates: the positions in double (the FP64
+            # injector's values), split into FP32 value + FP32 residual
+            f64 = [torch.empty(Np, dtype=torch.float64, device=self.comm.device)
+                   for _ in range(4)]
+            call("ccl_fill_grid", CCL_F64, ncells, *[t.data_ptr() for t in f64],
+                 theta.data_ptr(), Xg_d.data_ptr(), Rg_d.data_ptr(), Nx_loc, npx, npr, npth,
+                 stream())
+            for arg, t in zip(("x", "y", "z"), f64):
+                D[arg + "_new"].copy_(t)
+                D[arg + "_lo_new"].copy_(t - D[arg + "_new"].to(torch.float64))
+            D["w_new"].copy_(f64[3])
+        else:
+            call("ccl_fill_grid", self._dt, ncells, D["x_new"].data_ptr(),
+                 D["y_new"].data_ptr(), D["z_new"].data_ptr(), D["w_new"].data_ptr(),
+                 theta.data_ptr(), Xg_d.data_ptr(), Rg_d.data_ptr(), Nx_loc, npx, npr, npth,
+                 stream())
         D["w_new"] *= A["w0"]
         if density_profiles is not None:
             for prf in density_profiles:
@@ -104,7 +121,10 @@ class ParticleMethodsCU(GenericMethodsCU):
             D[arg + "_new"] = torch.empty(Np, dtype=real, device=self.comm.device)
         self._new_low_parts(Np)
         for arg in ("x", "y", "z"):
-            self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"], sigma=parts_in["L" + arg])
+            v = self._fill_arr_randn(D[arg + "_new"], mu=parts_in[arg + "_c"],
+                                     sigma=parts_in["L" + arg])
+            if arg + "_lo_new" in D:  # the draws' FP32 rounding residual
+                self._upload(D[arg + "_lo_new"], v - v.astype(np.float32).astype(np.float64))
         for arg in ("px", "py", "pz"):
             parts_in.setdefault(arg + "_c", 0)
             parts_in.setdefault("d" + arg, 0)
@@ -210,6 +230,7 @@ class ParticleMethodsCU(GenericMethodsCU):
     def _fill_arr_randn(self, arr, mu=0, sigma=1):
         v = mu + sigma * self._rng.standard_normal(arr.numel())
         self._upload(arr, v)
+        return v
 
     def _fill_arr_rand(self, arr, xmin=0, xmax=1):
         v = xmin + (xmax - xmin) * self._rng.random(arr.numel())

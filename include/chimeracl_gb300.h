@@ -168,6 +168,25 @@ int ccl_deposit_vector(int dtype, int M, const uint32_t *sort_indx,
                        double dx_inv, int Nr, double rmin, double dr_inv,
                        void *const *J, void *stream);
 
+/* The two deposits for FP32 particles whose coordinates are held as
+ * hi + lo (x + x_lo, ...; see ccl_push_x_compensated): the cell and the
+ * angle come from x, y, z, the shape-function fractions from the full
+ * coordinates (the cell edge and the radius formed as float pairs), so they
+ * resolve a 2^-24 fraction of a cell however far the coordinate is from 0.
+ * No counterpart in the reference (its coordinates are FP64).  dtype must
+ * be CCL_F32. */
+int ccl_deposit_scalar_lo(int dtype, int M, const uint32_t *sort_indx,
+                          const uint32_t *cell_offset, const void *x, const void *y,
+                          const void *z, const void *w, int charge, int Nx, double xmin,
+                          double dx_inv, int Nr, double rmin, double dr_inv, void *const *rho,
+                          const void *x_lo, const void *y_lo, const void *z_lo, void *stream);
+int ccl_deposit_vector_lo(int dtype, int M, const uint32_t *sort_indx,
+                          const uint32_t *cell_offset, const void *x, const void *y,
+                          const void *z, const void *ux, const void *uy, const void *uz,
+                          const void *g_inv, const void *w, int charge, int Nx, double xmin,
+                          double dx_inv, int Nr, double rmin, double dr_inv, void *const *J,
+                          const void *x_lo, const void *y_lo, const void *z_lo, void *stream);
+
 /* Axis treatment (row 1 -= row 0) then multiplication by dV_inv[ir] for
  * nfld fields of M+1 modes (flds: nfld*(M+1) pointers, field-major).
  * Replaces postproc_depose_scalar / postproc_depose_vector
@@ -205,6 +224,17 @@ int ccl_gather_push_cells(int dtype, int M, long np, const void *x, const void *
                           const uint32_t *np_stay, double factor_push, int Nx,
                           double xmin, double dx_inv, int Nr, double rmin,
                           double dr_inv, const void *const *flds, void *stream);
+
+/* The same gather for FP32 coordinates held as hi + lo: interpolation
+ * fractions from the full coordinates, as in ccl_deposit_scalar_lo.  dtype
+ * must be CCL_F32. */
+int ccl_gather_push_cells_lo(int dtype, int M, long np, const void *x, const void *y,
+                             const void *z, void *px, void *py, void *pz, void *g_inv,
+                             const uint32_t *sort_indx, const uint32_t *cell_offset,
+                             const uint32_t *np_stay, double factor_push, int Nx, double xmin,
+                             double dx_inv, int Nr, double rmin, double dr_inv,
+                             const void *const *flds, const void *x_lo, const void *y_lo,
+                             const void *z_lo, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Spectral transforms  (chimeraCL/methods/transformer_methods_cl.py)  */

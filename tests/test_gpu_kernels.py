@@ -485,6 +485,111 @@ def test_gather_push_fp32(cuda, port, M, cells):
         assert err < 2e-5, (k, err)
 
 
+def _split(p):
+    """Coordinates as FP32 value + FP32 residual; the other components
+    rounded to FP32 (only coordinates carry low parts)."""
+    q = {k: to32(v) for k, v in p.items()}
+    lo = {k: to32(p[k] - to64(q[k])) for k in ("x", "y", "z")}
+    ref = {k: to64(q[k]) for k in p}
+    for k in ("x", "y", "z"):
+        ref[k] = p[k]  # the oracle takes the double coordinates
+    return q, lo, ref
+
+
+@pytest.mark.parametrize("M,vec", [(0, False), (1, False), (1, True)])
+def test_deposit_fp32_low_parts(cuda, port, M, vec):
+    """Compensated FP32 coordinates (hi + lo) at x ~ -1e4, where the FP32
+    spacing is 8e-3 of a cell: the _lo deposit against the FP64 oracle on the
+    double coordinates within 2e-5 of the deposited magnitude, the same
+    deposit from hi alone at least 10x further off."""
+    rng = np.random.default_rng(60 + M + 5 * vec)
+    g = geom(160, 40, Xmin=-10020.0, Xmax=-10000.0)
+    q, lo, p = _split(particles(rng, 60000, g, boundaries=False))
+    _, _, off, srt = oracle_sort(port, p, g)
+    names = ["J" + c for c in "xyz"] if vec else ["rho"]
+    f0 = {k: to64(to32(v)) for k, v in fields(rng, g["Nr"], g["Nx"], M, names).items()}
+    ref = {k: v.copy() for k, v in f0.items()}
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    nxnr4 = (g["Nr"]) // 2 * (g["Nx"]) // 2
+    geo = (g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"])
+    if vec:
+        port.depose_vector(M, nxnr4, srt, p["x"], p["y"], p["z"], p["px"], p["py"], p["pz"],
+                           p["g_inv"], p["w"], off, -1, *geo, [ref[k] for k in order])
+    else:
+        port.depose_scalar(M, nxnr4, srt, p["x"], p["y"], p["z"], p["w"], off, -1, *geo,
+                           [ref[k] for k in order])
+    pd = {k: dev(v) for k, v in q.items()}
+    ld = [dev(lo[k]).data_ptr() for k in ("x", "y", "z")]
+    errs = []
+    for use_lo in (True, False):
+        d = {k: dev(to32(v)) for k, v in f0.items()}
+        if vec:
+            args = [CCL_F32, M, dev(srt).data_ptr(), dev(off).data_ptr(), pd["x"].data_ptr(),
+                    pd["y"].data_ptr(), pd["z"].data_ptr(), pd["px"].data_ptr(),
+                    pd["py"].data_ptr(), pd["pz"].data_ptr(), pd["g_inv"].data_ptr(),
+                    pd["w"].data_ptr(), -1, *geo, PP([d[k] for k in order])]
+            name = "ccl_deposit_vector"
+        else:
+            args = [CCL_F32, M, dev(srt).data_ptr(), dev(off).data_ptr(), pd["x"].data_ptr(),
+                    pd["y"].data_ptr(), pd["z"].data_ptr(), pd["w"].data_ptr(), -1, *geo,
+                    PP([d[k] for k in order])]
+            name = "ccl_deposit_scalar"
+        if use_lo:
+            call(name + "_lo", *args, *ld, S())
+        else:
+            call(name, *args, S())
+        errs.append(max(np.abs(to64(host(d[k])) - ref[k]).max() / np.abs(ref[k] - f0[k]).max()
+                        for k in order))
+    assert errs[0] < 2e-5 and errs[1] > 10 * errs[0], errs
+
+
+@pytest.mark.parametrize("M", [0, 1])
+def test_gather_push_cells_fp32_low_parts(cuda, port, M):
+    """The tiled FP32 gather + push with compensated coordinates at x ~ -1e4:
+    momentum increments within 5e-5 of the FP64 oracle's on the double
+    coordinates, from hi alone at least 10x further off."""
+    rng = np.random.default_rng(70 + M)
+    g = geom(128, 32, Xmin=-10020.0, Xmax=-10000.0)
+    q, lo, p = _split(particles(rng, 50000, g, boundaries=False))
+    _, _, off, srt = oracle_sort(port, p, g)
+    np_stay = int(off[-2])
+    names = ["E" + c for c in "xyz"] + ["B" + c for c in "xyz"]
+    f = {k: to64(to32(v)) for k, v in fields(rng, g["Nr"], g["Nx"], M, names).items()}
+    order = [n + "_m" + str(m) for m in range(M + 1) for n in names]
+    ref = {k: p[k].copy() for k in ("px", "py", "pz", "g_inv")}
+    fp = 0.37
+    geo = (g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"])
+    port.gather_and_push(M, p["x"], p["y"], p["z"], ref["px"], ref["py"], ref["pz"], ref["g_inv"],
+                         srt, fp, p["x"].size, np_stay, *geo, [f[k] for k in order])
+    fd = [dev(to32(f[k])) for k in order]
+    nst = torch.tensor([np_stay], dtype=torch.int32, device="cuda")
+    ld = [dev(lo[k]).data_ptr() for k in ("x", "y", "z")]
+    errs = []
+    for use_lo in (True, False):
+        pd = {k: dev(v) for k, v in q.items()}
+        args = [CCL_F32, M, p["x"].size, pd["x"].data_ptr(), pd["y"].data_ptr(),
+                pd["z"].data_ptr(), pd["px"].data_ptr(), pd["py"].data_ptr(), pd["pz"].data_ptr(),
+                pd["g_inv"].data_ptr(), dev(srt).data_ptr(), dev(off).data_ptr(), nst.data_ptr(),
+                fp, *geo, PP(fd)]
+        if use_lo:
+            call("ccl_gather_push_cells_lo", *args, *ld, S())
+        else:
+            call("ccl_gather_push_cells", *args, S())
+        errs.append(max(np.abs(to64(host(pd[k])) - ref[k]).max() / np.abs(ref[k] - p[k]).max()
+                        for k in ("px", "py", "pz")))
+    assert errs[0] < 5e-5 and errs[1] > 10 * errs[0], errs
+
+
+def test_low_parts_rejected_for_fp64(cuda):
+    lib = _lib.load()
+    t = torch.zeros(64, dtype=torch.float64, device="cuda")
+    P = t.data_ptr()
+    arr = (C.c_void_p * 1)(P)
+    rc = lib.ccl_deposit_scalar_lo(CCL_F64, 0, P, P, P, P, P, P, -1, 16, 0.0, 1.0, 8, 0.0, 1.0,
+                                   arr, P, P, P, S())
+    assert rc != 0 and b"FP32" in lib.ccl_last_error()
+
+
 # ------------------------------------------------------------------- spectral
 def cplx(rng, *shape):
     return rng.normal(size=shape) + 1j * rng.normal(size=shape)
