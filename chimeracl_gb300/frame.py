@@ -52,9 +52,15 @@ class Frame:
             sp.align_parts()
             # right_lim = max x of the last Nppc+1 particles + ddx/2, kept on
             # the device until the next shift reads it (the value is the
-            # same double sum; the read no longer stalls this step)
+            # same double sum; the read no longer stalls this step).  With
+            # compensated coordinates x is x + x_lo: the next slab is then
+            # placed where the FP64 run places it (from a rounded x the whole
+            # slab would shift by that rounding)
             if sp.Args["Np"] > 0:
                 nppc = int(np.prod(sp.Args["Nppc"]) + 1)
-                x_max = sp.DataDev["x"][-nppc:].max().to(torch.float64)
+                x_tail = sp.DataDev["x"][-nppc:].to(torch.float64)
+                if "x_lo" in sp.DataDev:
+                    x_tail = x_tail + sp.DataDev["x_lo"][-nppc:].to(torch.float64)
+                x_max = x_tail.max()
                 dict.__setitem__(sp.Args, "right_lim",
                                  LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))

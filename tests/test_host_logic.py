@@ -100,3 +100,54 @@ def test_injector_draws_match_oracle():
     th_p = 0 + (2 * np.pi - 0) * rng_p.random(100)
     th_o = 0.0 + (2 * np.pi - 0.0) * rng_o.random(100)
     np.testing.assert_array_equal(th_p, th_o)
+
+
+class _FrameSpecies:
+    """Stub species for Frame.inject_plasma: records the injection domain."""
+
+    def __init__(self, x, x_lo=None):
+        import torch
+        self.Args = {"Np": len(x), "Nppc": np.array([2, 1, 4]), "ddx": 0.25, "right_lim": 0.0}
+        self.DataDev = {"x": torch.tensor(x, dtype=torch.float32)}
+        if x_lo is not None:
+            self.DataDev["x_lo"] = torch.tensor(x_lo, dtype=torch.float32)
+        self.comm = None
+        self.domains = []
+
+    def make_new_domain(self, dom, density_profiles=None):
+        self.domains.append(dict(dom))
+
+    def add_new_particles(self, source=None):
+        pass
+
+    def free_added(self):
+        pass
+
+    def sort_parts(self, grid):
+        pass
+
+    def align_parts(self):
+        pass
+
+
+@pytest.mark.parametrize("compensated", [False, True])
+def test_injector_right_limit(compensated):
+    """right_lim = max x of the last Nppc+1 particles + ddx/2 (frame.py:58-64),
+    read lazily at the next shift; with compensated coordinates from x + x_lo
+    in double."""
+    from chimeracl_gb300.frame import Frame
+    from chimeracl_gb300.methods.generic_methods_cu import ArgsDict
+    x = np.float32(np.linspace(-3.0, 7.3, 12))
+    lo = np.float32(np.spacing(x) * 0.25)
+    sp = _FrameSpecies(x, lo if compensated else None)
+    sp.Args = ArgsDict(sp.Args)
+    grid = _Stub()
+    grid.Args = {"Xmax": 8.0, "Rmin": 0.0, "Rmax": 4.0}
+    fr = Frame({"Steps": 2, "Velocity": 1.0, "dt": 0.5})
+    fr.inject_plasma([sp], grid)
+    want = float(x[-9:].astype(np.float64).max())
+    if compensated:
+        want = float((x[-9:].astype(np.float64) + lo[-9:].astype(np.float64)).max())
+    assert sp.Args["right_lim"] == want + 0.125
+    fr.inject_plasma([sp], grid)  # the next shift starts there
+    assert sp.domains[-1]["Xmin"] == want + 0.125
