@@ -610,7 +610,9 @@ def run_accuracy(args):
     workload (2x1x4 particles per cell: every radial position on a grid
     node) and with 2x2x4 per cell (none on a node): against the FP64 run on
     the same seed, and against the FP64 run on the same FP32-rounded
-    particles (the step error alone)."""
+    particles (the step error alone); and the mixed form with compensated
+    coordinates (FP64-exact injection, cell-relative fractions) against the
+    FP64 run on the same seed."""
     import torch
     out = {}
     for name, nppc in (("2x1x4", None), ("2x2x4", (2, 2, 4))):
@@ -618,10 +620,12 @@ def run_accuracy(args):
         if nppc:
             cfg["eons_in"]["Nppc"] = nppc
         runs = {}
-        for tag, prec, cls in (("fp64", "fp64", None),
-                               ("fp64_fp32_particles", "fp64", fp32_injected_particles()),
-                               ("mixed", "mixed", None)):
-            solver, eons, ions, loop = build_run(cfg, prec, particles_cls=cls)
+        for tag, prec, cls, kw in (
+                ("fp64", "fp64", None, {}),
+                ("fp64_fp32_particles", "fp64", fp32_injected_particles(), {}),
+                ("mixed", "mixed", None, {}),
+                ("mixed_compensated", "mixed", None, {"compensated_positions": True})):
+            solver, eons, ions, loop = build_run(cfg, prec, particles_cls=cls, **kw)
             for _ in range(args.acc_steps):
                 loop.step()
             torch.cuda.synchronize()
@@ -632,6 +636,8 @@ def run_accuracy(args):
                                                          runs["fp64_fp32_particles"]),
             "fp64_same_particles_vs_fp64": compare_runs(cfg, runs["fp64_fp32_particles"],
                                                         runs["fp64"]),
+            "mixed_compensated_vs_fp64": compare_runs(cfg, runs["mixed_compensated"],
+                                                      runs["fp64"]),
             "electrons": {k: int(r["eons"].Args["Np"]) for k, r in runs.items()}}
         del runs
         torch.cuda.empty_cache()
