@@ -58,9 +58,22 @@ class Frame:
             # slab would shift by that rounding)
             if sp.Args["Np"] > 0:
                 nppc = int(np.prod(sp.Args["Nppc"]) + 1)
-                x_tail = sp.DataDev["x"][-nppc:].to(torch.float64)
+                x = sp.DataDev["x"]
+                x_tail = x[-nppc:].to(torch.float64)
                 if "x_lo" in sp.DataDev:
                     x_tail = x_tail + sp.DataDev["x_lo"][-nppc:].to(torch.float64)
                 x_max = x_tail.max()
+                if x.dtype == torch.float32 and "x_lo" not in sp.DataDev and \
+                        "_inj_last_x" in sp.Args:
+                    # FP32 coordinates: the last particles are normally the
+                    # fresh slab's last column; where the maximum is that
+                    # column's FP32 value, take the double value it rounds
+                    # (an FP32 right limit would shift every later slab by
+                    # its rounding)
+                    c = float(sp.Args["_inj_last_x"])
+                    c64 = torch.full((), c, dtype=torch.float64, device=x.device)
+                    same = x[-nppc:].max() == torch.full((), float(np.float32(c)),
+                                                         dtype=torch.float32, device=x.device)
+                    x_max = torch.where(same, c64, x_max)
                 dict.__setitem__(sp.Args, "right_lim",
                                  LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))

@@ -55,6 +55,11 @@ class ParticleMethodsCU(GenericMethodsCU):
         Xg = xmin + A["dx"] * np.arange(Nx_loc)
         Rg = rmin + A["dr"] * np.arange(Nr_loc)
         A["right_lim"] = Xg[-1]
+        # x of the slab's last particle column, in the injector's double
+        # arithmetic (particles_generic.cl:62-74 order): what an FP32 store
+        # of that column rounds
+        npx = int(A["Nppc"][0])
+        A["_inj_last_x"] = float(Xg[-2] + (0.5 + (npx - 1)) * (1.0 / npx) * (Xg[-1] - Xg[-2]))
         ncells = (Nx_loc - 1) * (Nr_loc - 1)
         Np = int(ncells * np.prod(A["Nppc"]))
         real = self.comm.real

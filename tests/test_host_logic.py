@@ -151,3 +151,25 @@ def test_injector_right_limit(compensated):
     assert sp.Args["right_lim"] == want + 0.125
     fr.inject_plasma([sp], grid)  # the next shift starts there
     assert sp.domains[-1]["Xmin"] == want + 0.125
+
+
+def test_injector_right_limit_fp32_uses_the_lattice_value():
+    """FP32 coordinates: where the maximum of the last particles is the FP32
+    value of the slab's last column, right_lim is that column's double value
+    + ddx/2; otherwise (a particle moved past it) the FP32 maximum's."""
+    from chimeracl_gb300.frame import Frame
+    from chimeracl_gb300.methods.generic_methods_cu import ArgsDict
+    c = -0.1 + 7.0 / 3.0  # a lattice x that FP32 does not hold exactly
+    assert float(np.float32(c)) != c
+    grid = _Stub()
+    grid.Args = {"Xmax": 8.0, "Rmin": 0.0, "Rmax": 4.0}
+    for moved in (False, True):
+        x = np.float32(np.linspace(-3.0, 1.0, 12))
+        x[-1] = np.float32(c) if not moved else np.float32(c + 0.01)
+        sp = _FrameSpecies(x)
+        sp.Args = ArgsDict(sp.Args)
+        sp.Args["_inj_last_x"] = c
+        fr = Frame({"Steps": 2, "Velocity": 1.0, "dt": 0.5})
+        fr.inject_plasma([sp], grid)
+        want = c if not moved else float(np.float32(c + 0.01))
+        assert sp.Args["right_lim"] == want + 0.125, moved
