@@ -66,14 +66,15 @@ class Frame:
                 if x.dtype == torch.float32 and "x_lo" not in sp.DataDev and \
                         "_inj_last_x" in sp.Args:
                     # FP32 coordinates: the last particles are normally the
-                    # fresh slab's last column; where the maximum is that
-                    # column's FP32 value, take the double value it rounds
-                    # (an FP32 right limit would shift every later slab by
-                    # its rounding)
-                    c = float(sp.Args["_inj_last_x"])
-                    c64 = torch.full((), c, dtype=torch.float64, device=x.device)
-                    same = x[-nppc:].max() == torch.full((), float(np.float32(c)),
-                                                         dtype=torch.float32, device=x.device)
-                    x_max = torch.where(same, c64, x_max)
+                    # fresh slab's last columns; where the maximum is one of
+                    # those columns' FP32 value, take the double value it
+                    # rounds (an FP32 right limit would shift every later
+                    # slab by its rounding)
+                    xm32 = x[-nppc:].max()
+                    for c in reversed(sp.Args["_inj_last_x"]):  # the last column wins
+                        c64 = torch.full((), c, dtype=torch.float64, device=x.device)
+                        same = xm32 == torch.full((), float(np.float32(c)), dtype=torch.float32,
+                                                  device=x.device)
+                        x_max = torch.where(same, c64, x_max)
                 dict.__setitem__(sp.Args, "right_lim",
                                  LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))

@@ -55,11 +55,14 @@ class ParticleMethodsCU(GenericMethodsCU):
         Xg = xmin + A["dx"] * np.arange(Nx_loc)
         Rg = rmin + A["dr"] * np.arange(Nr_loc)
         A["right_lim"] = Xg[-1]
-        # x of the slab's last particle column, in the injector's double
-        # arithmetic (particles_generic.cl:62-74 order): what an FP32 store
-        # of that column rounds
+        # x of the slab's particle columns in its last two cells, last first,
+        # in the injector's double arithmetic (particles_generic.cl:62-74
+        # order): what an FP32 store of those columns rounds (the last cell
+        # can fall outside the window and be dropped)
         npx = int(A["Nppc"][0])
-        A["_inj_last_x"] = float(Xg[-2] + (0.5 + (npx - 1)) * (1.0 / npx) * (Xg[-1] - Xg[-2]))
+        A["_inj_last_x"] = [float(Xg[ix] + (0.5 + ixx) * (1.0 / npx) * (Xg[ix + 1] - Xg[ix]))
+                            for ix in (Nx_loc - 2, Nx_loc - 3) if ix >= 0
+                            for ixx in range(npx - 1, -1, -1)]
         ncells = (Nx_loc - 1) * (Nr_loc - 1)
         Np = int(ncells * np.prod(A["Nppc"]))
         real = self.comm.real

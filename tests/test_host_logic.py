@@ -161,15 +161,17 @@ def test_injector_right_limit_fp32_uses_the_lattice_value():
     from chimeracl_gb300.methods.generic_methods_cu import ArgsDict
     c = -0.1 + 7.0 / 3.0  # a lattice x that FP32 does not hold exactly
     assert float(np.float32(c)) != c
+    cols = [c, c - 0.125, c - 0.25, c - 0.375]  # last column first
     grid = _Stub()
     grid.Args = {"Xmax": 8.0, "Rmin": 0.0, "Rmax": 4.0}
-    for moved in (False, True):
+    for case in ("last", "dropped", "moved"):
         x = np.float32(np.linspace(-3.0, 1.0, 12))
-        x[-1] = np.float32(c) if not moved else np.float32(c + 0.01)
+        x[-1] = {"last": np.float32(c), "dropped": np.float32(cols[2]),
+                 "moved": np.float32(c + 0.01)}[case]
         sp = _FrameSpecies(x)
         sp.Args = ArgsDict(sp.Args)
-        sp.Args["_inj_last_x"] = c
+        sp.Args["_inj_last_x"] = cols
         fr = Frame({"Steps": 2, "Velocity": 1.0, "dt": 0.5})
         fr.inject_plasma([sp], grid)
-        want = c if not moved else float(np.float32(c + 0.01))
-        assert sp.Args["right_lim"] == want + 0.125, moved
+        want = {"last": c, "dropped": cols[2], "moved": float(np.float32(c + 0.01))}[case]
+        assert sp.Args["right_lim"] == want + 0.125, case
