@@ -70,11 +70,12 @@ class Frame:
                     # those columns' FP32 value, take the double value it
                     # rounds (an FP32 right limit would shift every later
                     # slab by its rounding)
-                    xm32 = x[-nppc:].max()
-                    for c in reversed(sp.Args["_inj_last_x"]):  # the last column wins
-                        c64 = torch.full((), c, dtype=torch.float64, device=x.device)
-                        same = xm32 == torch.full((), float(np.float32(c)), dtype=torch.float32,
-                                                  device=x.device)
-                        x_max = torch.where(same, c64, x_max)
+                    # (the candidates travel by one asynchronous pinned copy)
+                    cand = torch.tensor(sp.Args["_inj_last_x"], dtype=torch.float64)
+                    if x.is_cuda:
+                        cand = cand.pin_memory().to(x.device, non_blocking=True)
+                    same = x[-nppc:].max() == cand.to(torch.float32)
+                    first = torch.argmax(same.to(torch.int32))  # the last column wins
+                    x_max = torch.where(same.any(), cand[first], x_max)
                 dict.__setitem__(sp.Args, "right_lim",
                                  LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))
