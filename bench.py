@@ -588,6 +588,102 @@ def run_ours(args):
     return 0
 
 
+BATCHED_WORKLOAD = "lpa_batched_uneven_64"
+
+
+def batched_cases(n=64, seed=0):
+    """The batched small-run workload: n independent LPA runs with Nz drawn
+    from {256, 384, 512, 768, 1024} and Nr from {32, 64, 96, 128}, m = 0, 1,
+    1x1x4 macro-electrons per cell, n_e in [5e-4, 3e-3] n_c, laser a0 in
+    [1, 3] and w0 in [4, 10] lambda0 (tau = 5, centred and focused at
+    z = -10), on the 512 x 64 run's cells (dz = 40/512, dr = 20/64), moving
+    window with injection every 20 steps, absorbing edges of min(50, Nz/16)
+    cells (50 would reach the laser on the shortest windows); seeded."""
+    rng = np.random.default_rng(seed)
+    dx, dr = 40.0 / 512, 20.0 / 64
+    cases = []
+    for i in range(n):
+        nx = int(rng.choice([256, 384, 512, 768, 1024]))
+        nr = int(rng.choice([32, 64, 96, 128]))
+        dens, a0, w0 = (float(rng.uniform(*b)) for b in ((5e-4, 3e-3), (1.0, 3.0), (4.0, 10.0)))
+        win = dict(Xmin=-nx * dx, Xmax=0.0, Rmin=0.0, Rmax=nr * dr)
+        cases.append(dict(
+            grid_in=dict(win, Nx=nx, Nr=nr, M=1, DampCells=min(50, nx // 16)),
+            eons_in=dict(Nppc=(1, 1, 4), dens=dens, charge=-1),
+            frame_in=dict(Velocity=1.0, Steps=20),
+            laser_in=dict(k0=1.0, a0=a0, x0=-10.0, Lx=5.0 / (2 * np.sqrt(np.log(2))), R=w0,
+                          x_foc=-10.0),
+            prefill=dict(win), profiles=None, seed=seed * 1000 + i))
+    return cases
+
+
+def run_batched(args):
+    """Aggregate electron particle-steps/s of the batched workload through
+    PIC_batch (lane count picked by its autotuner during the warm-up),
+    beside the same runs stepped one by one on one stream."""
+    import torch
+    from chimeracl_gb300.batch import PIC_batch
+    from chimeracl_gb300 import _lib
+    cases = batched_cases(args.batch_runs, seed=args.batch_seed)
+    runs = [build_run(c, "mixed") for c in cases]
+    loops = [r[3] for r in runs]
+    b = PIC_batch(loops)
+    while b.lanes is None and b.it < 200:  # tuning, then the warm-up proper
+        b.step()
+    for _ in range(args.warmup):
+        b.step()
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        n0 = _lib.launch_count()
+        with ClockSampler(0) as clk:
+            time.sleep(0.3)
+            e0.record()
+            np_sum = fn()
+            e1.record()
+            torch.cuda.synchronize()
+        return np_sum, e0.elapsed_time(e1), _lib.launch_count() - n0, clk.summary()
+
+    def batched():
+        np_sum = 0
+        for _ in range(args.steps):
+            np_sum += b.electrons()
+            b.step()
+        return np_sum
+
+    def alone():
+        np_sum = 0
+        for lp in loops:
+            for _ in range(args.steps):
+                np_sum += int(lp.species[0].Args["Np"])
+                lp.step()
+        return np_sum
+
+    nb, msb, lb, clk = timed(batched)
+    n1, ms1, l1, _ = timed(alone)
+    line = {
+        "metric": "electron particle-steps/s (batched runs)", "value": nb / (msb * 1e-3),
+        "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": msb / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+bf16x3", "data": "synthetic (seeded plasma, lasers)",
+        "config": {"workload": BATCHED_WORKLOAD, "runs": len(runs),
+                   "grids": sorted({(c["grid_in"]["Nx"], c["grid_in"]["Nr"]) for c in cases}),
+                   "ppc": [1, 1, 4], "modes": 2, "frame_steps": 20,
+                   "l2": "working set larger than L2; no flush"},
+        "lanes": b.lanes,
+        "lane_tuning_ms": {str(c): round(1e3 * statistics.median(v), 3)
+                           for c, v in b.tune_log.items() if v},
+        "one_by_one": {"value": n1 / (ms1 * 1e-3), "ms_per_step": ms1 / args.steps},
+        "batched_over_one_by_one": (nb / msb) / (n1 / ms1),
+        "host_launch_calls": lb,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def fp32_injected_particles():
     """Particles (FP64) whose injector output -- coordinates and weights of
     every prefilled or injected particle -- is rounded through FP32: the
@@ -656,6 +752,10 @@ def main(argv=None):
     ap.add_argument("--accuracy", action="store_true",
                     help="run the mixed-vs-FP64 accuracy study instead of the benchmark")
     ap.add_argument("--acc-steps", type=int, default=608)
+    ap.add_argument("--workload", default="single", choices=["single", "batched"],
+                    help="batched: 64 small uneven runs through PIC_batch (1 GPU)")
+    ap.add_argument("--batch-runs", type=int, default=64)
+    ap.add_argument("--batch-seed", type=int, default=0)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
@@ -663,6 +763,8 @@ def main(argv=None):
         return run_reference(args)
     if args.accuracy:
         return run_accuracy(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

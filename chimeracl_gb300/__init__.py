@@ -27,6 +27,9 @@ def __getattr__(name):
     if name == "PIC_loop":
         from .pic_loop import PIC_loop
         return PIC_loop
+    if name == "PIC_batch":
+        from .batch import PIC_batch
+        return PIC_batch
     if name == "add_gausian_pulse":
         from .laser import add_gausian_pulse
         return add_gausian_pulse

@@ -1,0 +1,126 @@
+"""PIC_batch's scheduling on the CPU, with fakes for torch's stream objects
+and for the runs: every run stepped once per batch step on a stream of its
+own, the lane chaining (run i after run i - lanes), one lane while any run
+takes its first step, and the lane autotuner (the fastest candidate kept;
+window-shift and capturing steps left out of its timings)."""
+import contextlib
+
+import pytest
+import torch
+
+import chimeracl_gb300.batch as bm
+
+
+class FakeStream:
+    log = None
+    count = 0
+
+    def __init__(self, name=None):
+        FakeStream.count += 1
+        self.name = name if name is not None else "s%d" % (FakeStream.count - 1)
+
+    def wait_stream(self, other):
+        FakeStream.log.append(("wait", self.name, other.name))
+
+
+class FakeLoop:
+    def __init__(self, idx, log, steps=5, capture_at=()):
+        self.idx, self.log = idx, log
+        self.it = 0
+        self.graphs, self.timit, self.diags = True, False, []
+        self.graph_captures = 0
+        self.frame_steps = steps
+        self.capture_at = set(capture_at)
+        self.species = []
+
+    def _frame_due(self):
+        return self.it % self.frame_steps == 0
+
+    def step(self):
+        self.log.append(("step", self.idx, bm.torch.cuda.current_stream().name))
+        if self.it in self.capture_at:
+            self.graph_captures += 1
+        self.it += 1
+
+
+@pytest.fixture
+def fakes(monkeypatch):
+    log = []
+    FakeStream.log, FakeStream.count = log, 0
+    default = FakeStream("cur")
+    FakeStream.count = 0
+    state = {"cur": default}
+
+    @contextlib.contextmanager
+    def use(s):
+        prev, state["cur"] = state["cur"], s
+        try:
+            yield
+        finally:
+            state["cur"] = prev
+
+    monkeypatch.setattr(torch.cuda, "Stream", FakeStream)
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a: state["cur"])
+    monkeypatch.setattr(torch.cuda, "stream", use)
+    return log
+
+
+def test_lane_of_deals_runs_round_robin():
+    assert bm.PIC_batch.lane_of(5, 2) == [[0, 2, 4], [1, 3]]
+    assert bm.PIC_batch.lane_of(3, 3) == [[0], [1], [2]]
+    assert bm.PIC_batch.lane_of(4, 1) == [[0, 1, 2, 3]]
+
+
+def test_arguments_checked():
+    with pytest.raises(ValueError):
+        bm.PIC_batch([])
+    with pytest.raises(ValueError):
+        bm.PIC_batch([object()] * 3, lanes=4)
+    with pytest.raises(ValueError):
+        bm.PIC_batch([object()] * 3, candidates=(5, 8))
+
+
+def test_each_run_on_its_own_stream_chained_by_lanes(fakes):
+    log = fakes
+    loops = [FakeLoop(i, log) for i in range(5)]
+    b = bm.PIC_batch(loops, lanes=2)
+    b.step()  # first steps: one lane whatever `lanes` says
+    waits = [e for e in log if e[0] == "wait" and e[1] != "cur"]
+    assert waits == [("wait", "s0", "cur"), ("wait", "s1", "s0"), ("wait", "s2", "s1"),
+                     ("wait", "s3", "s2"), ("wait", "s4", "s3")]
+    log.clear()
+    b.step()
+    steps = [e for e in log if e[0] == "step"]
+    assert steps == [("step", i, "s%d" % i) for i in range(5)]  # streams kept
+    waits = [e for e in log if e[0] == "wait" and e[1] != "cur"]
+    assert waits == [("wait", "s0", "cur"), ("wait", "s1", "cur"), ("wait", "s2", "s0"),
+                     ("wait", "s3", "s1"), ("wait", "s4", "s2")]
+    joins = [e for e in log if e[0] == "wait" and e[1] == "cur"]
+    assert joins == [("wait", "cur", "s%d" % i) for i in range(5)]
+    assert all(lp.it == 2 for lp in loops) and b.it == 2
+
+
+def test_autotuner_keeps_the_fastest_lane_count(fakes):
+    log = fakes
+    loops = [FakeLoop(i, log, steps=7, capture_at=(1, 8)) for i in range(4)]
+    b = bm.PIC_batch(loops, candidates=(1, 2, 4), tune_steps=2)
+    t = [0.0]
+    cost = {1: 3.0, 2: 1.0, 4: 2.0}
+    issued = []
+    orig = b._issue
+
+    def issue(k):
+        issued.append(k)
+        t[0] += cost[k]
+        orig(k)
+
+    b._issue, b._clock, b._sync = issue, (lambda: t[0]), (lambda: None)
+    b.run(16)
+    # step 0: first steps (one lane); steps 1 and 8 capture, 7 and 14 shift
+    # the window: untimed.  Timed steps go to the candidates in order.
+    assert issued[:1] == [1]
+    assert {c: len(v) for c, v in b.tune_log.items()} == {1: 2, 2: 2, 4: 2}
+    assert all(v == [cost[c]] * 2 for c, v in b.tune_log.items())
+    assert b.lanes == 2
+    assert issued[-3:] == [2, 2, 2]
+    assert all(lp.it == 16 for lp in loops)
