@@ -539,19 +539,9 @@ class OFrame:
 
 
 # ----------------------------------------------------------------------
-def add_gausian_pulse(solver, laser):
-    """laser.py:3-37"""
-    A, D = solver.Args, solver.D
-    k0 = 2 * np.pi * laser["k0"]
-    a0, Lx, R, x0, xf = (laser[k] for k in ("a0", "Lx", "R", "x0", "x_foc"))
-    Xf = x0 - xf
-    Xg, Rg = A["Xgrid"], A["Rgrid"]
-    kx, w = A["kx"][None, :], A["w_m0"]
-    D["Ez_m0"][1:] = (a0 * np.sin(k0 * (Xg[None, :] - x0))
-                      * np.exp(-(Xg[None, :] - x0) ** 2 / Lx ** 2 - Rg[1:, None] ** 2 / R ** 2)
-                      * (abs(Rg[1:, None]) < 3.5 * R) * (abs(Xg[None, :] - x0) < 3.5 * Lx))
-    solver.fb_transform(scals=["Ez"], dir=0)
-    EE = D["Ez_fb_m0"].copy()
+def _focus_pulse(EE, w, kx, Xf):
+    """laser.py:24-33: spectral E -> (E, G) of the forward-moving pulse
+    moved back by Xf."""
     DT = -1.0j * w * np.sign(kx + (kx == 0))
     GG = DT * EE
     EEt = np.cos(w * Xf) * EE + np.sin(w * Xf) / w * GG
@@ -559,8 +549,37 @@ def add_gausian_pulse(solver, laser):
     EE = EEt
     EE *= np.exp(1.0j * kx * Xf)
     GG *= np.exp(1.0j * kx * Xf)
+    return EE, GG
+
+
+def add_gausian_pulse(solver, laser):
+    """laser.py:3-37.  Restatement extension without reference code:
+    laser["astig"] = a2 (M >= 2) adds the first-order astigmatic term
+    Ez_m2 = -(a2/2) (r/R)^2 x the mode-0 profile (the expansion of
+    exp(-r^2 (1 + a2 cos 2 phi)/R^2) with fields read as
+    F_0 + 2 Re(F_2 e^{-2 i phi})), focused with w_m2."""
+    A, D = solver.Args, solver.D
+    k0 = 2 * np.pi * laser["k0"]
+    a0, Lx, R, x0, xf = (laser[k] for k in ("a0", "Lx", "R", "x0", "x_foc"))
+    a2 = float(laser.get("astig", 0.0) or 0.0)
+    if a2 and A["M"] < 2:
+        raise ValueError("an astigmatic laser (astig != 0) needs M >= 2 modes")
+    Xf = x0 - xf
+    Xg, Rg = A["Xgrid"], A["Rgrid"]
+    kx, w = A["kx"][None, :], A["w_m0"]
+    D["Ez_m0"][1:] = (a0 * np.sin(k0 * (Xg[None, :] - x0))
+                      * np.exp(-(Xg[None, :] - x0) ** 2 / Lx ** 2 - Rg[1:, None] ** 2 / R ** 2)
+                      * (abs(Rg[1:, None]) < 3.5 * R) * (abs(Xg[None, :] - x0) < 3.5 * Lx))
+    if a2:
+        D["Ez_m2"][1:] = -0.5 * a2 * (Rg[1:, None] / R) ** 2 * D["Ez_m0"][1:]
+    solver.fb_transform(scals=["Ez"], dir=0)
+    EE, GG = _focus_pulse(D["Ez_fb_m0"].copy(), w, kx, Xf)
     D["Ez_fb_m0"][:] = EE
     D["Gz_fb_m0"][:] = GG
+    if a2:
+        EE, GG = _focus_pulse(D["Ez_fb_m2"].copy(), A["w_m2"], kx, Xf)
+        D["Ez_fb_m2"][:] = EE
+        D["Gz_fb_m2"][:] = GG
     solver.restore_B_fb()
     solver.fb_transform(vects=["B", "E"], dir=1)
 
