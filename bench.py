@@ -588,6 +588,61 @@ def run_ours(args):
     return 0
 
 
+LARGE_MODES_WORKLOAD = "lpa_large_modes_4096x512_m2"
+
+
+def large_modes_workload(seed=0):
+    """The large-mode run: Nz = 4096, Nr = 512 on the single run's cells
+    (window z in [-160, 0], r in [0, 80] lambda0), modes m = 0, 1, 2, 2x2x4
+    macro-electrons per cell (about 33.5M) in uniform n_e = 1e-3 n_c,
+    immobile ions, laser a0 = 4, w0 = 12, tau = 10 (field FWHM) centred and
+    focused at z = -20 (its envelope is 1.5e-5 of the peak at the window's
+    front), with a 20% m = 2 astigmatic term; moving window with injection
+    every 20 steps; seeded."""
+    tau = 10.0
+    return dict(
+        grid_in=dict(Xmin=-160.0, Xmax=0.0, Nx=4096, Rmin=0.0, Rmax=80.0, Nr=512, M=2,
+                     DampCells=50),
+        eons_in=dict(Nppc=(2, 2, 4), dens=1e-3, charge=-1),
+        frame_in=dict(Velocity=1.0, Steps=20),
+        laser_in=dict(k0=1.0, a0=4.0, x0=-20.0, Lx=tau / (2 * np.sqrt(np.log(2))), R=12.0,
+                      x_foc=-20.0, astig=0.2),
+        prefill=dict(Xmin=-160.0, Xmax=0.0, Rmin=0.0, Rmax=80.0),
+        profiles=None, seed=seed)
+
+
+def run_large_modes(args):
+    """The large-mode run in the mixed form and in FP64 on the same seed:
+    device-timed steps of each (CUDA events, after the warm-up) and the
+    mixed run's relative error against the FP64 run per field (E, B, rho of
+    each mode, pointwise L2) and in the integrated diagnostics at the same
+    step."""
+    import torch
+    cfg = large_modes_workload(seed=args.batch_seed)
+    r32 = time_arm(cfg, "mixed", args.steps, args.warmup, 0, None)
+    r64 = time_arm(cfg, "fp64", args.steps, args.warmup, 0, None)
+    torch.cuda.synchronize()
+    g = cfg["grid_in"]
+    line = {
+        "metric": "electron particle-steps/s (large-mode run)",
+        "value": r32["np_sum"] / (r32["ms"] * 1e-3), "unit": "particle-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r32["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (radial GEMMs SIMT FP32: Nr - 1 > 256)",
+        "data": "synthetic (seeded plasma, laser)",
+        "config": {"workload": LARGE_MODES_WORKLOAD, "Nz": g["Nx"], "Nr": g["Nr"],
+                   "modes": g["M"] + 1, "ppc": [2, 2, 4], "a0": 4.0, "w0": 12.0, "tau": 10.0,
+                   "astig": 0.2, "l2": "working set larger than L2; no flush"},
+        "fp64": {"value": r64["np_sum"] / (r64["ms"] * 1e-3),
+                 "ms_per_step": r64["ms"] / args.steps},
+        "mixed_over_fp64": (r32["np_sum"] / r32["ms"]) / (r64["np_sum"] / r64["ms"]),
+        "mixed_vs_fp64_error": compare_runs(cfg, r32, r64),
+        "clocks": r32["clocks"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 BATCHED_WORKLOAD = "lpa_batched_uneven_64"
 
 
@@ -752,8 +807,9 @@ def main(argv=None):
     ap.add_argument("--accuracy", action="store_true",
                     help="run the mixed-vs-FP64 accuracy study instead of the benchmark")
     ap.add_argument("--acc-steps", type=int, default=608)
-    ap.add_argument("--workload", default="single", choices=["single", "batched"],
-                    help="batched: 64 small uneven runs through PIC_batch (1 GPU)")
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "large_modes"],
+                    help="batched: 64 small uneven runs through PIC_batch; large_modes: "
+                         "the 4096 x 512, m = 0..2 run, mixed against FP64 (1 GPU)")
     ap.add_argument("--batch-runs", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=0)
     args = ap.parse_args(argv)
@@ -765,6 +821,8 @@ def main(argv=None):
         return run_accuracy(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "large_modes":
+        return run_large_modes(args)
     return run_ours(args)
 
 
