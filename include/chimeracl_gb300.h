@@ -32,7 +32,7 @@ extern "C" {
 #define CCL_OK 0
 #define CCL_ERR_ARG 1         /* invalid argument (null pointer, bad size) */
 #define CCL_ERR_CUDA 2        /* a CUDA launch or runtime call failed */
-#define CCL_ERR_UNSUPPORTED 3 /* a size or mode this build does not handle */
+#define CCL_ERR_UNSUPPORTED 3 /* a size or mode this library does not handle */
 #define CCL_ERR_WORKSPACE 4   /* workspace smaller than required */
 
 #define CCL_F64 0

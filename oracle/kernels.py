@@ -4,7 +4,7 @@ ctypes front ends for the two CPU kernel sets the oracle can run on:
 
 * ``PortKernels``  -- ``oracle/liboracle.so``, this repository's plain-C
   restatement of the reference kernels (``oracle/oracle_kernels.c``).  It
-  builds on any host (x86_64 here, aarch64 on the GPU machine).
+  builds on any host (x86_64 or aarch64).
 * ``RefKernels``   -- ``oracle/_ref/libref_*.so``, the reference's own OpenCL
   kernels (``chimeraCL/kernels/*.cl``) compiled unchanged as C++ through
   ``oracle/cl_shim.hpp``.  Only where the reference tree is present.

@@ -1,7 +1,7 @@
 /*
  * THE ORACLE -- test infrastructure only.  Nothing in the product imports,
  * links or calls this file; tests, __graft_entry__.smoke() and bench.py's CPU
- * baseline use it as the checker.
+ * baseline use it to check the product and as the timed CPU baseline.
  *
  * A plain-C restatement of the arithmetic of chimeraCL's OpenCL kernels
  * (chimeraCL/kernels/*.cl), one function per reference kernel, taking host

@@ -157,8 +157,8 @@ def test_full_run_diagnostics_fp64(cuda):
 
 
 def test_one_step_fp64_astigmatic_laser(cuda):
-    """The large-mode configuration's laser form: a 20% m = 2 astigmatic
-    term (M = 2) set up on both sides, then one step -- fields within 1e-12
+    """The laser form of the 4096 x 512, m = 0..2 run: a 20% m = 2
+    astigmatic term (M = 2) set up on both sides, then one step -- fields within 1e-12
     of their physical scale, sort arrays identical, particles within 1e-12."""
     cfg = small_lpa(Nx=128, Nr=32, M=2, seed=14)
     cfg["laser_in"]["astig"] = 0.2

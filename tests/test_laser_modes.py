@@ -1,4 +1,4 @@
-"""The astigmatic laser term (m = 2, config 3's 20% astigmatic component) in
+"""The astigmatic laser term (m = 2; the 4096 x 512 run's 20% component) in
 the oracle's laser set-up, on the CPU: with the focus at the pulse the
 spectral round trip returns Ez_m2 = -(a2/2) (r/R)^2 x the mode-0 profile,
 the mode-0 fields are those of the plain laser bit for bit, the synthesised
