@@ -8,6 +8,18 @@ from .._lib import CCL_F64, PP, call, sort_workspace_bytes, stream
 from .generic_methods_cu import GenericMethodsCU, LazyScalar
 
 
+def injector_last_columns(Xg, npx):
+    """x of the particle columns of an injected slab's last two cells, last
+    column first, in the injector's double arithmetic (particles_generic.cl:
+    62-74, x = xmin + ((0.5 + ixx) * (1/npx)) * Lx): the values whose FP32
+    rounding the slab stores there.  The last cell can fall outside the
+    window and be dropped, hence two."""
+    Nx_loc = len(Xg)
+    return [float(Xg[ix] + (0.5 + ixx) * (1.0 / npx) * (Xg[ix + 1] - Xg[ix]))
+            for ix in (Nx_loc - 2, Nx_loc - 3) if ix >= 0
+            for ixx in range(npx - 1, -1, -1)]
+
+
 class ParticleMethodsCU(GenericMethodsCU):
     def init_particle_methods(self):
         self.init_generic_methods()
@@ -55,14 +67,8 @@ class ParticleMethodsCU(GenericMethodsCU):
         Xg = xmin + A["dx"] * np.arange(Nx_loc)
         Rg = rmin + A["dr"] * np.arange(Nr_loc)
         A["right_lim"] = Xg[-1]
-        # x of the slab's particle columns in its last two cells, last first,
-        # in the injector's double arithmetic (particles_generic.cl:62-74
-        # order): what an FP32 store of those columns rounds (the last cell
-        # can fall outside the window and be dropped)
-        npx = int(A["Nppc"][0])
-        A["_inj_last_x"] = [float(Xg[ix] + (0.5 + ixx) * (1.0 / npx) * (Xg[ix + 1] - Xg[ix]))
-                            for ix in (Nx_loc - 2, Nx_loc - 3) if ix >= 0
-                            for ixx in range(npx - 1, -1, -1)]
+        # candidates for the next right limit of FP32 coordinates
+        A["_inj_last_x"] = injector_last_columns(Xg, int(A["Nppc"][0]))
         ncells = (Nx_loc - 1) * (Nr_loc - 1)
         Np = int(ncells * np.prod(A["Nppc"]))
         real = self.comm.real

@@ -175,3 +175,37 @@ def test_injector_right_limit_fp32_uses_the_lattice_value():
         fr.inject_plasma([sp], grid)
         want = {"last": c, "dropped": cols[2], "moved": float(np.float32(c + 0.01))}[case]
         assert sp.Args["right_lim"] == want + 0.125, case
+
+
+@pytest.mark.parametrize("nppc", [(2, 2, 4), (2, 1, 4)])
+def test_fp64_right_limits_are_injector_columns(nppc):
+    """The premise of the FP32 forms' right limit, on the oracle's FP64 runs
+    (a0 = 3 laser, moving window, five shifts): after each injection, sort
+    and align, the largest x among the last Nppc + 1 particles -- what
+    right_lim is formed from -- is exactly one of the injector's
+    last-column values as the product computes them."""
+    from chimeracl_gb300.methods.particles_methods_cu import injector_last_columns
+    from tests.lpa_setup import build_oracle, small_lpa
+    cfg = small_lpa(Nx=128, Nr=16, M=1, nppc=nppc, a0=3.0, steps=10, seed=7)
+    osol, oe, oi, oloop = build_oracle(cfg)
+    seen = []
+    cand = {}
+    make, align = oe.make_new_domain, oe.align_parts
+
+    def make_new_domain(pin, density_profiles=None):
+        n = int(np.ceil((pin["Xmax"] - pin["Xmin"]) / oe.Args["dx"]) + 1)
+        Xg = pin["Xmin"] + oe.Args["dx"] * np.arange(n)
+        cand["x"] = injector_last_columns(Xg, int(oe.Args["Nppc"][0]))
+        return make(pin, density_profiles=density_profiles)
+
+    def align_parts():
+        align()
+        k = int(np.prod(oe.Args["Nppc"]) + 1)
+        seen.append((float(oe.D["x"][-k:].max()), list(cand["x"])))
+
+    oe.make_new_domain, oe.align_parts = make_new_domain, align_parts
+    for _ in range(41):
+        oloop.step()
+    assert len(seen) == 5
+    for x_max, xs in seen:
+        assert x_max in xs, (x_max, xs)
