@@ -25,7 +25,9 @@ steps try each candidate in turn (``tune_steps`` timed steps each), the
 smallest median host time per step (issue to device idle) wins, and later
 steps use it.  A step is eligible when no run shifts its window and no run
 captures a graph in it (those steps run eagerly and capture; their time
-says nothing about the lane count).  Results do not depend on the lane
+says nothing about the lane count); steps that are not run with the
+largest candidate, so runs that never replay graphs (diagnostics attached,
+timers on) keep full concurrency.  Results do not depend on the lane
 count, so tuning on the real steps costs only the slower candidates' time.
 
 First steps.  A run's first step builds the library's lazily created,
@@ -121,8 +123,15 @@ class PIC_batch:
             k = self.lanes
         else:
             cand = self._candidate()
-            k = self._pick() if cand is None else cand
-        if cand is not None and self._eligible():
+            if cand is None:
+                k = self._pick()
+            elif self._eligible():
+                k = cand
+            else:
+                # an untimed step while tuning (window shift, capture, or
+                # runs that never replay graphs): all lanes
+                k, cand = self.candidates[-1], None
+        if cand is not None:
             caps0 = sum(lp.graph_captures for lp in self.loops)
             self._sync()
             t0 = self._clock()

@@ -116,11 +116,27 @@ def test_autotuner_keeps_the_fastest_lane_count(fakes):
 
     b._issue, b._clock, b._sync = issue, (lambda: t[0]), (lambda: None)
     b.run(16)
-    # step 0: first steps (one lane); steps 1 and 8 capture, 7 and 14 shift
-    # the window: untimed.  Timed steps go to the candidates in order.
-    assert issued[:1] == [1]
+    # step 0: first steps (one lane); step 7 shifts the window (untimed, all
+    # lanes); steps 1 and 8 capture (timed, discarded).  Timed steps go to
+    # the candidates in order.
+    assert issued[:3] == [1, 1, 1] and issued[7] == 4
     assert {c: len(v) for c, v in b.tune_log.items()} == {1: 2, 2: 2, 4: 2}
     assert all(v == [cost[c]] * 2 for c, v in b.tune_log.items())
     assert b.lanes == 2
     assert issued[-3:] == [2, 2, 2]
     assert all(lp.it == 16 for lp in loops)
+
+
+def test_runs_that_never_replay_keep_all_lanes(fakes):
+    log = fakes
+    loops = [FakeLoop(i, log) for i in range(3)]
+    for lp in loops:
+        lp.diags = ["a diagnostic"]  # eager steps: never timed
+    b = bm.PIC_batch(loops, candidates=(1, 3))
+    b._sync = lambda: None
+    b.run(6)
+    assert b.lanes is None and all(len(v) == 0 for v in b.tune_log.values())
+    log.clear()
+    b.step()
+    waits = [e for e in log if e[0] == "wait" and e[1] != "cur"]
+    assert waits == [("wait", "s%d" % i, "cur") for i in range(3)]
