@@ -393,10 +393,8 @@ def e2e_arm(run, steps):
                 d2h=(comm.d2h_bytes - d0) / steps)
 
 
-def cpu_oracle_rate(cfg, steps, warmup=1):
-    """The oracle (reference step restated; C kernels with OpenMP over the
-    host cores, numpy FFT and GEMM) on the same workload: electron
-    particle-steps/s over `steps` steps after `warmup`."""
+def _oracle_rate_here(cfg, steps, warmup):
+    """Time the oracle in this process (see cpu_oracle_rate)."""
     from oracle import pic_oracle as po
     from oracle.kernels import PortKernels
     K = PortKernels()
@@ -412,6 +410,29 @@ def cpu_oracle_rate(cfg, steps, warmup=1):
         loop.step()
     t = time.perf_counter() - t0
     return n / t, K.num_threads(), t
+
+
+def cpu_oracle_rate(cfg, steps, warmup=1):
+    """The oracle (reference step restated; C kernels with OpenMP over the
+    host cores, numpy FFT and GEMM) on the same workload: electron
+    particle-steps/s over `steps` steps after `warmup`, the thread count,
+    the seconds.
+
+    It runs in a child process without torch, with OMP_WAIT_POLICY=passive:
+    OpenMP worker threads that spin between the oracle's short kernels
+    compete with numpy's BLAS threads for the cores (measured: 1.4x slower
+    on the 2048 x 256 workload, 12x on 512 x 64), and once a library has
+    started OpenMP in a process the policy can no longer be set."""
+    env = dict(os.environ, OMP_WAIT_POLICY="passive")
+    code = ("import json, sys; sys.path.insert(0, %r); import bench; "
+            "cfg = json.load(sys.stdin); "
+            "print(json.dumps(bench._oracle_rate_here(cfg, %d, %d)))" % (HERE, steps, warmup))
+    r = subprocess.run([sys.executable, "-c", code], input=json.dumps(cfg), env=env, cwd=HERE,
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CPU oracle run failed:\n" + r.stderr[-2000:])
+    rate, cores, t = json.loads(r.stdout.strip().splitlines()[-1])
+    return rate, cores, t
 
 
 def load_peaks():

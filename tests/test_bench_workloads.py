@@ -47,3 +47,12 @@ def test_batched_runs_ranges_and_seeding():
         assert lo < las["x0"] - 2 * las["Lx"] and las["x0"] + 2 * las["Lx"] < hi
     sizes = {(c["grid_in"]["Nx"], c["grid_in"]["Nr"]) for c in cases}
     assert len(sizes) > 10  # uneven
+
+
+def test_cpu_oracle_rate_in_a_child_process():
+    """The CPU baseline leg (the oracle in a child process without torch,
+    OpenMP threads passive): a rate, the thread count and the time come
+    back."""
+    from tests.lpa_setup import small_lpa
+    rate, cores, t = bench.cpu_oracle_rate(small_lpa(Nx=64, Nr=16, M=1), steps=2, warmup=1)
+    assert rate > 0 and cores >= 1 and t > 0
