@@ -1,7 +1,13 @@
 import os
 import sys
 
-import pytest
+# The oracle's OpenMP threads would otherwise spin between its short kernels
+# and compete with numpy's BLAS threads for the cores (12x slower oracle
+# steps on a 512 x 64 grid); the policy has to be set before the first
+# library that uses OpenMP (torch, the oracle) is loaded.
+os.environ.setdefault("OMP_WAIT_POLICY", "passive")
+
+import pytest  # noqa: E402
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
