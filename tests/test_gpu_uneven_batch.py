@@ -1,5 +1,5 @@
 """PIC_batch on the GPU: three mixed-precision runs of uneven grid sizes
-(256 x 32, 128 x 32, 96 x 24; different seeds, densities and lasers),
+(256 x 32, 128 x 32, 64 x 24; different seeds, densities and lasers),
 stepped together through two window shifts with the lane autotuner active,
 give bit for bit the fields and particles of the same runs stepped one
 after the other on one stream."""
@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = [dict(Nx=256, Nr=32, seed=41, a0=2.0, dens=1e-3, R=6.0),
          dict(Nx=128, Nr=32, seed=42, a0=1.5, dens=2e-3, R=5.0),
-         dict(Nx=96, Nr=24, seed=43, a0=2.5, dens=5e-4, R=4.0)]
+         dict(Nx=64, Nr=24, seed=43, a0=2.5, dens=5e-4, R=4.0)]
 STEPS = 25
 
 
