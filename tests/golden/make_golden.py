@@ -20,6 +20,15 @@ CASES = {
     "lpa_m0_64x16.npz": dict(Nx=64, Nr=16, M=0, steps=2, nsteps=3, seed=22),
 }
 
+# full runs: the 512 x 64, M = 1 LPA configuration (a0 = 2 laser, 2x2x4
+# macro-electrons per cell, moving window with injection every 20 steps)
+# for 200 steps; the fixture keeps summaries (integrated diagnostics,
+# counts, the final cell offsets and on-axis field rows), not the 0.5M
+# particles
+FULL_RUNS = {
+    "lpa_m1_512x64_200steps.npz": dict(Nx=512, Nr=64, M=1, nsteps=200, seed=21),
+}
+
 FIELDS = ("rho", "Jx", "Jz", "Ex", "Ez", "By", "Bz")
 
 
@@ -56,6 +65,27 @@ def run_case(case, K):
     return collect(s, e)
 
 
+def run_full(case, K):
+    """A full run (FULL_RUNS) through the oracle host with kernel set K;
+    returns its summary arrays."""
+    from oracle import pic_oracle as po
+    from tests.lpa_setup import small_lpa
+    cfg = small_lpa(Nx=case["Nx"], Nr=case["Nr"], M=case["M"], seed=case["seed"])
+    s, e, i, loop = po.build_lpa(copy.deepcopy(cfg["grid_in"]), cfg["eons_in"], cfg["frame_in"],
+                                 cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"])
+    for _ in range(case["nsteps"]):
+        loop.step()
+    d = po.diagnostics(s, [e])
+    st = {"diag:" + k: np.float64(v) for k, v in d.items()}
+    st["count:Np"] = np.int64(e.Args["Np"])
+    st["count:Np_stay"] = np.int64(e.Args["Np_stay"])
+    st["key:cell_offset"] = np.asarray(e.D["cell_offset"]).astype(np.uint32)
+    for f in ("Ex", "Ez", "rho"):
+        st[f"axis:{f}_m0"] = np.asarray(s.D[f"{f}_m0"][1])
+        st[f"axis:{f}_m1"] = np.asarray(s.D[f"{f}_m1"][1])
+    return st
+
+
 def main():
     from oracle.kernels import RefKernels
     K = RefKernels()
@@ -63,6 +93,10 @@ def main():
         st = run_case(case, K)
         np.savez_compressed(os.path.join(HERE, name), **st)
         print(name, sum(v.nbytes for v in st.values()) // 1024, "KiB raw")
+    for name, case in FULL_RUNS.items():
+        st = run_full(case, K)
+        np.savez_compressed(os.path.join(HERE, name), **st)
+        print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
 
 
 if __name__ == "__main__":

@@ -173,6 +173,24 @@ def test_oracle_reproduces_golden(K, name):
             assert np.abs(state[k] - g[k]).max() <= 1e-13 * scale, k
 
 
+def test_oracle_reproduces_full_run_golden(K):
+    """The 512 x 64, M = 1 LPA configuration for 200 steps (ten window
+    shifts with injection) through the C restatement reproduces the run of
+    the reference's own kernels: counts and final cell offsets identical,
+    integrated diagnostics and on-axis field rows within 1e-12."""
+    from tests.golden.make_golden import FULL_RUNS, run_full
+    name = "lpa_m1_512x64_200steps.npz"
+    g = _golden(name)
+    st = run_full(FULL_RUNS[name], K)
+    assert set(st) == set(g.files)
+    for k in g.files:
+        if k.startswith(("key:", "count:")):
+            np.testing.assert_array_equal(st[k], g[k], err_msg=k)
+        else:
+            scale = max(float(np.abs(g[k]).max()), 1e-300)
+            assert float(np.abs(st[k] - g[k]).max()) <= 1e-12 * scale, k
+
+
 def test_known_answer_fourier_bessel_round_trip(K):
     """examples/test_transformer.py: forward + backward Fourier-Bessel
     transform of a deposited beam returns the deposit (reduced beam)."""
