@@ -138,8 +138,9 @@ class _Host:
 def test_full_run_diagnostics_fp64(cuda):
     """The 512 x 64, M = 1 configuration (about 0.5M electrons, a0 = 2 laser,
     moving window) for 200 steps -- ten window shifts with injection --
-    through the public API and through the oracle: field energy, on-axis Ez
-    wake amplitude and electron kinetic energy within 1e-6 relative."""
+    through the public API, through the oracle and in the committed run of
+    the reference's own kernels: field energy, on-axis Ez wake amplitude and
+    electron kinetic energy within 1e-6 relative."""
     from oracle.pic_oracle import diagnostics
     cfg = small_lpa(Nx=512, Nr=64, M=1, seed=21)
     sol, e, i, loop = build_product(cfg)
@@ -154,6 +155,14 @@ def test_full_run_diagnostics_fp64(cuda):
     for k in ref:
         err = abs(got[k] / ref[k] - 1.0)
         assert err < 1e-6, (k, got[k], ref[k], err)
+    # the same run of the reference's own kernels (committed fixture)
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "lpa_m1_512x64_200steps.npz"))
+    assert e.Args["Np"] == int(g["count:Np"])
+    for k in ref:
+        err = abs(got[k] / float(g["diag:" + k]) - 1.0)
+        assert err < 1e-6, (k, got[k], float(g["diag:" + k]), err)
 
 
 def test_one_step_fp64_astigmatic_laser(cuda):
