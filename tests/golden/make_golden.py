@@ -2,7 +2,7 @@
 OpenCL kernels (compiled unchanged as C++ into oracle/_ref) driven by the
 oracle's host restatement of the reference step.
 
-    python -m tests.golden.make_golden        # needs oracle/_ref built
+    python -m tests.golden.make_golden [name.npz ...]   # needs oracle/_ref built
 
 Each case is a small moving-window LPA run (prefilled plasma, immobile ions,
 Gaussian laser, frame shift + injection every `steps` steps) stopped after
@@ -27,6 +27,12 @@ CASES = {
 # particles
 FULL_RUNS = {
     "lpa_m1_512x64_200steps.npz": dict(Nx=512, Nr=64, M=1, nsteps=200, seed=21),
+}
+
+# the 2048 x 256, M = 1 single run (2x1x4 per cell, density up-ramp over the
+# window's first 20 lambda0, a0 = 3 laser), 3 steps from its first injection
+BENCH_RUNS = {
+    "lpa_m1_2048x256_3steps.npz": dict(nsteps=3, seed=1000),
 }
 
 FIELDS = ("rho", "Jx", "Jz", "Ex", "Ez", "By", "Bz")
@@ -65,14 +71,16 @@ def run_case(case, K):
     return collect(s, e)
 
 
-def run_full(case, K):
-    """A full run (FULL_RUNS) through the oracle host with kernel set K;
-    returns its summary arrays."""
+def run_full(case, K, cfg=None):
+    """A full run (FULL_RUNS, or BENCH_RUNS with the benchmark's `cfg`)
+    through the oracle host with kernel set K; returns its summary arrays."""
     from oracle import pic_oracle as po
     from tests.lpa_setup import small_lpa
-    cfg = small_lpa(Nx=case["Nx"], Nr=case["Nr"], M=case["M"], seed=case["seed"])
+    if cfg is None:
+        cfg = small_lpa(Nx=case["Nx"], Nr=case["Nr"], M=case["M"], seed=case["seed"])
     s, e, i, loop = po.build_lpa(copy.deepcopy(cfg["grid_in"]), cfg["eons_in"], cfg["frame_in"],
-                                 cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"])
+                                 cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"],
+                                 density_profiles=cfg.get("profiles"))
     for _ in range(case["nsteps"]):
         loop.step()
     d = po.diagnostics(s, [e])
@@ -97,7 +105,35 @@ def main():
         st = run_full(case, K)
         np.savez_compressed(os.path.join(HERE, name), **st)
         print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
+    for name, case in BENCH_RUNS.items():
+        st = run_full(case, K, cfg=bench_cfg(case))
+        np.savez_compressed(os.path.join(HERE, name), **st)
+        print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
+
+
+def bench_cfg(case):
+    import bench
+    return bench.workload(seed=case["seed"])
+
+
+def main_only(names):
+    """Regenerate only the named fixtures."""
+    from oracle.kernels import RefKernels
+    K = RefKernels()
+    for name in names:
+        if name in BENCH_RUNS:
+            st = run_full(BENCH_RUNS[name], K, cfg=bench_cfg(BENCH_RUNS[name]))
+        elif name in FULL_RUNS:
+            st = run_full(FULL_RUNS[name], K)
+        else:
+            st = run_case(CASES[name], K)
+        np.savez_compressed(os.path.join(HERE, name), **st)
+        print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    if len(sys.argv) > 1:
+        main_only(sys.argv[1:])
+    else:
+        main()

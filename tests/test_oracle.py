@@ -173,15 +173,19 @@ def test_oracle_reproduces_golden(K, name):
             assert np.abs(state[k] - g[k]).max() <= 1e-13 * scale, k
 
 
-def test_oracle_reproduces_full_run_golden(K):
-    """The 512 x 64, M = 1 LPA configuration for 200 steps (ten window
-    shifts with injection) through the C restatement reproduces the run of
-    the reference's own kernels: counts and final cell offsets identical,
-    integrated diagnostics and on-axis field rows within 1e-12."""
-    from tests.golden.make_golden import FULL_RUNS, run_full
-    name = "lpa_m1_512x64_200steps.npz"
+@pytest.mark.parametrize("name", ["lpa_m1_512x64_200steps.npz", "lpa_m1_2048x256_3steps.npz"])
+def test_oracle_reproduces_full_run_golden(K, name):
+    """Runs of the reference's own kernels reproduced by the C restatement:
+    the 512 x 64, M = 1 LPA configuration for 200 steps (ten window shifts
+    with injection), and the 2048 x 256 single run (2x1x4 per cell, density
+    up-ramp) for its first 3 steps -- counts and final cell offsets
+    identical, integrated diagnostics and on-axis field rows within 1e-12."""
+    from tests.golden.make_golden import BENCH_RUNS, FULL_RUNS, bench_cfg, run_full
     g = _golden(name)
-    st = run_full(FULL_RUNS[name], K)
+    if name in BENCH_RUNS:
+        st = run_full(BENCH_RUNS[name], K, cfg=bench_cfg(BENCH_RUNS[name]))
+    else:
+        st = run_full(FULL_RUNS[name], K)
     assert set(st) == set(g.files)
     for k in g.files:
         if k.startswith(("key:", "count:")):
