@@ -39,6 +39,16 @@ Window shifts.  A run whose window shifts in a step reads two device
 scalars on the host (``Np_stay``, ``right_lim``); those reads wait for that
 run's stream only, while the other runs' kernels keep executing.
 
+One graph (``one_graph=True``).  On an eligible step (below) the whole
+batch step -- every run's particle work, field solve and gather + push, on
+the runs' streams with the lane chaining -- is captured into one CUDA graph
+on a capture stream that the runs' streams fork from and join back to, and
+replayed with one launch per batch step while no run's signature changes
+(its device buffers, particle counts, grid origin) and the lane count
+stays.  A run's window shift steps it alone (eagerly, on its stream) and
+changes its signature, so the next eligible step captures the batch again.
+Each run's phase factors are refreshed before a capture, outside it.
+
 CUDA maps streams onto ``CUDA_DEVICE_MAX_CONNECTIONS`` hardware queues (8
 unless that variable is set before CUDA starts); lanes beyond that share
 queues."""
@@ -49,7 +59,7 @@ import torch
 
 
 class PIC_batch:
-    def __init__(self, loops, lanes=None, candidates=None, tune_steps=3):
+    def __init__(self, loops, lanes=None, candidates=None, tune_steps=3, one_graph=False):
         self.loops = list(loops)
         if not self.loops:
             raise ValueError("PIC_batch needs at least one run")
@@ -68,6 +78,14 @@ class PIC_batch:
         # candidate -> host seconds of its timed steps
         self.tune_log = {c: [] for c in self.candidates}
         self._streams = None
+        self.one_graph = bool(one_graph)
+        # [graph, signature, refs kept alive, library launches captured]
+        self._bgraph = None
+        self._cap_stream = None
+        self.graph_captures = 0  # batch graphs captured
+        self.graph_replays = 0  # batch steps served by one graph replay
+        self.graph_kernels_captured = 0
+        self.graph_kernels_replayed = 0
         self.it = 0
         # replaceable for tests: a clock and a device-wide synchronisation
         self._clock = time.perf_counter
@@ -96,7 +114,9 @@ class PIC_batch:
         (eager) step: the step replays graphs only, unless a signature
         changed (checked after the step through the capture count)."""
         for lp in self.loops:
-            if lp.it == 0 or lp._frame_due() or not lp.graphs or lp.timit or lp.diags:
+            if lp.it == 0 or lp._frame_due() or lp.timit or lp.diags:
+                return False
+            if not (lp.graphs or self.one_graph):
                 return False
         return True
 
@@ -115,6 +135,70 @@ class PIC_batch:
         for s in self._streams:
             cur.wait_stream(s)
 
+    def _batch_signature(self, k):
+        sigs = [lp._signature("pa") for lp in self.loops]
+        return (k,) + tuple(sg[0] for sg in sigs), tuple(sg[1] for sg in sigs)
+
+    def _capture_batch(self, k):
+        """Capture one step of every run into one graph: run i on its own
+        stream, forked from the capture stream (i < k) or from run i - k's
+        stream, all joined back before the capture ends."""
+        from . import _lib
+        self._bgraph = None
+        for lp in self.loops:
+            for sol in lp.solvers:  # phase factors for the current origin
+                sol._phase(0)
+                sol._phase(1)
+        if self._streams is None:
+            self._streams = [torch.cuda.Stream() for _ in self.loops]
+        if self._cap_stream is None:
+            self._cap_stream = torch.cuda.Stream()
+        cap, streams = self._cap_stream, self._streams
+        n0 = _lib.launch_count()
+        g = torch.cuda.CUDAGraph()
+        cur = torch.cuda.current_stream()
+        cap.wait_stream(cur)
+        with torch.cuda.stream(cap):
+            g.capture_begin()
+            try:
+                for i, (lp, s) in enumerate(zip(self.loops, streams)):
+                    s.wait_stream(cap if i < k else streams[i - k])
+                    with torch.cuda.stream(s):
+                        lp._particles_before(graph_mode=True)
+                        lp._fields(graph_mode=True)
+                        lp._particles_after(graph_mode=True)
+                for s in streams:
+                    cap.wait_stream(s)
+            finally:
+                g.capture_end()
+        cur.wait_stream(cap)
+        nk = _lib.launch_count() - n0
+        sig, refs = self._batch_signature(k)
+        self._bgraph = [g, sig, refs, nk]
+        self.graph_captures += 1
+        self.graph_kernels_captured += nk
+
+    def _replay_batch(self, k):
+        """One batch step as one graph replay (captured first when the
+        signature changed)."""
+        if self._bgraph is None or self._batch_signature(k)[0] != self._bgraph[1]:
+            self._capture_batch(k)
+        self._bgraph[0].replay()
+        self.graph_kernels_replayed += self._bgraph[3]
+        for lp in self.loops:
+            lp.it += 1
+            lp.graph_replays += 1
+        self.graph_replays += 1
+
+    def _run(self, k):
+        if self.one_graph and self._eligible():
+            self._replay_batch(k)
+        else:
+            self._issue(k)
+
+    def _captures(self):
+        return self.graph_captures + sum(lp.graph_captures for lp in self.loops)
+
     def step(self):
         cand = None
         if any(lp.it == 0 for lp in self.loops):
@@ -132,16 +216,16 @@ class PIC_batch:
                 # runs that never replay graphs): all lanes
                 k, cand = self.candidates[-1], None
         if cand is not None:
-            caps0 = sum(lp.graph_captures for lp in self.loops)
+            caps0 = self._captures()
             self._sync()
             t0 = self._clock()
-            self._issue(k)
+            self._run(k)
             self._sync()
             dt = self._clock() - t0
-            if sum(lp.graph_captures for lp in self.loops) == caps0:
+            if self._captures() == caps0:
                 self.tune_log[cand].append(dt)
         else:
-            self._issue(k)
+            self._run(k)
         self.it += 1
         return self.it
 

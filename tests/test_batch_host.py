@@ -140,3 +140,95 @@ def test_runs_that_never_replay_keep_all_lanes(fakes):
     b.step()
     waits = [e for e in log if e[0] == "wait" and e[1] != "cur"]
     assert waits == [("wait", "s%d" % i, "cur") for i in range(3)]
+
+
+class FakeGraph:
+    log = None
+
+    def capture_begin(self):
+        FakeGraph.log.append(("capture_begin",))
+
+    def capture_end(self):
+        FakeGraph.log.append(("capture_end",))
+
+    def replay(self):
+        FakeGraph.log.append(("replay", id(self)))
+
+
+class FakeSolver:
+    def __init__(self, log, idx):
+        self.log, self.idx = log, idx
+
+    def _phase(self, d):
+        self.log.append(("phase", self.idx, d))
+
+
+class PieceLoop(FakeLoop):
+    """A run whose step pieces log the stream they are issued on; its
+    signature changes at each window shift (new origin)."""
+
+    def __init__(self, idx, log, steps=5):
+        super().__init__(idx, log, steps=steps)
+        self.solvers = [FakeSolver(log, idx)]
+        self.graph_replays = 0
+        self.origin = 0
+
+    def _signature(self, piece):
+        return (self.idx, self.origin), ()
+
+    def step(self):
+        if self._frame_due():
+            self.origin += 1
+        super().step()
+
+    def _piece(self, name):
+        self.log.append((name, self.idx, bm.torch.cuda.current_stream().name))
+
+    def _particles_before(self, graph_mode):
+        assert graph_mode
+        self._piece("pa")
+
+    def _fields(self, graph_mode):
+        self._piece("f")
+
+    def _particles_after(self, graph_mode):
+        self._piece("pb")
+
+
+def test_one_graph_captures_once_and_replays(fakes, monkeypatch):
+    log = fakes
+    FakeGraph.log = log
+    monkeypatch.setattr(torch.cuda, "CUDAGraph", FakeGraph)
+    from chimeracl_gb300 import _lib
+    monkeypatch.setattr(_lib, "launch_count", lambda: 0)
+    loops = [PieceLoop(i, log, steps=5) for i in range(3)]
+    b = bm.PIC_batch(loops, lanes=2, one_graph=True)
+    b.step()  # first steps: each run alone
+    assert b.graph_captures == 0 and all(lp.it == 1 for lp in loops)
+    log.clear()
+    b.step()  # captured, then replayed once
+    i0 = log.index(("capture_begin",))
+    i1 = log.index(("capture_end",))
+    # phases refreshed before the capture, outside it
+    assert all(("phase", i, d) in log[:i0] for i in range(3) for d in (0, 1))
+    inside = log[i0 + 1:i1]
+    pieces = [e for e in inside if e[0] in ("pa", "f", "pb")]
+    assert pieces == [(p, i, "s%d" % i) for i in range(3) for p in ("pa", "f", "pb")]
+    forks = [e for e in inside if e[0] == "wait" and e[1] != "s3"]
+    # s3 is the capture stream: runs 0, 1 fork from it, run 2 from run 0
+    assert forks == [("wait", "s0", "s3"), ("wait", "s1", "s3"), ("wait", "s2", "s0")]
+    joins = [e for e in inside if e[0] == "wait" and e[1] == "s3"]
+    assert joins == [("wait", "s3", "s%d" % i) for i in range(3)]
+    assert [e[0] for e in log[i1:]].count("replay") == 1
+    assert b.graph_captures == 1 and b.graph_replays == 1 and all(lp.it == 2 for lp in loops)
+    log.clear()
+    b.run(2)  # steps 2, 3: replays only
+    assert not any(e[0] in ("capture_begin", "pa") for e in log)
+    assert [e[0] for e in log].count("replay") == 2 and b.graph_captures == 1
+    log.clear()
+    b.step()  # step 4: no shift yet (it = 4); replay
+    b.step()  # step 5: window shift, every run alone
+    assert [e[0] for e in log].count("replay") == 1
+    assert all(lp.origin == 2 for lp in loops)
+    b.step()  # new signatures: captured again
+    assert b.graph_captures == 2 and all(lp.it == 7 for lp in loops)
