@@ -476,6 +476,11 @@ int ccl_dht_bf16x3_gemm_batch(int batch, int m, int k, const int *ncols,
 
 int ccl_dht_bf16x3_status(int reset) { return umma_status(reset); }
 
+int ccl_wait_probe(long spins, int arrive, int *gave_up, void *stream) {
+  NONNULL(gave_up);
+  return umma_wait_probe(spins, arrive, gave_up, S(stream));
+}
+
 int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
                       const void *c2, const void *c3, void *const *flds,
                       void *stream) {

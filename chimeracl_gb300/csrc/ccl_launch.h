@@ -138,6 +138,7 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
                     const void *const *X, const long *ldx, void *const *Y, const long *ldy,
                     double are, double aim, double beta, cudaStream_t s);
 int umma_status(int reset);
+int umma_wait_probe(long spins, int arrive, int *gave_up, cudaStream_t s);
 
 size_t index_sort_ws_bytes(long np, long ncells);
 int iota_u32(uint32_t *a, long n, cudaStream_t s);

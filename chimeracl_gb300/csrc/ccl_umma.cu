@@ -652,6 +652,32 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
   return CCL_OK;
 }
 
+// ------------------------------------------------------------------ wait probe
+// The bounded wait of the kernels above, made to run out on purpose: one
+// thread initialises an mbarrier that expects one arrival and (unless
+// `arrive`) nothing arrives; it polls phase 0 at most `spins` times and
+// writes 1 to *gave_up when the wait ran out, 0 when the phase completed.
+// It touches only its own shared memory and *gave_up, and ends after at
+// most `spins` polls.
+__global__ void k_wait_probe(long spins, int arrive, int *gave_up) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (arrive) mbar_arrive(&bar);
+  bool done = false;
+  for (long i = 0; i < spins && !done; i++) done = mbar_try_wait(&bar, 0);
+  *gave_up = done ? 0 : 1;
+}
+
+int umma_wait_probe(long spins, int arrive, int *gave_up, cudaStream_t s) {
+  CCL_REQUIRE(spins >= 1 && spins <= UM_SPIN_LIMIT, CCL_ERR_ARG,
+              "wait probe: spins=%ld outside [1, %ld]", spins, UM_SPIN_LIMIT);
+  k_wait_probe<<<1, 32, 0, s>>>(spins, arrive, gave_up);
+  CCL_LAUNCH_CHECK("wait_probe");
+  return CCL_OK;
+}
+
 int umma_status(int reset) {
   int v = 0;
   cudaMemcpyFromSymbol(&v, g_umma_error, sizeof(int));

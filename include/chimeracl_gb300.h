@@ -344,6 +344,14 @@ int ccl_dht_bf16x3_gemm_batch(int batch, int m, int k, const int *ncols,
                               double alpha_im, double beta, void *stream);
 int ccl_dht_bf16x3_status(int reset);
 
+/* Failure-detection check, no counterpart in the reference (which has no
+ * device waits): the tensor-core GEMM's bounded mbarrier wait on a barrier
+ * that nothing arrives on (arrive == 0) or that one arrival completes
+ * (arrive != 0), polled at most `spins` times (1 <= spins <= 20,000,000,
+ * about a second).  Writes 1 to the device int *gave_up when the wait ran
+ * out and 0 when it completed; the context stays usable either way. */
+int ccl_wait_probe(long spins, int arrive, int *gave_up, void *stream);
+
 /* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
  * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,
  * dN0_x..z, dN1_x..z; c1 = cos(w dt), c2 = sin(w dt) w, c3 = 1/w^2 (real).
