@@ -395,9 +395,11 @@ def e2e_arm(run, steps):
 
 
 def _oracle_rate_here(cfg, steps, warmup):
-    """Time the oracle in this process (see cpu_oracle_rate)."""
+    """Time the oracle in this process (see cpu_oracle_rate), its FFTs on all
+    host threads."""
     from oracle import pic_oracle as po
     from oracle.kernels import PortKernels
+    po.use_threaded_fft(-1)
     K = PortKernels()
     s, e, i, loop = po.build_lpa(copy.deepcopy(cfg["grid_in"]), cfg["eons_in"], cfg["frame_in"],
                                  cfg["laser_in"], prefill=cfg["prefill"], K=K, seed=cfg["seed"],
@@ -417,7 +419,8 @@ def cpu_oracle_rate(cfg, steps, warmup=1):
     """The oracle (reference step restated; C kernels with OpenMP over the
     host cores, numpy FFT and GEMM) on the same workload: electron
     particle-steps/s over `steps` steps after `warmup`, the thread count,
-    the seconds.
+    the seconds.  The oracle's FFTs run on all host threads (scipy.fft) as
+    its kernels (OpenMP) and GEMMs (BLAS) do.
 
     It runs in a child process without torch, with OMP_WAIT_POLICY=passive:
     OpenMP worker threads that spin between the oracle's short kernels

@@ -25,6 +25,24 @@ from scipy.special import jn, jn_zeros
 
 from .kernels import get_kernels
 
+# The longitudinal transforms: numpy's FFT by default (forward unnormalised,
+# inverse 1/N, the convention of the reference's pyFFTW/numpy path).  The
+# timed CPU baseline may switch to scipy's multi-threaded FFT of the same
+# convention (use_threaded_fft); the tests and fixtures keep numpy's.
+_FFT = {"fft": np.fft.fft, "ifft": np.fft.ifft}
+
+
+def use_threaded_fft(workers=-1):
+    """Take scipy.fft with `workers` threads for the oracle's transforms
+    (same convention; results differ from numpy's in the last bits)."""
+    import scipy.fft as sf
+    _FFT["fft"] = lambda a, axis: sf.fft(a, axis=axis, workers=workers)
+    _FFT["ifft"] = lambda a, axis: sf.ifft(a, axis=axis, workers=workers)
+
+
+def use_numpy_fft():
+    _FFT["fft"], _FFT["ifft"] = np.fft.fft, np.fft.ifft
+
 VEC = ("x", "y", "z")
 
 
@@ -205,13 +223,13 @@ class OGrid:
                         out = np.dot(A["DHT_m" + s], np.ascontiguousarray(src))
                 else:
                     out = src.astype(np.complex128)
-                out = np.ascontiguousarray(np.fft.fft(out, axis=1))
+                out = np.ascontiguousarray(_FFT["fft"](out, axis=1))
                 K.multiply_by_phase(out, phs)
                 D[arg + "_fb_m" + s][:] = out
             else:
                 buf = D[arg + "_fb_m" + s].copy()
                 K.multiply_by_phase(buf, phs)
-                buf = np.ascontiguousarray(np.fft.ifft(buf, axis=1))
+                buf = np.ascontiguousarray(_FFT["ifft"](buf, axis=1))
                 if m == 0:
                     re = np.empty(buf.shape)
                     K.cast_c2d(buf, re)

@@ -251,3 +251,26 @@ def test_known_answer_laser_group_velocity(K):
     e1, e2 = laser_velocity_errors(K)
     assert e1 < 1e-3 and e2 < 2e-2
     np.testing.assert_allclose([e1, e2], [1.0390489878432e-04, 1.0728571893408624e-02], rtol=1e-6)
+
+
+def test_threaded_fft_oracle_matches_numpy_fft(K):
+    """The timed CPU baseline's oracle (scipy's multi-threaded FFT) agrees
+    with the tests' oracle (numpy's FFT) to rounding over a few LPA steps."""
+    from tests.lpa_setup import build_oracle, small_lpa
+    cfg = small_lpa(Nx=96, Nr=24, M=1, seed=4, steps=3)
+    runs = []
+    for threaded in (False, True):
+        if threaded:
+            po.use_threaded_fft(-1)
+        try:
+            s, e, i, loop = build_oracle(cfg)
+            for _ in range(5):
+                loop.step()
+        finally:
+            po.use_numpy_fft()
+        runs.append((s, e))
+    (s0, e0), (s1, e1) = runs
+    assert e0.Args["Np"] == e1.Args["Np"]
+    for k in ("Ex_m0", "Ez_m0", "Ez_m1", "By_m1", "rho_m0"):
+        scale = max(np.abs(s0.D[k]).max(), 1e-300)
+        assert np.abs(s1.D[k] - s0.D[k]).max() <= 1e-10 * scale, k
