@@ -35,6 +35,30 @@ BENCH_RUNS = {
     "lpa_m1_2048x256_3steps.npz": dict(nsteps=3, seed=1000),
 }
 
+# further grid shapes: 1024 x 128 on the 512 x 64 run's window (the
+# differentiable run's grid, FP64 forward) for 20 steps, and the 384 x 96
+# run of the batched workload (1x1x4 per cell, entry 6 of its 64 seeded
+# runs) for 30 steps
+SHAPE_RUNS = {
+    "lpa_m1_1024x128_20steps.npz": dict(kind="window", Nx=1024, Nr=128, M=1, nsteps=20,
+                                        seed=31),
+    "lpa_m1_384x96_30steps.npz": dict(kind="batched", index=6, nsteps=30, seed=0),
+}
+
+
+def golden_run(name):
+    """(case, cfg or None) of a full-run fixture by file name."""
+    if name in FULL_RUNS:
+        return FULL_RUNS[name], None
+    if name in BENCH_RUNS:
+        return BENCH_RUNS[name], bench_cfg(BENCH_RUNS[name])
+    case = SHAPE_RUNS[name]
+    if case["kind"] == "window":
+        from tests.lpa_setup import small_lpa
+        return case, small_lpa(Nx=case["Nx"], Nr=case["Nr"], M=case["M"], seed=case["seed"])
+    import bench
+    return case, bench.batched_cases(64, seed=case["seed"])[case["index"]]
+
 FIELDS = ("rho", "Jx", "Jz", "Ex", "Ez", "By", "Bz")
 
 
@@ -105,8 +129,9 @@ def main():
         st = run_full(case, K)
         np.savez_compressed(os.path.join(HERE, name), **st)
         print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
-    for name, case in BENCH_RUNS.items():
-        st = run_full(case, K, cfg=bench_cfg(case))
+    for name in list(BENCH_RUNS) + list(SHAPE_RUNS):
+        case, cfg = golden_run(name)
+        st = run_full(case, K, cfg=cfg)
         np.savez_compressed(os.path.join(HERE, name), **st)
         print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
 
@@ -121,12 +146,11 @@ def main_only(names):
     from oracle.kernels import RefKernels
     K = RefKernels()
     for name in names:
-        if name in BENCH_RUNS:
-            st = run_full(BENCH_RUNS[name], K, cfg=bench_cfg(BENCH_RUNS[name]))
-        elif name in FULL_RUNS:
-            st = run_full(FULL_RUNS[name], K)
-        else:
+        if name in CASES:
             st = run_case(CASES[name], K)
+        else:
+            case, cfg = golden_run(name)
+            st = run_full(case, K, cfg=cfg)
         np.savez_compressed(os.path.join(HERE, name), **st)
         print(name, sum(np.asarray(v).nbytes for v in st.values()) // 1024, "KiB raw")
 

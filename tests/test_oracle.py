@@ -173,19 +173,20 @@ def test_oracle_reproduces_golden(K, name):
             assert np.abs(state[k] - g[k]).max() <= 1e-13 * scale, k
 
 
-@pytest.mark.parametrize("name", ["lpa_m1_512x64_200steps.npz", "lpa_m1_2048x256_3steps.npz"])
+@pytest.mark.parametrize("name", ["lpa_m1_512x64_200steps.npz", "lpa_m1_2048x256_3steps.npz",
+                                  "lpa_m1_1024x128_20steps.npz", "lpa_m1_384x96_30steps.npz"])
 def test_oracle_reproduces_full_run_golden(K, name):
     """Runs of the reference's own kernels reproduced by the C restatement:
     the 512 x 64, M = 1 LPA configuration for 200 steps (ten window shifts
-    with injection), and the 2048 x 256 single run (2x1x4 per cell, density
-    up-ramp) for its first 3 steps -- counts and final cell offsets
-    identical, integrated diagnostics and on-axis field rows within 1e-12."""
-    from tests.golden.make_golden import BENCH_RUNS, FULL_RUNS, bench_cfg, run_full
+    with injection), the 2048 x 256 single run (2x1x4 per cell, density
+    up-ramp) for its first 3 steps, 1024 x 128 on the 512 x 64 window for 20
+    steps and a 384 x 96 run of the batched workload (1x1x4 per cell) for 30
+    -- counts and final cell offsets identical, integrated diagnostics and
+    on-axis field rows within 1e-12."""
+    from tests.golden.make_golden import golden_run, run_full
     g = _golden(name)
-    if name in BENCH_RUNS:
-        st = run_full(BENCH_RUNS[name], K, cfg=bench_cfg(BENCH_RUNS[name]))
-    else:
-        st = run_full(FULL_RUNS[name], K)
+    case, cfg = golden_run(name)
+    st = run_full(case, K, cfg=cfg)
     assert set(st) == set(g.files)
     for k in g.files:
         if k.startswith(("key:", "count:")):
