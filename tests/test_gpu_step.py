@@ -164,23 +164,3 @@ def test_full_run_diagnostics_fp64(cuda):
         err = abs(got[k] / float(g["diag:" + k]) - 1.0)
         assert err < 1e-6, (k, got[k], float(g["diag:" + k]), err)
 
-
-def test_one_step_fp64_astigmatic_laser(cuda):
-    """The laser form of the 4096 x 512, m = 0..2 run: a 20% m = 2
-    astigmatic term (M = 2) set up on both sides, then one step -- fields within 1e-12
-    of their physical scale, sort arrays identical, particles within 1e-12."""
-    cfg = small_lpa(Nx=128, Nr=32, M=2, seed=14)
-    cfg["laser_in"]["astig"] = 0.2
-    sol, e, i, loop = build_product(cfg)
-    osol, oe, oi, oloop = build_oracle(cfg)
-    dens = cfg["eons_in"]["dens"]
-    assert float(sol.DataDev["Ez_m2"].abs().max()) > 0
-    assert compare_fields(sol, osol, dens=dens) < 1e-12
-    loop.step()
-    oloop.step()
-    torch.cuda.synchronize()
-    _sort_equal(e, oe)
-    _sort_equal(i, oi)
-    worst = compare_fields(sol, osol, dens=dens)
-    assert worst < 1e-12, worst
-    _particles_equal(e, oe, tol=1e-12)
