@@ -275,3 +275,55 @@ def test_threaded_fft_oracle_matches_numpy_fft(K):
     for k in ("Ex_m0", "Ez_m0", "Ez_m1", "By_m1", "rho_m0"):
         scale = max(np.abs(s0.D[k]).max(), 1e-300)
         assert np.abs(s1.D[k] - s0.D[k]).max() <= 1e-10 * scale, k
+
+
+def test_port_higher_modes_follow_their_definition(K):
+    """The restated kernels for modes the reference does not ship (it has
+    m = 0, 1 only; the restatement goes to m = 3), pinned by their
+    definitions, with m = 1 -- pinned bit for bit to the reference's kernel
+    above -- confirming the convention: a particle at angle phi
+    (e^{i phi} = (y + i z)/r) deposits rho_m = rho_0 e^{i m phi}; a uniform
+    mode-m field c acts on it as 2 Re(c e^{-i m phi}) (seen through the push
+    from rest with E alone, which is linear in E)."""
+    from tests.test_gpu_kernels import geom, oracle_sort
+    g = geom(40, 12)
+    M, Nr, Nx = 3, g["Nr"], g["Nx"]
+    nxnr4 = Nr // 2 * Nx // 2
+    geo = (g["Nx"], g["Xmin"], g["dx_inv"], g["Nr"], g["Rmin"], g["dr_inv"])
+    for phi in (0.3, 2.1, -1.2):
+        r = 2.0
+        p = {"x": np.array([-4.3]), "y": np.array([r * np.cos(phi)]),
+             "z": np.array([r * np.sin(phi)]), "w": np.array([1.3])}
+        _, _, off, srt = oracle_sort(K, p, g)
+        rho = [np.zeros((Nr, Nx))] + [np.zeros((Nr, Nx), np.complex128) for _ in range(M)]
+        K.depose_scalar(M, nxnr4, srt, p["x"], p["y"], p["z"], p["w"], off, -1, *geo, rho)
+        scale = np.abs(rho[0]).max()
+        assert scale > 0
+        for m in range(1, M + 1):
+            want = rho[0] * np.exp(1j * m * phi)
+            assert np.abs(rho[m] - want).max() <= 1e-14 * scale, (phi, m)
+
+        def kick(fields):
+            u = [np.zeros(1), np.zeros(1), np.zeros(1)]
+            g_inv = np.ones(1)
+            K.gather_and_push(M, p["x"], p["y"], p["z"], u[0], u[1], u[2], g_inv, srt, 0.37, 1,
+                              int(off[-2]), *geo, fields)
+            return np.array([c[0] for c in u])
+
+        def uniform_e(m, c):
+            f = []
+            for mm in range(M + 1):
+                for n in ("Ex", "Ey", "Ez", "Bx", "By", "Bz"):
+                    a = np.zeros((Nr, Nx)) if mm == 0 else np.zeros((Nr, Nx), np.complex128)
+                    if mm == m and n[0] == "E":
+                        a[:] = c
+                    f.append(a)
+            return f
+
+        du0 = kick(uniform_e(0, 1.0))
+        assert np.all(np.abs(du0) > 0)
+        for m in range(1, M + 1):
+            c = 0.7 - 0.4j
+            du = kick(uniform_e(m, c))
+            want = du0 * 2 * np.real(c * np.exp(-1j * m * phi))
+            assert np.abs(du - want).max() <= 1e-13 * np.abs(du0).max(), (phi, m)
