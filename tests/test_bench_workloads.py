@@ -56,3 +56,29 @@ def test_cpu_oracle_rate_in_a_child_process():
     from tests.lpa_setup import small_lpa
     rate, cores, t = bench.cpu_oracle_rate(small_lpa(Nx=64, Nr=16, M=1), steps=2, warmup=1)
     assert rate > 0 and cores >= 1 and t > 0
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference` (the oracle on the host cores, 1 step):
+    one JSON line with the contract's keys, its own rate as e2e, no
+    host-device traffic."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True,
+                       cwd=root, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+              "cpu_baseline", "e2e", "steps_timed"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps_timed"] == 1
+    assert d["config"]["workload"] == bench.WORKLOAD
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
