@@ -575,18 +575,41 @@ template <typename T> __global__ void k_twiddles(int n, cplx<T> *tw) {
   }
 }
 
-template <typename T> static const cplx<T> *twiddles(int n, cudaStream_t s) {
+// A table enters the cache only once it is complete (the building stream
+// is synchronised), so a call on another stream or host thread never reads
+// a table still being written.  Building one inside a stream capture would
+// only record the kernel (and cudaMalloc is not allowed there): the first
+// transform of each length must run outside any capture, else *why is set
+// and nullptr returned.
+template <typename T>
+static const cplx<T> *twiddles(int n, cudaStream_t s, const char **why) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, void *> cache;
   int dev = 0;
-  cudaGetDevice(&dev);
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *why = "cudaGetDevice failed";
+    return nullptr;
+  }
   std::lock_guard<std::mutex> lk(mu);
   auto key = std::make_pair(dev, n);
   auto it = cache.find(key);
   if (it != cache.end()) return (const cplx<T> *)it->second;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    *why = "first transform of this length inside a stream capture (run one outside it first)";
+    return nullptr;
+  }
   void *p = nullptr;
-  if (cudaMalloc(&p, sizeof(cplx<T>) * (size_t)n) != cudaSuccess) return nullptr;
+  if (cudaMalloc(&p, sizeof(cplx<T>) * (size_t)n) != cudaSuccess) {
+    *why = "cudaMalloc failed";
+    return nullptr;
+  }
   k_twiddles<T><<<(n + 255) / 256, 256, 0, s>>>(n, (cplx<T> *)p);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaFree(p);
+    *why = "twiddle kernel failed";
+    return nullptr;
+  }
   cache[key] = p;
   return (const cplx<T> *)p;
 }
@@ -645,8 +668,9 @@ int fft_forward_batch(int batch, int nrows, int nx, const void *const *in,
     b.ld[i] = in_ld[i];
     b.real[i] = in_real[i];
   }
-  const cplx<T> *tw = twiddles<T>(nx, s);
-  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  const char *why = "";
+  const cplx<T> *tw = twiddles<T>(nx, s, &why);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
 #define CCL_L(NN) k_fft_fwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
     CCL_REG_DISPATCH(nx, CCL_L)
@@ -681,8 +705,9 @@ int fft_backward_batch(int batch, int nrows, int nx, const void *const *in,
     b.ld[i] = out_ld[i];
     b.real[i] = out_real[i];
   }
-  const cplx<T> *tw = twiddles<T>(nx, s);
-  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  const char *why = "";
+  const cplx<T> *tw = twiddles<T>(nx, s, &why);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
 #define CCL_L(NN) k_fft_bwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
     CCL_REG_DISPATCH(nx, CCL_L)
@@ -716,8 +741,9 @@ int damp_batch(int batch, int nrows, int nx, void *const *spec,
     b.ld[i] = nx;
     b.real[i] = rs_real[i];
   }
-  const cplx<T> *tw = twiddles<T>(nx, s);
-  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table allocation failed");
+  const char *why = "";
+  const cplx<T> *tw = twiddles<T>(nx, s, &why);
+  CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
 #define CCL_L(NN)                                                                           \
   k_damp_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs_p, (const T *)phs_m, \

@@ -11,7 +11,7 @@
 // (grid_deposit_m1.cl:105-138).  The corner sums are then added to the node
 // tile in shared memory in four phases, one per cell colour
 // (ix&1) + 2(ir&1): the order in which the reference's four colour launches
-// add them (grid_methods_cl.py:261-264).  The result is the reference's sum,
+// add them (grid_methods_cl.py:66-69).  The result is the reference's sum,
 // term by term and in the same order, without its four launches.
 #pragma once
 #include "ccl_common.cuh"
@@ -283,7 +283,7 @@ int deposit_m(const u32 *sort_indx, const u32 *cell_off, const T *x,
     f.p[i] = flds[i];
   }
   dim3 grid((g.Nx + DEP_NTX - 1) / DEP_NTX, (g.Nr + DEP_NTR - 1) / DEP_NTR);
-  // the reference passes the charge as a signed char (grid_methods_cl.py:259)
+  // the reference passes the charge as a signed char (grid_methods_cl.py:61)
   T q = (T)(signed char)charge;
   if constexpr (sizeof(T) == 4) {
     if (lo) {

@@ -1,9 +1,12 @@
 // Allocation-free form of the cell sort: the workspace of ccl_index_sort
 // lives in a file-scope device array instead of caller-owned memory.
 //
-// The scratch is looked up once per device (cudaGetSymbolAddress, with that
-// device current) on the first call from that device, and every call then
-// runs the unchanged ccl_index_sort with it.  Nothing here allocates device
+// The scratch's device address is looked up (cudaGetSymbolAddress, with the
+// calling device current) on every call made outside a stream capture, so a
+// new context after cudaDeviceReset is picked up; a call made while its
+// stream is being captured reuses the address of the last uncaptured call on
+// that device, and is refused (CCL_ERR_UNSUPPORTED) when there was none.
+// Every call then runs the unchanged ccl_index_sort with it.  Nothing here allocates device
 // or host memory.  ccl_index_sort clears what must start at zero (the
 // per-cell counts and the scatter cursors) itself, on the stream, before
 // use; the rest of the scratch is written before it is read.  One scratch
@@ -25,8 +28,8 @@ __device__ __align__(256) unsigned char g_sort_scratch[kSortScratchBytes];
 std::mutex g_mu;
 void *g_scratch[kMaxDevices] = {};
 
-// the scratch's device address for the current device (set-up on first use)
-int scratch_for_current_device(void **out) {
+// the scratch's device address for the current device
+int scratch_for_current_device(cudaStream_t stream, void **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -37,8 +40,20 @@ int scratch_for_current_device(void **out) {
     ccl::set_error("ccl_index_sort_noalloc: device %d outside [0, %d)", dev, kMaxDevices);
     return CCL_ERR_UNSUPPORTED;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) {
+    ccl::set_error("ccl_index_sort_noalloc: cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+    return CCL_ERR_CUDA;
+  }
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch[dev]) {
+  if (cap != cudaStreamCaptureStatusNone) {
+    if (!g_scratch[dev]) {
+      ccl::set_error("ccl_index_sort_noalloc: first call on device %d inside a stream capture; "
+                     "call it once outside the capture first", dev);
+      return CCL_ERR_UNSUPPORTED;
+    }
+  } else {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess || !p) {
@@ -73,7 +88,7 @@ extern "C" int ccl_index_sort_noalloc(int dtype, long np, const void *x, const v
     return CCL_ERR_WORKSPACE;
   }
   void *ws = nullptr;
-  if ((rc = scratch_for_current_device(&ws))) return rc;
+  if ((rc = scratch_for_current_device((cudaStream_t)stream, &ws))) return rc;
   return ccl_index_sort(dtype, np, x, y, z, Nx, xmin, dx_inv, Nr, rmin, dr_inv, indx_in_cell,
                         sum_in_cell, cell_offset, sort_indx, np_stay, ws, kSortScratchBytes,
                         stream);

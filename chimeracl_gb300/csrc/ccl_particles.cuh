@@ -581,7 +581,9 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
               sort_ws_bytes(np, C));
   SortWs w = carve_sort_ws(ws, np, C);
   const long ntiles = (np + ST_TILE - 1) / ST_TILE;
-  cudaMemsetAsync(counts, 0, (C + 1) * sizeof(u32), s);
+  cudaError_t me = cudaMemsetAsync(counts, 0, (C + 1) * sizeof(u32), s);
+  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the counts: %s",
+              cudaGetErrorString(me));
   if (np > 0) {
     k_keys<T><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, x, y, z, g, indx, counts,
                                                       w.tile_ovf);
@@ -599,8 +601,10 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
     if (rc) return rc;
   }
   // cursors and multi-claim bits are adjacent: one memset clears both
-  cudaMemsetAsync(w.cursor, 0, (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32),
-                  s);
+  me = cudaMemsetAsync(w.cursor, 0,
+                       (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32), s);
+  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the cursors: %s",
+              cudaGetErrorString(me));
   k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
                                                     w.cursor, w.multi, w.tile_ovf, ovf_scanned,
                                                     sort_indx);

@@ -31,7 +31,7 @@ class GridMethodsCU(GenericMethodsCU):
         return self.DataDev[key]
 
     def depose_scalar(self, parts, src_scalar, dest_fld, charge):
-        """grid_methods_cl.py:239-264 (one launch instead of four colours)."""
+        """grid_methods_cl.py:44-69 (one launch instead of four colours)."""
         if parts.Args["Np"] <= 0:
             return
         D, M = parts.DataDev, self.Args["M"]
@@ -49,7 +49,7 @@ class GridMethodsCU(GenericMethodsCU):
         return [D[k].data_ptr() for k in ("x_lo", "y_lo", "z_lo")]
 
     def depose_vector(self, parts, vec, factors, vec_fld, charge):
-        """grid_methods_cl.py:266-290; factors = [g_inv, w]."""
+        """grid_methods_cl.py:71-95; factors = [g_inv, w]."""
         if parts.Args["Np"] <= 0:
             return
         D, M = parts.DataDev, self.Args["M"]
@@ -71,22 +71,22 @@ class GridMethodsCU(GenericMethodsCU):
              self.Args["Nr"], self._real_dev("dV_inv").data_ptr(), stream())
 
     def postproc_depose_scalar(self, fld):
-        """grid_methods_cl.py:293-319"""
+        """grid_methods_cl.py:98-124"""
         self._postproc([fld])
 
     def postproc_depose_vector(self, vec_fld):
-        """grid_methods_cl.py:321-346"""
+        """grid_methods_cl.py:126-151"""
         self._postproc([vec_fld + c for c in self.Args["vec_comps"]])
 
     def preproc_project_vec(self, vec_fld):
-        """grid_methods_cl.py:348-361"""
+        """grid_methods_cl.py:153-166"""
         M = self.Args["M"]
         names = [vec_fld + c for c in self.Args["vec_comps"]]
         flds = [self.DataDev[f + "_m" + str(m)] for f in names for m in range(M + 1)]
         call("ccl_warp_axis", self._dt, M, len(names), PP(flds), self.Args["Nx"], stream())
 
     def _gather_and_push(self, parts, flds):
-        """grid_methods_cl.py:363-387"""
+        """grid_methods_cl.py:168-192"""
         if parts.Args["Np"] == 0:
             return
         D, M = parts.DataDev, self.Args["M"]

@@ -98,9 +98,11 @@ int ccl_index_sort(int dtype, long np, const void *x, const void *y,
  * device memory is reserved up front by another framework).  The workspace is
  * a file-scope 8 MiB device array -- enough for up to 2,000,000 cells with up
  * to 2^26 particles; larger inputs return CCL_ERR_WORKSPACE without
- * launching anything.  The first call on a device does a one-time set-up
- * (looks up the array's device address) and should come before any stream
- * capture.  Nothing is allocated.  Calls that overlap in time on one device
+ * launching anything.  Each call outside a stream capture looks up the
+ * array's device address on the calling device (cudaGetSymbolAddress); a
+ * call inside a capture reuses the last one, so the first call on a device
+ * must come before any stream capture (inside one it returns
+ * CCL_ERR_UNSUPPORTED).  Nothing is allocated.  Calls that overlap in time on one device
  * (other streams, other host threads) share the array and race; outputs
  * and their meaning are those of ccl_index_sort. */
 int ccl_index_sort_noalloc(int dtype, long np, const void *x, const void *y,
@@ -148,7 +150,7 @@ int ccl_gamma_inv(int dtype, long np, const void *px, const void *py,
 
 /* rho_m += sum over sorted particles of q*w*S(x)S(r) e^{i m phi},
  * m = 0..M; rho is a host array of M+1 device pointers (m=0 real (Nr,Nx),
- * m>=1 complex (Nr,Nx)).  Replaces depose_scalar (grid_methods_cl.py:239-264,
+ * m>=1 complex (Nr,Nx)).  Replaces depose_scalar (grid_methods_cl.py:44-69,
  * grid_deposit_m0.cl:20-129, grid_deposit_m1.cl:20-152). */
 int ccl_deposit_scalar(int dtype, int M, const uint32_t *sort_indx,
                        const uint32_t *cell_offset, const void *x,
@@ -158,7 +160,7 @@ int ccl_deposit_scalar(int dtype, int M, const uint32_t *sort_indx,
 
 /* J_k,m += q*w*g_inv*u_k*S(x)S(r) e^{i m phi}; J is a host array of 3*(M+1)
  * device pointers ordered m-major then x,y,z.  Replaces depose_vector
- * (grid_methods_cl.py:266-290, grid_deposit_m0.cl:148-277,
+ * (grid_methods_cl.py:71-95, grid_deposit_m0.cl:148-277,
  * grid_deposit_m1.cl:171-327). */
 int ccl_deposit_vector(int dtype, int M, const uint32_t *sort_indx,
                        const uint32_t *cell_offset, const void *x,
@@ -190,12 +192,12 @@ int ccl_deposit_vector_lo(int dtype, int M, const uint32_t *sort_indx,
 /* Axis treatment (row 1 -= row 0) then multiplication by dV_inv[ir] for
  * nfld fields of M+1 modes (flds: nfld*(M+1) pointers, field-major).
  * Replaces postproc_depose_scalar / postproc_depose_vector
- * (grid_methods_cl.py:293-346, grid_generic.cl:4-59). */
+ * (grid_methods_cl.py:98-151, grid_generic.cl:4-59). */
 int ccl_deposit_postproc(int dtype, int M, int nfld, void *const *flds,
                          int Nx, int Nr, const void *dV_inv, void *stream);
 
 /* Ghost row 0 = +row 1 (m=0) or -row 1 (m>=1) for nfld fields.
- * Replaces preproc_project_vec (grid_methods_cl.py:348-361,
+ * Replaces preproc_project_vec (grid_methods_cl.py:153-166,
  * grid_generic.cl:63-86). */
 int ccl_warp_axis(int dtype, int M, int nfld, void *const *flds, int Nx,
                   void *stream);
@@ -204,7 +206,7 @@ int ccl_warp_axis(int dtype, int M, int nfld, void *const *flds, int Nx,
  * Ex,Ey,Ez,Bx,By,Bz) and Boris push of u, g_inv, for the np particles of
  * sort_indx; particles with number >= *np_stay are skipped as in the
  * reference.  factor_push = 2 pi dt q/m.  Replaces _gather_and_push
- * (grid_methods_cl.py:363-387, grid_deposit_m0.cl:280-427,
+ * (grid_methods_cl.py:168-192, grid_deposit_m0.cl:280-427,
  * grid_deposit_m1.cl:330-511). */
 int ccl_gather_push(int dtype, int M, long np, const void *x, const void *y,
                     const void *z, void *px, void *py, void *pz, void *g_inv,
@@ -274,7 +276,7 @@ int ccl_fft_backward_rows(int dtype, int nrows, int nx, const void *in,
  * ix > nx-nf, also applied to rs row 0), then half forward transform (FFT,
  * phase phs_minus) back into `spec`.  Replaces damp_fields for one component
  * (solver.py:32-35, transformer_methods_cl.py:385-455,
- * solver_methods_cl.py:389-408, solver_ms_pic.cl:5-55). */
+ * solver_methods_cl.py:64-83, solver_ms_pic.cl:5-55). */
 int ccl_damp_rows(int dtype, int nrows, int nx, void *spec, void *rs,
                   int rs_real, const void *phs_plus, const void *phs_minus,
                   const void *profile, int nf, void *stream);
@@ -355,7 +357,7 @@ int ccl_wait_probe(long spins, int arrive, int *gave_up, void *stream);
 /* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
  * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,
  * dN0_x..z, dN1_x..z; c1 = cos(w dt), c2 = sin(w dt) w, c3 = 1/w^2 (real).
- * Replaces advance_fields -> advance_e_g_m (solver_methods_cl.py:368-387,
+ * Replaces advance_fields -> advance_e_g_m (solver_methods_cl.py:43-62,
  * solver_ms_pic.cl:57-143). */
 int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
                       const void *c2, const void *c3, void *const *flds,

@@ -198,7 +198,7 @@ class RefKernels:
     """The reference's own OpenCL kernels, compiled unchanged as C++ (serial).
 
     Launch sizes follow the reference's methods layer: deposits run the four
-    colour offsets over NxNr_4 work-items each (grid_methods_cl.py:239-290),
+    colour offsets over NxNr_4 work-items each (grid_methods_cl.py:44-95),
     everything else one work-item per element."""
 
     name = "ref"

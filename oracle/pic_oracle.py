@@ -174,7 +174,7 @@ class OGrid:
         self._postproc(["J" + c for c in VEC])
 
     def _postproc(self, names):
-        # grid_methods_cl.py:293-346: axis row, then 1/dV, per component
+        # grid_methods_cl.py:98-151: axis row, then 1/dV, per component
         A, D, K = self.Args, self.D, self.K
         for f in names:
             arrs = [D[f + "_m" + str(m)] for m in range(A["M"] + 1)]
