@@ -166,6 +166,58 @@ def compare_runs(cfg, run, ref):
             "at_step": ref["loop"].it}
 
 
+FULL_RUN_STEPS = 500  # the single run's length
+
+
+def advance_to(run, n):
+    """Step a run (dict of build_run's objects) until its loop reaches step n."""
+    while run["loop"].it < n:
+        run["loop"].step()
+
+
+def full_run_accuracy(cfg, r32, r64, device_index=0):
+    """The mixed run against the FP64 run on the same seed at the end of the
+    full-length run (FULL_RUN_STEPS, or later if both are past it), beside
+    (a) the FP64 run's own sensitivity there -- the FP64 run with its
+    injected coordinates and weights rounded to FP32 (2^-24 relative),
+    against the FP64 run: with 2x1x4 particles per cell every radial
+    coordinate sits on a grid node, so cell indices and window exits of the
+    outermost rows are rounding ties -- and (b) the same comparison with
+    2x2x4 particles per cell (no ties)."""
+    import torch
+    n = max(FULL_RUN_STEPS, r32["loop"].it, r64["loop"].it)
+    advance_to(r32, n)
+    advance_to(r64, n)
+    torch.cuda.synchronize()
+    acc = compare_runs(cfg, r32, r64)
+    acc["layout"] = "x".join(map(str, cfg["eons_in"]["Nppc"]))
+    acc["electrons"] = {"mixed": int(r32["eons"].Args["Np"]), "fp64": int(r64["eons"].Args["Np"])}
+    keys = ("field_energy_rel_err", "wake_ex_rel_err", "kinetic_rel_err", "field_l2_rel_err")
+    alt = dict(zip(("solver", "eons", "ions", "loop"),
+                   build_run(cfg, "fp64", device_index, particles_cls=fp32_injected_particles())))
+    advance_to(alt, n)
+    torch.cuda.synchronize()
+    se = compare_runs(cfg, alt, r64)
+    acc["fp64_self_sensitivity"] = {k: se[k] for k in keys}
+    del alt
+    torch.cuda.empty_cache()
+    cfg2 = copy.deepcopy(cfg)
+    cfg2["eons_in"]["Nppc"] = (2, 2, 4)
+    pair = {}
+    for prec in ("fp64", "mixed"):
+        pair[prec] = dict(zip(("solver", "eons", "ions", "loop"),
+                              build_run(cfg2, prec, device_index)))
+        advance_to(pair[prec], n)
+    torch.cuda.synchronize()
+    a2 = compare_runs(cfg2, pair["mixed"], pair["fp64"])
+    acc2 = {k: a2[k] for k in keys + ("at_step",)}
+    acc2["layout"] = "2x2x4"
+    acc2["field_l2_rel_err_per_field"] = a2["field_l2_rel_err_per_field"]
+    del pair
+    torch.cuda.empty_cache()
+    return acc, acc2
+
+
 def wake_amplitude(ez_row, xgrid, x_laser, Lx):
     sel = xgrid < (x_laser - 2 * Lx)
     return float(np.abs(ez_row[sel]).max()) if sel.any() else float("nan")
@@ -567,16 +619,9 @@ def run_ours(args):
     remove_probe(orig)
     prof = probe.summary()
     r64 = time_arm(cfg, "fp64", args.steps, args.warmup, local, dist)
-    # accuracy of the FP32 run vs the FP64 run at the same step
-    n_extra = args.steps + min(args.steps, 5)
-    for _ in range(n_extra - args.steps):
-        r64["loop"].step()
-    for _ in range(args.steps):  # e2e advanced the FP32 run by `steps`
-        r64["loop"].step()
-    torch.cuda.synchronize()
-    acc = {}
-    if r32["loop"].it == r64["loop"].it:
-        acc = compare_runs(cfg, r32, r64)
+    # accuracy of the mixed run vs the FP64 run at the end of the full run
+    # (untimed: both runs are stepped on to the workload's 500 steps)
+    acc, acc2 = ({}, {}) if args.no_accuracy else full_run_accuracy(cfg, r32, r64, local)
     ms32 = reduce_max(dist, r32["ms"], dev)
     ms64 = reduce_max(dist, r64["ms"], dev)
     np32 = reduce_sum(dist, r32["np_sum"], dev)
@@ -597,6 +642,7 @@ def run_ours(args):
                      "gpu_launches": r64["launches"]},
             "mixed_over_fp64": value / v64,
             "mixed_vs_fp64_error": acc,
+            "mixed_vs_fp64_error_2x2x4": acc2,
             "e2e": {"value": e2e_np / e2e_s, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
             "gpu_launches": r32["launches"],
@@ -606,6 +652,13 @@ def run_ours(args):
             "kernel_probe": {k: {"launches": v["launches"], "ms_total": round(v["ms_total"], 4)}
                              for k, v in prof.items()},
         }
+        if world == 1 and not args.no_extra_workloads:
+            # the large-mode and batched workloads, with few steps each, and
+            # the differentiable run's adjoint
+            line["large_modes"] = large_modes_line(min(args.steps, 10), 3, args.batch_seed)
+            line["batched"] = batched_line(args.batch_runs, min(args.steps, 20), 3,
+                                           args.batch_seed)
+            line["adjoint"] = adjoint_line()
         if world == 1 and not args.no_cpu_baseline:
             rate, cores, t = cpu_oracle_rate(cfg, steps=args.cpu_steps, warmup=1)
             line["cpu_baseline"] = {"value": rate, "unit": "particle-steps/s", "cores": cores,
@@ -642,13 +695,23 @@ def large_modes_workload(seed=0):
 
 
 def run_large_modes(args):
+    print(json.dumps(large_modes_line(args.steps, args.warmup, args.batch_seed)))
+    return 0
+
+
+def large_modes_line(steps, warmup, seed):
     """The large-mode run in the mixed form and in FP64 on the same seed:
     device-timed steps of each (CUDA events, after the warm-up) and the
     mixed run's relative error against the FP64 run per field (E, B, rho of
     each mode, pointwise L2) and in the integrated diagnostics at the same
     step."""
     import torch
-    cfg = large_modes_workload(seed=args.batch_seed)
+
+    class _A:
+        pass
+    args = _A()
+    args.steps, args.warmup = steps, warmup
+    cfg = large_modes_workload(seed=seed)
     r32 = time_arm(cfg, "mixed", args.steps, args.warmup, 0, None)
     r64 = time_arm(cfg, "fp64", args.steps, args.warmup, 0, None)
     torch.cuda.synchronize()
@@ -667,10 +730,12 @@ def run_large_modes(args):
                  "ms_per_step": r64["ms"] / args.steps},
         "mixed_over_fp64": (r32["np_sum"] / r32["ms"]) / (r64["np_sum"] / r64["ms"]),
         "mixed_vs_fp64_error": compare_runs(cfg, r32, r64),
+        "gpu_launches": r32["launches"],
         "clocks": r32["clocks"],
     }
-    print(json.dumps(line))
-    return 0
+    del r32, r64
+    torch.cuda.empty_cache()
+    return line
 
 
 BATCHED_WORKLOAD = "lpa_batched_uneven_64"
@@ -704,6 +769,11 @@ def batched_cases(n=64, seed=0):
 
 
 def run_batched(args):
+    print(json.dumps(batched_line(args.batch_runs, args.steps, args.warmup, args.batch_seed)))
+    return 0
+
+
+def batched_line(nruns, steps, warmup, seed):
     """Aggregate electron particle-steps/s of the batched workload through
     PIC_batch in both of its modes -- each run's step on its own stream, and
     the whole batch step as one CUDA graph -- with the lane count picked by
@@ -712,7 +782,11 @@ def run_batched(args):
     import torch
     from chimeracl_gb300.batch import PIC_batch
     from chimeracl_gb300 import _lib
-    cases = batched_cases(args.batch_runs, seed=args.batch_seed)
+    class _A:
+        pass
+    args = _A()
+    args.steps, args.warmup = steps, warmup
+    cases = batched_cases(nruns, seed=seed)
     runs = [build_run(c, "mixed") for c in cases]
     loops = [r[3] for r in runs]
 
@@ -725,17 +799,25 @@ def run_batched(args):
         torch.cuda.synchronize()
         return bt
 
-    def timed(fn):
+    def kernels_run(bts):
+        # library kernels launched eagerly or replayed from graphs (the
+        # loops' own graphs and the batches' one-graph captures)
+        objs = list(loops) + list(bts)
+        return (_lib.launch_count()
+                - sum(o.graph_kernels_captured for o in objs)
+                + sum(o.graph_kernels_replayed for o in objs))
+
+    def timed(fn, bts=()):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        n0 = _lib.launch_count()
+        n0 = kernels_run(bts)
         with ClockSampler(0) as clk:
             time.sleep(0.3)
             e0.record()
             np_sum = fn()
             e1.record()
             torch.cuda.synchronize()
-        return np_sum, e0.elapsed_time(e1), _lib.launch_count() - n0, clk.summary()
+        return np_sum, e0.elapsed_time(e1), kernels_run(bts) - n0, clk.summary()
 
     def batched(bt):
         def fn():
@@ -757,13 +839,13 @@ def run_batched(args):
     # each run's step on its own stream (three graph replays per run), then
     # the whole batch step as one graph, then the runs one by one
     b = tuned(False)
-    nb, msb, lb, clk = timed(batched(b))
+    nb, msb, lb, clk = timed(batched(b), [b])
     bg = tuned(True)
-    ng, msg, lg, _ = timed(batched(bg))
+    ng, msg, lg, _ = timed(batched(bg), [bg])
     n1, ms1, l1, _ = timed(alone)
-    modes = {"streams": (nb, msb, b), "one_graph": (ng, msg, bg)}
+    modes = {"streams": (nb, msb, b, lb), "one_graph": (ng, msg, bg, lg)}
     best = max(modes, key=lambda m: modes[m][0] / modes[m][1])
-    nb, msb, b = modes[best]
+    nb, msb, b, lb = modes[best]
     line = {
         "metric": "electron particle-steps/s (batched runs)", "value": nb / (msb * 1e-3),
         "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -782,10 +864,74 @@ def run_batched(args):
         "one_by_one": {"value": n1 / (ms1 * 1e-3), "ms_per_step": ms1 / args.steps},
         "batched_over_one_by_one": (nb / msb) / (n1 / ms1),
         "one_graph_replays": bg.graph_replays,
+        "gpu_launches": lb,
         "clocks": clk,
     }
-    print(json.dumps(line))
-    return 0
+    del runs, loops, b, bg, modes
+    torch.cuda.empty_cache()
+    return line
+
+
+ADJOINT_WORKLOAD = "lpa_differentiable_1024x128_100steps"
+
+
+def adjoint_line(seed=0, nsteps=100, every=10, precision="mixed"):
+    """The differentiable run (1024 x 128 on the 512 x 64 run's window, m =
+    0, 1, 2x2x4 per cell, a0 = 2 laser, 32 density knots, 100 steps): the
+    plain forward step (graph replays, no checkpoints) against the adjoint:
+    the forward with a checkpoint every `every` steps and the reverse sweep
+    (each segment recomputed from its checkpoint, then stepped backwards),
+    per step; the gradients of the wake loss w.r.t. (a0, w0, x_foc)."""
+    import torch
+    from chimeracl_gb300.adjoint import build_problem_run, differentiable_problem
+    problem, params, knots = differentiable_problem(seed=seed, nsteps=nsteps, every=every,
+                                                    precision=precision)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    # the plain forward: warm-up, then the rest of the run timed
+    run = build_problem_run(problem, params, knots)
+    warm = 3
+    for _ in range(warm):
+        run["loop"].step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(nsteps - warm):
+        run["loop"].step()
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / (nsteps - warm)
+    del run
+    # forward with checkpoints, then the reverse sweep (twice: the first
+    # builds the library's lazily created tables and the reverse step's
+    # graphs' first captures; the second is timed)
+    run = build_problem_run(problem, params, knots)
+    adj = run["adjoint"]
+    _, t_fwd = timed(lambda: adj.run(nsteps))
+    loss = float(adj.wake_loss(problem["loss_width"]))
+    adj.gradients(problem["loss_width"])
+    (g_laser, g_knots), t_bwd = timed(lambda: adj.gradients(problem["loss_width"]))
+    adj.profile_phases = True
+    adj.gradients(problem["loss_width"])
+    phases = {k: round(1e3 * v / nsteps, 4) for k, v in adj.timing.items()}
+    line = {"workload": ADJOINT_WORKLOAD, "precision": precision, "steps": nsteps,
+            "checkpoint_every": every, "loss": loss,
+            "forward_ms_per_step": fwd_ms,
+            "forward_with_checkpoints_ms_per_step": 1e3 * t_fwd / nsteps,
+            "adjoint_ms_per_step": 1e3 * t_bwd / nsteps,
+            "adjoint_over_forward": (1e3 * t_bwd / nsteps) / fwd_ms,
+            "adjoint_phases_ms_per_step": phases,
+            "grad_a0_w0_xfoc": [float(v) for v in g_laser],
+            "grad_knots_max": float(np.abs(g_knots).max())}
+    del run, adj
+    torch.cuda.empty_cache()
+    return line
 
 
 def fp32_injected_particles():
@@ -853,12 +999,18 @@ def main(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the full-length mixed-vs-FP64 comparison")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="skip the large-mode and batched lines of the default run")
     ap.add_argument("--accuracy", action="store_true",
                     help="run the mixed-vs-FP64 accuracy study instead of the benchmark")
     ap.add_argument("--acc-steps", type=int, default=608)
-    ap.add_argument("--workload", default="single", choices=["single", "batched", "large_modes"],
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "batched", "large_modes", "adjoint"],
                     help="batched: 64 small uneven runs through PIC_batch; large_modes: "
-                         "the 4096 x 512, m = 0..2 run, mixed against FP64 (1 GPU)")
+                         "the 4096 x 512, m = 0..2 run, mixed against FP64 (1 GPU); "
+                         "adjoint: the differentiable run's forward and reverse sweep")
     ap.add_argument("--batch-runs", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=0)
     args = ap.parse_args(argv)
@@ -872,6 +1024,9 @@ def main(argv=None):
         return run_batched(args)
     if args.workload == "large_modes":
         return run_large_modes(args)
+    if args.workload == "adjoint":
+        print(json.dumps(adjoint_line()))
+        return 0
     return run_ours(args)
 
 

@@ -80,6 +80,24 @@ SIGNATURES = {
     "ccl_cast_c2d": [_i, _l, _vp, _vp, _vp],
     "ccl_profile_edges": [_i, _i, _i, _i, _vp, _vp, _i, _vp],
     "ccl_multiply_by_phase": [_i, _i, _i, _vp, _vp, _vp],
+    # adjoint of the step
+    "ccl_deposit_adjoint": [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
+                            _i, _d, _d, _i, _d, _d, _pp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                            _vp, _vp],
+    "ccl_gather_push_adjoint": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i,
+                                _d, _d, _i, _d, _d, _pp, _pp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                _vp, _vp],
+    "ccl_push_x_adjoint": [_i, _l] + [_vp] * 11 + [_d, _vp],
+    "ccl_psatd_adjoint": [_i, _l, _vp, _vp, _pp, _vp],
+    "ccl_grad_combine_adjoint": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _vp],
+    "ccl_rot_combine_adjoint": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _pp, _vp],
+    "ccl_modes_adjoint_accumulate": [_i, _i, _i, _i, _i, _pp, _pp, _pp, _pp, _vp],
+    "ccl_add_batch": [_i, _i, _vp, _pp, _pp, _vp],
+    "ccl_copy_batch": [_i, _vp, _pp, _pp, _vp],
+    "ccl_deposit_postproc_adjoint": [_i, _i, _i, _pp, _i, _i, _vp, _vp],
+    "ccl_warp_axis_adjoint": [_i, _i, _i, _pp, _i, _vp],
+    "ccl_align_adjoint": [_i, _l, _i, _pp, _pp, _vp, _vp],
+    "ccl_dens_profile_adjoint": [_i, _l, _vp, _vp, _vp, _vp, _vp, _vp, _u32, _vp, _vp],
 }
 
 _lib = None

@@ -446,6 +446,134 @@ int ccl_profile_edges(int dtype, int cplx, int nrows, int nx, void *a,
 int ccl_multiply_by_phase(int dtype, int nrows, int nx, void *a,
                           const void *phs, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Adjoint of the step (reverse mode: gradients of a loss of the final */
+/* fields with respect to the laser and the density profile).  The     */
+/* reference has no adjoint: each entry point is the transpose of the  */
+/* forward operation cited, for the same particles and cells (the      */
+/* forward's cell sort is reused).  Adjoints of complex arrays are     */
+/* stored like the arrays, (dL/dRe, dL/dIm).                           */
+/* ------------------------------------------------------------------ */
+
+/* Transpose of the charge (vec = 0) or current (vec = 1) deposit
+ * (grid_methods_cl.py:44-95, grid_deposit_m1.cl:20-327): a gather of the
+ * node adjoints `lam` (the deposit targets' adjoints before the
+ * post-processing; vec: 3(M+1) pointers m-major then x, y, z, else M+1)
+ * with the shape functions and their derivatives.  Adds to lw and, when
+ * lx, ly, lz are given (all or none), to the position adjoints; vec also
+ * adds to lux, luy, luz, lg (adjoints of momenta and g_inv).  sort_indx,
+ * cell_offset: the forward's sort at the same positions. */
+int ccl_deposit_adjoint(int dtype, int vec, int M, const uint32_t *sort_indx,
+                        const uint32_t *cell_offset, const void *x, const void *y,
+                        const void *z, const void *ux, const void *uy, const void *uz,
+                        const void *g_inv, const void *w, int charge, int Nx, double xmin,
+                        double dx_inv, int Nr, double rmin, double dr_inv, void *const *lam,
+                        void *lx, void *ly, void *lz, void *lw, void *lux, void *luy,
+                        void *luz, void *lg, void *stream);
+
+/* Transpose of the gather + Boris push (grid_methods_cl.py:168-192,
+ * grid_deposit_m1.cl:330-511) for the particles the forward pushed (those
+ * of the valid cells of cell_offset whose number is below *np_stay).  flds:
+ * the real-space E, B the forward gathered (6(M+1) pointers, m-major then
+ * Ex, Ey, Ez, Bx, By, Bz, after the ghost rows); lflds: their adjoints,
+ * added to.  ux_old..: momenta before the push.  On entry lux, luy, luz,
+ * lg hold the adjoints of the pushed momenta and g_inv; for each pushed
+ * particle they become the adjoints of the momenta before the push (lg 0),
+ * and lx, ly, lz are added to. */
+int ccl_gather_push_adjoint(int dtype, int M, const void *x, const void *y, const void *z,
+                            const void *ux_old, const void *uy_old, const void *uz_old,
+                            const uint32_t *sort_indx, const uint32_t *cell_offset,
+                            const uint32_t *np_stay, double factor_push, int Nx, double xmin,
+                            double dx_inv, int Nr, double rmin, double dr_inv,
+                            const void *const *flds, void *const *lflds, void *lx, void *ly,
+                            void *lz, void *lux, void *luy, void *luz, void *lg,
+                            void *stream);
+
+/* Transpose of push_xyz (particles_methods_cl.py:206-223,
+ * particles_generic.cl:129-153): lu += dt g_inv lx, lg += dt (lx . u). */
+int ccl_push_x_adjoint(int dtype, long np, const void *ux, const void *uy, const void *uz,
+                       const void *g_inv, const void *lx, const void *ly, const void *lz,
+                       void *lux, void *luy, void *luz, void *lg, double dt, void *stream);
+
+/* Transpose of the PSATD update (solver_methods_cl.py:43-62,
+ * solver_ms_pic.cl:57-143) in one mode, with the eight coefficients per
+ * cell of ccl_psatd_advance_split (both precisions' updates are this
+ * linear map).  flds: 15 pointers -- lE xyz, lG xyz (in: adjoints of the
+ * updated fields; out: of the fields before the update), lJ xyz (written;
+ * times `filter` per cell when it is not NULL: the transpose of the
+ * smoothing filter of fields_smooth, transformer_methods_cl.py:79-85),
+ * lN0 xyz (written), lN1 xyz (added to). */
+int ccl_psatd_adjoint(int dtype, long ncells, const void *coef, const void *filter,
+                      void *const *flds, void *stream);
+
+/* Transpose of the gradient's combine step (transformer_methods_cl.py:
+ * 87-133, ccl_grad_combine), first half: from the gradient adjoints ldN
+ * (3(M+1), m-major, x y z) writes lrho[m] = -i kx ldN_x (the direct term)
+ * and the operands of the transposed radial products: Pm[m] (for
+ * dDHT_minus_m^T; for m = 0 through the m=-1 mirror) and Pp[m] (for
+ * dDHT_plus_m^T), NULL where the forward has no such term.  The products
+ * are then added by ccl_modes_adjoint_accumulate (ncomp 1). */
+int ccl_grad_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx,
+                             const void *const *ldN, void *const *lrho, void *const *Pm,
+                             void *const *Pp, void *stream);
+
+/* Transpose of the curl's combine step with the Poisson factor
+ * (transformer_methods_cl.py:185-263, 66-71, ccl_rot_combine), first
+ * half: adds the direct i kx terms of the B adjoints lB to lG and writes
+ * the operands Qm, Qp (3(M+1) each, NULL for absent modes) of the
+ * transposed radial products, added by ccl_modes_adjoint_accumulate
+ * (ncomp 3). */
+int ccl_rot_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx,
+                            const void *const *poiss, const void *const *lB, void *const *lG,
+                            void *const *Qm, void *const *Qp, void *stream);
+
+/* Second half of both: lo[j] += Rm[j+1] + Rp[j-1] (+ Rm[0] for j = 1)
+ * per component, where Rm[m] = dDHT_minus_m^T Pm[m] and Rp[m] =
+ * dDHT_plus_m^T Pp[m] (ncomp arrays per mode; NULL where absent); then
+ * lo[j] *= filt[j] where filt (M+1 real arrays) is not NULL. */
+int ccl_modes_adjoint_accumulate(int dtype, int M, int ncomp, int nrows, int nx,
+                                 void *const *lo, const void *const *Rm,
+                                 const void *const *Rp, const void *const *filt,
+                                 void *stream);
+
+/* dst[a][i] += src[a][i] for i < n[a] reals, a < narr <= 32, one launch.
+ * No counterpart in the reference (the adjoint's accumulations of
+ * transformed adjoints; append_c2c, generic.cl:18-29, per array). */
+int ccl_add_batch(int dtype, int narr, const long *n, void *const *dst, const void *const *src,
+                  void *stream);
+
+/* dst[a] <- src[a] (nbytes[a] bytes, a multiple of 4; 4-byte aligned) for
+ * a < narr <= 32, one launch.  No counterpart in the reference: the
+ * adjoint's records of forward steps and its per-step inputs. */
+int ccl_copy_batch(int narr, const long *nbytes, void *const *dst, const void *const *src,
+                   void *stream);
+
+/* Transpose of the deposit post-processing (grid_methods_cl.py:98-151,
+ * grid_generic.cl:4-59), in place: row 0 <- row 0 dV_inv[0] - row 1
+ * dV_inv[1], row ir <- row ir dV_inv[ir] for ir >= 1. */
+int ccl_deposit_postproc_adjoint(int dtype, int M, int nfld, void *const *flds, int Nx, int Nr,
+                                 const void *dV_inv, void *stream);
+
+/* Transpose of the ghost rows (grid_methods_cl.py:153-166,
+ * grid_generic.cl:63-86), in place: row 1 += (m = 0) or -= (m >= 1)
+ * row 0, then row 0 = 0. */
+int ccl_warp_axis_adjoint(int dtype, int M, int nfld, void *const *flds, int Nx, void *stream);
+
+/* Transpose of align (particles_methods_cl.py:263-286,
+ * particles_generic.cl:156-169): dst[c][sort_indx[i]] = src[c][i] for
+ * i < n; entries of dst that no index names are left as they are. */
+int ccl_align_adjoint(int dtype, long n, int ncomp, void *const *src, void *const *dst,
+                      const uint32_t *sort_indx, void *stream);
+
+/* Transpose of the density profile (particles_methods_cl.py:179-204,
+ * particles_generic.cl:6-30) with respect to its knot values: the weights
+ * w = w0 f(x) of np particles, f piecewise linear through (xx[k], ff[k]);
+ * lff[k] += sum_i lw[i] w[i] / f(x_i) df/dff[k](x_i) (double; 2 <= nloc <=
+ * 256 knots, as ccl_dens_profile takes them). */
+int ccl_dens_profile_adjoint(int dtype, long np, const void *x, const void *w, const void *lw,
+                             const double *xx, const double *ff, const double *dxm1,
+                             uint32_t nloc, double *lff, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

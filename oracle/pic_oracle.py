@@ -645,8 +645,11 @@ class OLoop:
 def diagnostics(solver, species):
     """Integrated diagnostics (defined identically for the oracle and the
     product): field energy  sum_m w_m sum (|E|^2+|B|^2) 2 pi r dr dx  over the
-    physical rows r > 0 (w_0 = 1, w_m>=1 = 2); on-axis Ez wake amplitude
-    max |Ez_m0[1, :]| over ix < ix_cut; kinetic energy sum w (gamma - 1) of the
+    physical rows r > 0 (w_0 = 1, w_m>=1 = 2); on-axis amplitudes
+    max |Ez_m0[1, :]| (the laser's polarisation component: x is the
+    propagation axis in these arrays) and max |Ex_m0[1, :]| (the longitudinal
+    field on the axis, the plasma wake: a linearly polarised laser has no
+    mode-0 longitudinal field); kinetic energy sum w (gamma - 1) of the
     mobile species."""
     A, D = solver.Args, solver.D
     r = A["Rgrid"][1:, None]
@@ -659,12 +662,14 @@ def diagnostics(solver, species):
                 a = D[f + c + "_m" + str(m)][1:]
                 We += wm * float((np.abs(a) ** 2 * vol).sum())
     ez = np.abs(D["Ez_m0"][1])
+    ex = np.abs(D["Ex_m0"][1])
     kin = 0.0
     for p in species:
         if "Immobile" in p.Args or p.Args["Np"] == 0:
             continue
         kin += float((p.D["w"] * (1.0 / p.D["g_inv"] - 1.0)).sum())
-    return {"field_energy": We, "ez_axis_max": float(ez.max()), "kinetic": kin}
+    return {"field_energy": We, "ez_axis_max": float(ez.max()), "wake_ex_max": float(ex.max()),
+            "kinetic": kin}
 
 
 def build_lpa(grid_in, eons_in, frame_in=None, laser_in=None, prefill=None, K=None, seed=0,

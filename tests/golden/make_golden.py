@@ -30,9 +30,13 @@ FULL_RUNS = {
 }
 
 # the 2048 x 256, M = 1 single run (2x1x4 per cell, density up-ramp over the
-# window's first 20 lambda0, a0 = 3 laser), 3 steps from its first injection
+# window's first 20 lambda0, a0 = 3 laser), 3 steps from its first injection;
+# and the same run with 2x2x4 per cell (no particle on a grid node: with one
+# radial particle per cell every radius is a rounding tie between two cells,
+# which the injector's last-bit sin/cos rounding decides)
 BENCH_RUNS = {
     "lpa_m1_2048x256_3steps.npz": dict(nsteps=3, seed=1000),
+    "lpa_m1_2048x256_2x2x4_3steps.npz": dict(nsteps=3, seed=1000, nppc=(2, 2, 4)),
 }
 
 # further grid shapes: 1024 x 128 on the 512 x 64 run's window (the
@@ -138,7 +142,10 @@ def main():
 
 def bench_cfg(case):
     import bench
-    return bench.workload(seed=case["seed"])
+    cfg = bench.workload(seed=case["seed"])
+    if "nppc" in case:
+        cfg["eons_in"]["Nppc"] = tuple(case["nppc"])
+    return cfg
 
 
 def main_only(names):

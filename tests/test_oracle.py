@@ -174,6 +174,7 @@ def test_oracle_reproduces_golden(K, name):
 
 
 @pytest.mark.parametrize("name", ["lpa_m1_512x64_200steps.npz", "lpa_m1_2048x256_3steps.npz",
+                                  "lpa_m1_2048x256_2x2x4_3steps.npz",
                                   "lpa_m1_1024x128_20steps.npz", "lpa_m1_384x96_30steps.npz"])
 def test_oracle_reproduces_full_run_golden(K, name):
     """Runs of the reference's own kernels reproduced by the C restatement:
