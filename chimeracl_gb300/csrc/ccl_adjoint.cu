@@ -276,6 +276,14 @@ __device__ __forceinline__ void cross3(const T a[3], const T b[3], T o[3]) {
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+// One thread per cell of a 32 x 8-cell tile (the forward deposit's
+// decomposition): the thread walks its cell's particles in sort order,
+// reverses each particle's push, and sums the particle's field adjoints on
+// the cell's 4 corner nodes in registers; the sums are added to the tile's
+// node accumulators in shared memory in four phases, one per cell colour
+// (ix & 1) + 2 (ir & 1) -- cells of one colour share no node, so no atomics --
+// and the tile's nodes go to the global adjoints with one atomic each (the
+// border nodes are shared with the neighbouring tiles).
 template <typename T, int M>
 __global__ void __launch_bounds__(AT_THREADS)
     k_gather_push_adj(const T *__restrict__ x, const T *__restrict__ y,
@@ -290,14 +298,9 @@ __global__ void __launch_bounds__(AT_THREADS)
   extern __shared__ __align__(16) unsigned char adj_sm[];
   T *fsm = (T *)adj_sm;                     // [AT_NR][AT_NX][NS] fields (m >= 1 doubled)
   T *asm_ = fsm + AT_NR * AT_NX * NS;       // the same layout: adjoint accumulators
-  __shared__ TileRows tr;
-  __shared__ typename AdjEdge<T>::type xedge[AT_TX], redge[AT_TR];
-  const int Nx = g.Nx, Nr = g.Nr;
+  const int Nx = g.Nx, Nr = g.Nr, nxc = Nx - 1;
   const int nx0 = blockIdx.x * AT_TX, nr0 = blockIdx.y * AT_TR;
   const u32 np_stay = *np_stay_p;
-  if (threadIdx.x < AT_TX) xedge[threadIdx.x] = adj_x_edge(g, nx0 + threadIdx.x);
-  else if (threadIdx.x < AT_TX + AT_TR)
-    redge[threadIdx.x - AT_TX] = adj_r_edge(g, nr0 + threadIdx.x - AT_TX);
   for (int t = threadIdx.x; t < AT_NR * AT_NX; t += AT_THREADS) {
     const int lr = t / AT_NX, lc = t - lr * AT_NX;
     const int nr = nr0 + lr, nx = nx0 + lc;
@@ -318,147 +321,166 @@ __global__ void __launch_bounds__(AT_THREADS)
 #pragma unroll
     for (int q = 0; q < NS; q++) a[q] = T(0);
   }
-  tile_rows(tr, cell_off, Nx, Nr, nx0, nr0);
-  const u32 total = tr.pre[AT_TR];
+  __syncthreads();
+  const int tx = threadIdx.x % AT_TX, ty = threadIdx.x / AT_TX;
+  const int ix = nx0 + tx, ir = nr0 + ty;
+  const bool valid = ix > 0 && ix < Nx - 2 && ir >= 0 && ir < Nr - 2;
+  T acc[4][NS];
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+#pragma unroll
+    for (int q = 0; q < NS; q++) acc[c][q] = T(0);
+  const int l0 = (ty * AT_NX + tx) * NS;
+  const int loff[4] = {l0, l0 + NS, l0 + AT_NX * NS, l0 + (AT_NX + 1) * NS};
   const T h = T(0.5) * dt;
-  for (u32 idx = threadIdx.x; idx < total; idx += AT_THREADS) {
-    int row;
-    u32 pos;
-    tile_item(tr, idx, row, pos);
-    const u32 p = sort_indx[pos];
-    if (p >= np_stay) continue;  // not pushed by the forward
-    const T xp = x[p], yp = y[p], zp = z[p];
-    const T rp = sqrt(yp * yp + zp * zp);
-    int ix = (int)floor((xp - g.xmin) * g.dx_inv);
-    ix = ix < tr.ixl ? tr.ixl : (ix > tr.ixh ? tr.ixh : ix);
-    const T sX1 = adj_frac(xp, xedge[ix - nx0], g.xmin, g.dx_inv);
-    const T sR1 = adj_frac(rp, redge[row], g.rmin, g.dr_inv);
-    PGeom<T, M> pg;
-    pgeom<T, M>(pg, xp, yp, zp, sX1, sR1, g.dx_inv, g.dr_inv);
-    const int l0 = (row * AT_NX + (ix - nx0)) * NS;
-    const int loff[4] = {l0, l0 + NS, l0 + AT_NX * NS, l0 + (AT_NX + 1) * NS};
-    // fields at the particle, their x, r and phi derivatives
-    T fld[6], fx[6], fr[6], fph[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      fld[k] = fx[k] = fr[k] = fph[k] = T(0);
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const T *d = fsm + loff[c];
-        T Fv = d[k], Dv = T(0);
-#pragma unroll
-        for (int m = 1; m <= M; m++) {
-          const T re = d[6 + 12 * (m - 1) + 2 * k], im = d[6 + 12 * (m - 1) + 2 * k + 1];
-          Fv += re * pg.cs[m] + im * pg.sn[m];
-          Dv += T(m) * (im * pg.cs[m] - re * pg.sn[m]);
-        }
-        fld[k] += pg.C[c] * Fv;
-        fx[k] += pg.Cx[c] * Fv;
-        fr[k] += pg.Cr[c] * Fv;
-        fph[k] += pg.C[c] * Dv;
-      }
-    }
-    // Boris push, forward (its intermediates)
-    const T u[3] = {uxo[p], uyo[p], uzo[p]};
-    T um[3], t[3], sv[3], u0[3], up[3], un[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) um[k] = u[k] + h * fld[k];
-    const T gi0 = T(1) / sqrt(T(1) + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
-#pragma unroll
-    for (int k = 0; k < 3; k++) t[k] = h * fld[3 + k] * gi0;
-    const T f2 = T(2) / (T(1) + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-#pragma unroll
-    for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
-    cross3(um, t, u0);
-#pragma unroll
-    for (int k = 0; k < 3; k++) u0[k] += um[k];
-    cross3(u0, sv, up);
-#pragma unroll
-    for (int k = 0; k < 3; k++) up[k] += um[k];
-#pragma unroll
-    for (int k = 0; k < 3; k++) un[k] = up[k] + h * fld[k];
-    const T gn = T(1) / sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
-    // ... and reversed
-    T lun[3] = {lux[p], luy[p], luz[p]};
-    const T lgn = lg[p];
-    const T gg3 = -lgn * gn * gn * gn;
-#pragma unroll
-    for (int k = 0; k < 3; k++) lun[k] += gg3 * un[k];
-    T lE[3], lB[3], lum[3], lu0[3], lsv[3], lt[3], tmp[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      lE[k] = h * lun[k];
-      lum[k] = lun[k];  // up = um + u0 x sv
-    }
-    cross3(sv, lun, lu0);
-    cross3(lun, u0, lsv);
-    cross3(t, lu0, tmp);  // u0 = um + um x t
-#pragma unroll
-    for (int k = 0; k < 3; k++) lum[k] += lu0[k] + tmp[k];
-    cross3(lu0, um, lt);
-    T lf2 = T(0);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      lt[k] += f2 * lsv[k];  // sv = t f2
-      lf2 += t[k] * lsv[k];
-    }
-    const T cf = -lf2 * f2 * f2;  // f2 = 2 / (1 + |t|^2)
-    T lgi0 = T(0);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      lt[k] += cf * t[k];
-      lB[k] = h * gi0 * lt[k];  // t = h B gi0
-      lgi0 += h * fld[3 + k] * lt[k];
-    }
-    const T cg = -lgi0 * gi0 * gi0 * gi0;  // gi0 = (1 + |um|^2)^-1/2
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      lum[k] += cg * um[k];
-      lE[k] += h * lum[k];  // um = u + h E
-    }
-    lux[p] = lum[0];
-    luy[p] = lum[1];
-    luz[p] = lum[2];
-    lg[p] = T(0);
-    // position adjoint from the gathered fields' derivatives
-    const T lf[6] = {lE[0], lE[1], lE[2], lB[0], lB[1], lB[2]};
-    T sx = T(0), sr = T(0), sphi = T(0);
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      sx += lf[k] * fx[k];
-      sr += lf[k] * fr[k];
-      sphi += lf[k] * fph[k];
-    }
-    T a, b;
-    polar_to_yz<T, M>(pg, sr, sphi, a, b);
-    lx[p] += sx;
-    ly[p] += a;
-    lz[p] += b;
-    // field adjoints onto the tile's nodes (mode m >= 1: 2 C (cos, sin))
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      T *d = asm_ + loff[c];
+  if (valid) {
+    const long cg = (long)ix + (long)ir * nxc;
+    const u32 q0 = cell_off[cg], q1 = cell_off[cg + 1];
+    const typename AdjEdge<T>::type ex = adj_x_edge(g, ix), er = adj_r_edge(g, ir);
+    for (u32 q = q0; q < q1; q++) {
+      const u32 p = sort_indx[q];
+      if (p >= np_stay) continue;  // not pushed by the forward
+      const T xp = x[p], yp = y[p], zp = z[p];
+      const T rp = sqrt(yp * yp + zp * zp);
+      const T sX1 = adj_frac(xp, ex, g.xmin, g.dx_inv);
+      const T sR1 = adj_frac(rp, er, g.rmin, g.dr_inv);
+      PGeom<T, M> pg;
+      pgeom<T, M>(pg, xp, yp, zp, sX1, sR1, g.dx_inv, g.dr_inv);
+      // fields at the particle, their x, r and phi derivatives
+      T fld[6], fx[6], fr[6], fph[6];
 #pragma unroll
       for (int k = 0; k < 6; k++) {
-        const T v = pg.C[c] * lf[k];
-        atomicAdd(d + k, v);
+        fld[k] = fx[k] = fr[k] = fph[k] = T(0);
 #pragma unroll
-        for (int m = 1; m <= M; m++) {
-          atomicAdd(d + 6 + 12 * (m - 1) + 2 * k, T(2) * v * pg.cs[m]);
-          atomicAdd(d + 6 + 12 * (m - 1) + 2 * k + 1, T(2) * v * pg.sn[m]);
+        for (int c = 0; c < 4; c++) {
+          const T *d = fsm + loff[c];
+          T Fv = d[k], Dv = T(0);
+#pragma unroll
+          for (int m = 1; m <= M; m++) {
+            const T re = d[6 + 12 * (m - 1) + 2 * k], im = d[6 + 12 * (m - 1) + 2 * k + 1];
+            Fv += re * pg.cs[m] + im * pg.sn[m];
+            Dv += T(m) * (im * pg.cs[m] - re * pg.sn[m]);
+          }
+          fld[k] += pg.C[c] * Fv;
+          fx[k] += pg.Cx[c] * Fv;
+          fr[k] += pg.Cr[c] * Fv;
+          fph[k] += pg.C[c] * Dv;
         }
+      }
+      // Boris push, forward (its intermediates)
+      const T u[3] = {uxo[p], uyo[p], uzo[p]};
+      T um[3], t[3], sv[3], u0[3], up[3], un[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) um[k] = u[k] + h * fld[k];
+      const T gi0 = T(1) / sqrt(T(1) + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+#pragma unroll
+      for (int k = 0; k < 3; k++) t[k] = h * fld[3 + k] * gi0;
+      const T f2 = T(2) / (T(1) + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+#pragma unroll
+      for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
+      cross3(um, t, u0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) u0[k] += um[k];
+      cross3(u0, sv, up);
+#pragma unroll
+      for (int k = 0; k < 3; k++) up[k] += um[k];
+#pragma unroll
+      for (int k = 0; k < 3; k++) un[k] = up[k] + h * fld[k];
+      const T gn = T(1) / sqrt(T(1) + un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+      // ... and reversed
+      T lun[3] = {lux[p], luy[p], luz[p]};
+      const T lgn = lg[p];
+      const T gg3 = -lgn * gn * gn * gn;
+#pragma unroll
+      for (int k = 0; k < 3; k++) lun[k] += gg3 * un[k];
+      T lE[3], lB[3], lum[3], lu0[3], lsv[3], lt[3], tmp[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        lE[k] = h * lun[k];
+        lum[k] = lun[k];  // up = um + u0 x sv
+      }
+      cross3(sv, lun, lu0);
+      cross3(lun, u0, lsv);
+      cross3(t, lu0, tmp);  // u0 = um + um x t
+#pragma unroll
+      for (int k = 0; k < 3; k++) lum[k] += lu0[k] + tmp[k];
+      cross3(lu0, um, lt);
+      T lf2 = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        lt[k] += f2 * lsv[k];  // sv = t f2
+        lf2 += t[k] * lsv[k];
+      }
+      const T cf = -lf2 * f2 * f2;  // f2 = 2 / (1 + |t|^2)
+      T lgi0 = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        lt[k] += cf * t[k];
+        lB[k] = h * gi0 * lt[k];  // t = h B gi0
+        lgi0 += h * fld[3 + k] * lt[k];
+      }
+      const T cg0 = -lgi0 * gi0 * gi0 * gi0;  // gi0 = (1 + |um|^2)^-1/2
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        lum[k] += cg0 * um[k];
+        lE[k] += h * lum[k];  // um = u + h E
+      }
+      lux[p] = lum[0];
+      luy[p] = lum[1];
+      luz[p] = lum[2];
+      lg[p] = T(0);
+      // position adjoint from the gathered fields' derivatives
+      const T lf[6] = {lE[0], lE[1], lE[2], lB[0], lB[1], lB[2]};
+      T sx = T(0), sr = T(0), sphi = T(0);
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        sx += lf[k] * fx[k];
+        sr += lf[k] * fr[k];
+        sphi += lf[k] * fph[k];
+      }
+      T a, b;
+      polar_to_yz<T, M>(pg, sr, sphi, a, b);
+      lx[p] += sx;
+      ly[p] += a;
+      lz[p] += b;
+      // the field adjoints on the cell's corners (mode m >= 1: 2 C (cos, sin))
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          const T v = pg.C[c] * lf[k];
+          acc[c][k] += v;
+#pragma unroll
+          for (int m = 1; m <= M; m++) {
+            acc[c][6 + 12 * (m - 1) + 2 * k] += T(2) * v * pg.cs[m];
+            acc[c][6 + 12 * (m - 1) + 2 * k + 1] += T(2) * v * pg.sn[m];
+          }
+        }
+    }
+  }
+  // the corner sums onto the tile's nodes, colour by colour
+  const int colour = (ix & 1) + 2 * (ir & 1);
+#pragma unroll
+  for (int col = 0; col < 4; col++) {
+    __syncthreads();
+    if (valid && colour == col) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        T *a = asm_ + loff[c];
+#pragma unroll
+        for (int q = 0; q < NS; q++) a[q] += acc[c][q];
       }
     }
   }
   __syncthreads();
   // flush the tile's node adjoints (border nodes are shared with the
   // neighbouring tiles)
-  for (int t = threadIdx.x; t < AT_NR * AT_NX; t += AT_THREADS) {
-    const int lr = t / AT_NX, lc = t - lr * AT_NX;
+  for (int tt = threadIdx.x; tt < AT_NR * AT_NX; tt += AT_THREADS) {
+    const int lr = tt / AT_NX, lc = tt - lr * AT_NX;
     const int nr = nr0 + lr, nx = nx0 + lc;
     if (nr >= Nr || nx >= Nx) continue;
     const long node = (long)nr * Nx + nx;
-    const T *a = asm_ + t * NS;
+    const T *a = asm_ + tt * NS;
 #pragma unroll
     for (int k = 0; k < 6; k++)
       if (a[k] != T(0)) atomicAdd((T *)lF.p[k] + node, a[k]);
