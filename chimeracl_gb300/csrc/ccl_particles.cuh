@@ -495,11 +495,15 @@ static __global__ void __launch_bounds__(ST_THREADS)
 }
 
 // Fix-up of the cells the scatter flagged (claimed by more than one warp
-// group; a single group writes its items in ascending order): one thread per
-// cell, segments of up to FX_REG items sorted in registers by Batcher's
-// odd-even merge network, longer ones by insertion sort in place.  Every
-// other cell is left untouched without reading it.
-constexpr int FX_REG = 16;
+// group; a single group writes its items in ascending order).  A warp takes
+// 32 consecutive cells, one per lane: segments of up to FX_REG items are
+// sorted by their lane in registers (Batcher's odd-even merge network);
+// longer ones -- a dense bunch of the plasma, or a whole layout of
+// particles on cell faces -- by the whole warp, one at a time, with a
+// bitonic sort in shared memory (up to FX_BUF items; a longer segment, not
+// met in practice, by insertion sort in place).  Every other cell is left
+// untouched without reading it.
+constexpr int FX_REG = 16, FX_WARPS = 4, FX_BUF = 2048;
 
 __device__ __forceinline__ void cswap(u32 &a, u32 &b) {
   const u32 lo = a < b ? a : b, hi = a < b ? b : a;
@@ -507,14 +511,47 @@ __device__ __forceinline__ void cswap(u32 &a, u32 &b) {
   b = hi;
 }
 
-static __global__ void __launch_bounds__(256)
+// ascending sort of g[0 .. n) (distinct values) by the 32 lanes of a warp
+// through buf (FX_BUF words of shared memory)
+__device__ __forceinline__ void warp_bitonic_sort(u32 *__restrict__ g, u32 n, u32 *buf,
+                                                  int lane) {
+  u32 P = 32;
+  while (P < n) P <<= 1;
+  for (u32 i = lane; i < P; i += 32) buf[i] = i < n ? g[i] : 0xffffffffu;
+  __syncwarp();
+  for (u32 k = 2; k <= P; k <<= 1)
+    for (u32 j = k >> 1; j > 0; j >>= 1) {
+      for (u32 i = lane; i < P; i += 32) {
+        const u32 l = i ^ j;
+        if (l > i) {
+          const u32 a = buf[i], b = buf[l];
+          if ((a > b) == ((i & k) == 0)) {
+            buf[i] = b;
+            buf[l] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  for (u32 i = lane; i < n; i += 32) g[i] = buf[i];
+  __syncwarp();
+}
+
+static __global__ void __launch_bounds__(FX_WARPS * 32)
     k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, const u32 *__restrict__ multi,
                  u32 *__restrict__ sort_indx) {
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < (long)C;
-       c += (long)gridDim.x * blockDim.x) {
-    if (!(multi[c >> 5] & (1u << (c & 31)))) continue;
-    const u32 p0 = cell_offset[c], p1 = cell_offset[c + 1], n = p1 - p0;
-    if (n <= (u32)FX_REG) {
+  __shared__ u32 buf[FX_WARPS][FX_BUF];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long stride = (long)gridDim.x * FX_WARPS * 32;
+  for (long c0 = ((long)blockIdx.x * FX_WARPS + warp) * 32; c0 < (long)C; c0 += stride) {
+    const long c = c0 + lane;
+    const bool flagged = c < (long)C && (multi[c >> 5] & (1u << (c & 31)));
+    u32 p0 = 0, n = 0;
+    if (flagged) {
+      p0 = cell_offset[c];
+      n = cell_offset[c + 1] - p0;
+    }
+    if (flagged && n <= (u32)FX_REG) {
       u32 v[FX_REG];
 #pragma unroll
       for (int i = 0; i < FX_REG; i++) v[i] = (u32)i < n ? sort_indx[p0 + i] : 0xffffffffu;
@@ -530,15 +567,26 @@ static __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int i = 0; i < FX_REG; i++)
         if ((u32)i < n) sort_indx[p0 + i] = v[i];
-    } else {
-      for (u32 a = p0 + 1; a < p1; a++) {
-        const u32 v = sort_indx[a];
-        u32 b = a;
-        while (b > p0 && sort_indx[b - 1] > v) {
-          sort_indx[b] = sort_indx[b - 1];
-          b--;
-        }
-        sort_indx[b] = v;
+    }
+    unsigned big = __ballot_sync(0xffffffffu, flagged && n > (u32)FX_REG);
+    while (big) {
+      const int l = __ffs(big) - 1;
+      big &= big - 1;
+      const u32 q0 = __shfl_sync(0xffffffffu, p0, l), qn = __shfl_sync(0xffffffffu, n, l);
+      if (qn <= (u32)FX_BUF) {
+        warp_bitonic_sort(sort_indx + q0, qn, buf[warp], lane);
+      } else {
+        if (lane == 0)
+          for (u32 a = q0 + 1; a < q0 + qn; a++) {
+            const u32 v = sort_indx[a];
+            u32 b = a;
+            while (b > q0 && sort_indx[b - 1] > v) {
+              sort_indx[b] = sort_indx[b - 1];
+              b--;
+            }
+            sort_indx[b] = v;
+          }
+        __syncwarp();
       }
     }
   }
@@ -610,7 +658,8 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
                                                     sort_indx);
   CCL_LAUNCH_CHECK("scatter");
   if (C > 0)
-    k_cell_fixup<<<grid_for(C, 256), 256, 0, s>>>((u32)C, cell_offset, w.multi, sort_indx);
+    k_cell_fixup<<<grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s>>>((u32)C, cell_offset,
+                                                                       w.multi, sort_indx);
   CCL_LAUNCH_CHECK("cell_fixup");
   return CCL_OK;
 }
