@@ -497,18 +497,40 @@ static __global__ void __launch_bounds__(ST_THREADS)
 // Fix-up of the cells the scatter flagged (claimed by more than one warp
 // group; a single group writes its items in ascending order).  A warp takes
 // 32 consecutive cells, one per lane: segments of up to FX_REG items are
-// sorted by their lane in registers (Batcher's odd-even merge network);
+// sorted by their lane in registers (Batcher's odd-even merge network over
+// 16 or 32 inputs);
 // longer ones -- a dense bunch of the plasma, or a whole layout of
 // particles on cell faces -- by the whole warp, one at a time, with a
 // bitonic sort in shared memory (up to FX_BUF items; a longer segment, not
 // met in practice, by insertion sort in place).  Every other cell is left
 // untouched without reading it.
-constexpr int FX_REG = 16, FX_WARPS = 4, FX_BUF = 2048;
+constexpr int FX_REG = 32, FX_WARPS = 4, FX_BUF = 2048;
 
 __device__ __forceinline__ void cswap(u32 &a, u32 &b) {
   const u32 lo = a < b ? a : b, hi = a < b ? b : a;
   a = lo;
   b = hi;
+}
+
+// ascending sort of g[0 .. n), n <= N, by one thread in registers
+// (Batcher's odd-even merge network over N inputs)
+template <int N>
+__device__ __forceinline__ void reg_sort(u32 *__restrict__ g, u32 n) {
+  u32 v[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) v[i] = (u32)i < n ? g[i] : 0xffffffffu;
+#pragma unroll
+  for (int p = 1; p < N; p <<= 1)
+#pragma unroll
+    for (int k = p; k >= 1; k >>= 1)
+#pragma unroll
+      for (int j = k % p; j <= N - 1 - k; j += 2 * k)
+#pragma unroll
+        for (int i = 0; i <= k - 1 && i + j + k <= N - 1; i++)
+          if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) cswap(v[i + j], v[i + j + k]);
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    if ((u32)i < n) g[i] = v[i];
 }
 
 // ascending sort of g[0 .. n) (distinct values) by the 32 lanes of a warp
@@ -551,23 +573,8 @@ static __global__ void __launch_bounds__(FX_WARPS * 32)
       p0 = cell_offset[c];
       n = cell_offset[c + 1] - p0;
     }
-    if (flagged && n <= (u32)FX_REG) {
-      u32 v[FX_REG];
-#pragma unroll
-      for (int i = 0; i < FX_REG; i++) v[i] = (u32)i < n ? sort_indx[p0 + i] : 0xffffffffu;
-#pragma unroll
-      for (int p = 1; p < FX_REG; p <<= 1)
-#pragma unroll
-        for (int k = p; k >= 1; k >>= 1)
-#pragma unroll
-          for (int j = k % p; j <= FX_REG - 1 - k; j += 2 * k)
-#pragma unroll
-            for (int i = 0; i <= k - 1 && i + j + k <= FX_REG - 1; i++)
-              if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) cswap(v[i + j], v[i + j + k]);
-#pragma unroll
-      for (int i = 0; i < FX_REG; i++)
-        if ((u32)i < n) sort_indx[p0 + i] = v[i];
-    }
+    if (flagged && n <= (u32)FX_REG / 2) reg_sort<FX_REG / 2>(sort_indx + p0, n);
+    else if (flagged && n <= (u32)FX_REG) reg_sort<FX_REG>(sort_indx + p0, n);
     unsigned big = __ballot_sync(0xffffffffu, flagged && n > (u32)FX_REG);
     while (big) {
       const int l = __ffs(big) - 1;
