@@ -1011,6 +1011,8 @@ def main(argv=None):
                     help="batched: 64 small uneven runs through PIC_batch; large_modes: "
                          "the 4096 x 512, m = 0..2 run, mixed against FP64 (1 GPU); "
                          "adjoint: the differentiable run's forward and reverse sweep")
+    ap.add_argument("--adj-steps", type=int, default=100,
+                    help="steps of the differentiable run (--workload adjoint)")
     ap.add_argument("--batch-runs", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=0)
     args = ap.parse_args(argv)
@@ -1025,7 +1027,7 @@ def main(argv=None):
     if args.workload == "large_modes":
         return run_large_modes(args)
     if args.workload == "adjoint":
-        print(json.dumps(adjoint_line()))
+        print(json.dumps(adjoint_line(nsteps=args.adj_steps)))
         return 0
     return run_ours(args)
 

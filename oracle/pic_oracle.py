@@ -282,6 +282,33 @@ class OGrid:
                 K.append_c2c(oy, b)
                 K.zpaxz(oz, complex(-1j), b)
 
+    def field_div(self, vin, sout):
+        """transformer_methods_cl.py:135-183: i kx V_x plus the radial
+        derivative products of (-i V_z - V_y) of mode m-1 (the m=-1 mirror
+        for m = 0) and of (-i V_z + V_y) of mode m+1."""
+        A, D, K = self.Args, self.D, self.K
+        M = A["M"]
+        for c in ("y", "z"):
+            self._get_mm1(vin + c, c)
+        for m in range(M + 1):
+            s = str(m)
+            out = D[sout + "_fb_m" + s]
+            out[:] = 0
+            K.ab_dot_x(1j, A["kx"], D[vin + "x_fb_m" + s], out)
+            if m > 0:
+                fy, fz = D[vin + "y_fb_m" + str(m - 1)], D[vin + "z_fb_m" + str(m - 1)]
+            elif M > 0:
+                fy, fz = D["buff_fb_m-1_y"], D["buff_fb_m-1_z"]
+            else:
+                continue
+            b0 = np.zeros_like(out)
+            K.axpbyz(-1j, fz, -1.0, fy, b0)
+            K.append_c2c(out, self._cdot(A["dDHT_minus_m" + s], b0))
+            if m < M:
+                fy, fz = D[vin + "y_fb_m" + str(m + 1)], D[vin + "z_fb_m" + str(m + 1)]
+                K.axpbyz(-1j, fz, 1.0, fy, b0)
+                K.append_c2c(out, self._cdot(A["dDHT_plus_m" + s], b0))
+
     def field_rot(self, fin, fout):
         A, D, K = self.Args, self.D, self.K
         M = A["M"]
