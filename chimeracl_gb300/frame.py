@@ -35,6 +35,12 @@ class Frame:
             steps = self.Args["Steps"]
         x_shift = steps * self.Args["dt"] * self.Args["Velocity"]
         for sp in species:
+            if "InjectorSource" in sp.Args:
+                # a species injected from a source takes the source's new
+                # slab; the reference also generates a slab of its own here
+                # and discards it (its draws reach nothing)
+                sp.add_new_particles(sp.Args["InjectorSource"])
+                continue
             if sp.Args["Np"] == 0:
                 sp.Args["right_lim"] = grid.Args["Xmax"] - x_shift
             dom = {"Xmin": sp.Args["right_lim"]}
@@ -42,10 +48,7 @@ class Frame:
             dom["Rmin"] = grid.Args["Rmin"] * (grid.Args["Rmin"] > 0)
             dom["Rmax"] = grid.Args["Rmax"]
             sp.make_new_domain(dom, density_profiles=self.Args["DensityProfiles"])
-            if "InjectorSource" in sp.Args:
-                sp.add_new_particles(sp.Args["InjectorSource"])
-            else:
-                sp.add_new_particles()
+            sp.add_new_particles()
         for sp in species:
             sp.free_added()
             sp.sort_parts(grid=grid)
@@ -56,7 +59,7 @@ class Frame:
             # compensated coordinates x is x + x_lo: the next slab is then
             # placed where the FP64 run places it (from a rounded x the whole
             # slab would shift by that rounding)
-            if sp.Args["Np"] > 0:
+            if sp.Args["Np"] > 0 and "InjectorSource" not in sp.Args:
                 nppc = int(np.prod(sp.Args["Nppc"]) + 1)
                 x = sp.DataDev["x"]
                 x_tail = x[-nppc:].to(torch.float64)
