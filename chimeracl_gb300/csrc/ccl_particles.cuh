@@ -467,30 +467,46 @@ static __global__ void __launch_bounds__(ST_THREADS)
                                                                  : (u32)np - cell_offset[C])
                                    : ovf_before + ovf_off[blockIdx.x];
   const bool tile_has_ovf = ovf_next != ovf_before;
+  u32 kk[ST_ITEMS];
 #pragma unroll
   for (int it = 0; it < ST_ITEMS; it++) {
     const long i = base + it * ST_THREADS + threadIdx.x;
-    const bool valid = i < np;
-    const u32 k = valid ? keys[i] : 0xffffffffu;
-    const bool ovf = valid && k == C;
-    if (tile_has_ovf) {
-      // overflow: block-ordered rank within this round of ST_THREADS items
+    kk[it] = i < np ? keys[i] : 0xffffffffu;
+  }
+  if (tile_has_ovf) {
+    // overflow: block-ordered rank within each round of ST_THREADS items
+#pragma unroll
+    for (int it = 0; it < ST_ITEMS; it++) {
+      const long i = base + it * ST_THREADS + threadIdx.x;
+      const bool ovf = kk[it] == C;  // invalid items hold 0xffffffff != C
       u32 rtot;
       const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
       if (ovf) sort_indx[tile_run + r] = (u32)i;
       tile_run += rtot;
     }
-    // in-window: warp-aggregated cursor
-    const unsigned peers = __match_any_sync(0xffffffffu, (valid && !ovf) ? k : 0xffffffffu);
-    const int leader = __ffs(peers) - 1;
-    u32 b0 = 0;
-    if (valid && !ovf && lane == leader) {
-      b0 = atomicAdd(&cursor[k], __popc(peers));
-      // a second claim on the cell: its order may need the fix-up
-      if (b0 != 0) atomicOr(&multi[k >> 5], 1u << (k & 31));
-    }
-    b0 = __shfl_sync(0xffffffffu, b0, leader);
-    if (valid && !ovf) sort_indx[cell_offset[k] + b0 + __popc(peers & lt)] = (u32)i;
+  }
+  // in-window: one cursor atomic per distinct cell per warp and round, all
+  // of the thread's atomics issued before any result is used
+  unsigned peers[ST_ITEMS];
+  u32 b0[ST_ITEMS];
+#pragma unroll
+  for (int it = 0; it < ST_ITEMS; it++) {
+    const u32 k = kk[it];
+    const bool win = k < C;
+    peers[it] = __match_any_sync(0xffffffffu, win ? k : 0xffffffffu);
+    b0[it] = 0;
+    if (win && lane == __ffs(peers[it]) - 1) b0[it] = atomicAdd(&cursor[k], __popc(peers[it]));
+  }
+#pragma unroll
+  for (int it = 0; it < ST_ITEMS; it++) {
+    const long i = base + it * ST_THREADS + threadIdx.x;
+    const u32 k = kk[it];
+    const bool win = k < C;
+    const int leader = __ffs(peers[it]) - 1;
+    // a second claim on the cell: its order may need the fix-up
+    if (win && lane == leader && b0[it] != 0) atomicOr(&multi[k >> 5], 1u << (k & 31));
+    const u32 b = __shfl_sync(0xffffffffu, b0[it], leader);
+    if (win) sort_indx[cell_offset[k] + b + __popc(peers[it] & lt)] = (u32)i;
   }
 }
 
