@@ -721,7 +721,7 @@ def large_modes_line(steps, warmup, seed):
         "value": r32["np_sum"] / (r32["ms"] * 1e-3), "unit": "particle-steps/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": r32["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (radial GEMMs SIMT FP32: Nr - 1 > 256)",
+        "vs_baseline": None, "dtype": "f32+bf16x3",
         "data": "synthetic (seeded plasma, laser)",
         "config": {"workload": LARGE_MODES_WORKLOAD, "Nz": g["Nx"], "Nr": g["Nr"],
                    "modes": g["M"] + 1, "ppc": [2, 2, 4], "a0": 4.0, "w0": 12.0, "tau": 10.0,

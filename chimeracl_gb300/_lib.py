@@ -29,6 +29,9 @@ SIGNATURES = {
     "ccl_index_sort_workspace": [_l, _l, C.POINTER(_sz)],
     "ccl_index_sort": [_i, _l, _vp, _vp, _vp, _i, _d, _d, _i, _d, _d,
                        _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp],
+    "ccl_push_x_keys": [_i, _l] + [_vp] * 10 + [_d, _i, _d, _d, _i, _d, _d, _vp, _vp, _vp, _sz,
+                                                 _vp],
+    "ccl_index_sort_keyed": [_l, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp],
     "ccl_index_sort_noalloc": [_i, _l, _vp, _vp, _vp, _i, _d, _d, _i, _d, _d,
                                _vp, _vp, _vp, _vp, _vp, _vp],
     "ccl_align": [_i, _l, _i, _pp, _pp, _vp, _vp],

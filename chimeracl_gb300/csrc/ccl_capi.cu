@@ -77,6 +77,47 @@ int ccl_push_x_compensated(int dtype, long np, void *x, void *y, void *z, void *
                                      S(stream)));
 }
 
+int ccl_push_x_keys(int dtype, long np, void *x, void *y, void *z, void *x_lo, void *y_lo,
+                    void *z_lo, const void *px, const void *py, const void *pz,
+                    const void *g_inv, double dt, int Nx, double xmin, double dx_inv, int Nr,
+                    double rmin, double dr_inv, uint32_t *indx_in_cell, uint32_t *sum_in_cell,
+                    void *workspace, size_t workspace_bytes, void *stream) {
+  DTYPE_CHECK(dtype);
+  NONNEG(np);
+  CCL_REQUIRE(np < 0xffffffffL, CCL_ERR_UNSUPPORTED,
+              "%s: np %ld exceeds 32-bit particle numbers", __func__, np);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  NONNULL(sum_in_cell); NONNULL(workspace);
+  CCL_REQUIRE((x_lo == nullptr) == (y_lo == nullptr) && (x_lo == nullptr) == (z_lo == nullptr),
+              CCL_ERR_ARG, "%s: give all three low parts or none", __func__);
+  if (np > 0) {
+    NONNULL(x); NONNULL(y); NONNULL(z); NONNULL(px); NONNULL(py); NONNULL(pz);
+    NONNULL(g_inv); NONNULL(indx_in_cell);
+  }
+  return DISPATCH(dtype, push_x_keys(np, x, y, z, x_lo, y_lo, z_lo, px, py, pz, g_inv, dt, Nx,
+                                     xmin, dx_inv, Nr, rmin, dr_inv, indx_in_cell, sum_in_cell,
+                                     workspace, workspace_bytes, S(stream)));
+}
+
+int ccl_index_sort_keyed(long np, int Nx, int Nr, const uint32_t *indx_in_cell,
+                         uint32_t *sum_in_cell, uint32_t *cell_offset, uint32_t *sort_indx,
+                         uint32_t *np_stay, void *workspace, size_t workspace_bytes,
+                         void *stream) {
+  NONNEG(np);
+  CCL_REQUIRE(np < 0xffffffffL, CCL_ERR_UNSUPPORTED,
+              "%s: np %ld exceeds 32-bit particle numbers", __func__, np);
+  int rc = grid_check(__func__, Nx, Nr);
+  if (rc) return rc;
+  NONNULL(sum_in_cell); NONNULL(cell_offset); NONNULL(np_stay); NONNULL(workspace);
+  if (np > 0) {
+    NONNULL(indx_in_cell); NONNULL(sort_indx);
+  }
+  return index_sort_keyed_launch(np, (long)(Nx - 1) * (Nr - 1), indx_in_cell, sum_in_cell,
+                                 cell_offset, sort_indx, np_stay, workspace, workspace_bytes,
+                                 S(stream));
+}
+
 int ccl_index_sort_workspace(long np, long ncells, size_t *bytes) {
   NONNEG(np);
   CCL_REQUIRE(ncells > 0, CCL_ERR_ARG, "%s: ncells %ld", __func__, ncells);
@@ -448,8 +489,8 @@ int ccl_dht_gemm(int dtype, int batch, int m, int k, int ncols, int cplx,
 
 int ccl_dht_bf16x3_prepare_bytes(int m, int k, size_t *bytes) {
   NONNULL(bytes);
-  CCL_REQUIRE(m > 0 && k > 0 && k <= 256 && m <= 256, CCL_ERR_UNSUPPORTED,
-              "%s: m=%d k=%d (m, k <= 256)", __func__, m, k);
+  CCL_REQUIRE(m > 0 && k > 0 && k <= 512 && m <= 512, CCL_ERR_UNSUPPORTED,
+              "%s: m=%d k=%d (m, k <= 512)", __func__, m, k);
   *bytes = umma_split_bytes(m, k);
   return CCL_OK;
 }

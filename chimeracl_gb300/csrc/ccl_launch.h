@@ -60,6 +60,11 @@ template <typename T> struct Ops {
                         uint32_t *counts, uint32_t *cell_offset,
                         uint32_t *sort_indx, uint32_t *np_stay, void *ws,
                         size_t ws_bytes, cudaStream_t s);
+  static int push_x_keys(long np, void *x, void *y, void *z, void *xl, void *yl, void *zl,
+                         const void *px, const void *py, const void *pz, const void *g_inv,
+                         double dt, int Nx, double xmin, double dx_inv, int Nr, double rmin,
+                         double dr_inv, uint32_t *indx, uint32_t *counts, void *ws,
+                         size_t ws_bytes, cudaStream_t s);
   static int align(long n, int ncomp, void *const *src, void *const *dst,
                    const uint32_t *idx, cudaStream_t s);
   static int fill_grid(long ncells, void *x, void *y, void *z, void *w,
@@ -141,6 +146,9 @@ int umma_status(int reset);
 int umma_wait_probe(long spins, int arrive, int *gave_up, cudaStream_t s);
 
 size_t index_sort_ws_bytes(long np, long ncells);
+int index_sort_keyed_launch(long np, long ncells, const uint32_t *indx, uint32_t *counts,
+                            uint32_t *cell_offset, uint32_t *sort_indx, uint32_t *np_stay,
+                            void *ws, size_t ws_bytes, cudaStream_t s);
 int iota_u32(uint32_t *a, long n, cudaStream_t s);
 
 }  // namespace ccl

@@ -41,6 +41,18 @@ int Ops<T>::index_sort(long np, const void *x, const void *y, const void *z,
 }
 
 template <typename T>
+int Ops<T>::push_x_keys(long np, void *x, void *y, void *z, void *xl, void *yl, void *zl,
+                        const void *px, const void *py, const void *pz, const void *g_inv,
+                        double dt, int Nx, double xmin, double dx_inv, int Nr, double rmin,
+                        double dr_inv, uint32_t *indx, uint32_t *counts, void *ws,
+                        size_t ws_bytes, cudaStream_t s) {
+  const GridP<T> g = make_gridp<T>(Nx, Nr, xmin, dx_inv, rmin, dr_inv);
+  return ccl::push_keys<T>(np, (T *)x, (T *)y, (T *)z, (T *)xl, (T *)yl, (T *)zl,
+                           (const T *)px, (const T *)py, (const T *)pz, (const T *)g_inv, dt,
+                           g, indx, counts, ws, ws_bytes, s);
+}
+
+template <typename T>
 int Ops<T>::align(long n, int ncomp, void *const *src, void *const *dst,
                   const uint32_t *idx, cudaStream_t s) {
   return ccl::align<T>(n, ncomp, src, dst, idx, s);

@@ -9,7 +9,16 @@
 namespace ccl {
 
 // ---------------------------------------------------------------------
-// push_xyz (particles_generic.cl:129-153)
+// push_xyz (particles_generic.cl:129-153): one particle's arithmetic
+template <typename T>
+__device__ __forceinline__ void push_one(T &xo, T &yo, T &zo, T a, T b, T c, T gi, T dt) {
+  T dt_g = dt * gi;
+  T ddx = a * dt_g, ddy = b * dt_g, ddz = c * dt_g;
+  xo = xo + ddx;
+  yo = yo + ddy;
+  zo = zo + ddz;
+}
+
 template <typename T>
 __global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
                          T *__restrict__ z, const T *__restrict__ px,
@@ -28,24 +37,18 @@ __global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
     T *g = (T *)&gx, *a = (T *)&ux, *b = (T *)&uy, *c = (T *)&uz;
     T *xo = (T *)&xx, *yo = (T *)&yy, *zo = (T *)&zz;
 #pragma unroll
-    for (int q = 0; q < VW; q++) {
-      T dt_g = dt * g[q];
-      T ddx = a[q] * dt_g, ddy = b[q] * dt_g, ddz = c[q] * dt_g;
-      xo[q] = xo[q] + ddx;
-      yo[q] = yo[q] + ddy;
-      zo[q] = zo[q] + ddz;
-    }
+    for (int q = 0; q < VW; q++) push_one(xo[q], yo[q], zo[q], a[q], b[q], c[q], g[q], dt);
     ((V *)x)[v] = xx;
     ((V *)y)[v] = yy;
     ((V *)z)[v] = zz;
   }
   for (long i = nv * VW + blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
        i += (long)gridDim.x * blockDim.x) {
-    T dt_g = dt * g_inv[i];
-    T ddx = px[i] * dt_g, ddy = py[i] * dt_g, ddz = pz[i] * dt_g;
-    x[i] = x[i] + ddx;
-    y[i] = y[i] + ddy;
-    z[i] = z[i] + ddz;
+    T xo = x[i], yo = y[i], zo = z[i];
+    push_one(xo, yo, zo, px[i], py[i], pz[i], g_inv[i], dt);
+    x[i] = xo;
+    y[i] = yo;
+    z[i] = zo;
   }
 }
 
@@ -93,6 +96,15 @@ __device__ __forceinline__ void comp_add(T &hi, T &lo, T d) {
 }
 
 template <typename T>
+__device__ __forceinline__ void push_one_comp(T &xo, T &yo, T &zo, T &xs, T &ys, T &zs, T a,
+                                              T b, T c, T gi, T dt) {
+  T dt_g = dt * gi;
+  comp_add(xo, xs, a * dt_g);
+  comp_add(yo, ys, b * dt_g);
+  comp_add(zo, zs, c * dt_g);
+}
+
+template <typename T>
 __global__ void k_push_x_comp(long np, T *__restrict__ x, T *__restrict__ y,
                               T *__restrict__ z, T *__restrict__ xl, T *__restrict__ yl,
                               T *__restrict__ zl, const T *__restrict__ px,
@@ -111,12 +123,8 @@ __global__ void k_push_x_comp(long np, T *__restrict__ x, T *__restrict__ y,
     T *xo = (T *)&xx, *yo = (T *)&yy, *zo = (T *)&zz;
     T *xs = (T *)&xe, *ys = (T *)&ye, *zs = (T *)&ze;
 #pragma unroll
-    for (int q = 0; q < VW; q++) {
-      T dt_g = dt * g[q];
-      comp_add(xo[q], xs[q], a[q] * dt_g);
-      comp_add(yo[q], ys[q], b[q] * dt_g);
-      comp_add(zo[q], zs[q], c[q] * dt_g);
-    }
+    for (int q = 0; q < VW; q++)
+      push_one_comp(xo[q], yo[q], zo[q], xs[q], ys[q], zs[q], a[q], b[q], c[q], g[q], dt);
     ((V *)x)[v] = xx;
     ((V *)y)[v] = yy;
     ((V *)z)[v] = zz;
@@ -126,11 +134,8 @@ __global__ void k_push_x_comp(long np, T *__restrict__ x, T *__restrict__ y,
   }
   for (long i = nv * VW + blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
        i += (long)gridDim.x * blockDim.x) {
-    T dt_g = dt * g_inv[i];
     T xo = x[i], yo = y[i], zo = z[i], xs = xl[i], ys = yl[i], zs = zl[i];
-    comp_add(xo, xs, px[i] * dt_g);
-    comp_add(yo, ys, py[i] * dt_g);
-    comp_add(zo, zs, pz[i] * dt_g);
+    push_one_comp(xo, yo, zo, xs, ys, zs, px[i], py[i], pz[i], g_inv[i], dt);
     x[i] = xo;
     y[i] = yo;
     z[i] = zo;
@@ -395,6 +400,99 @@ __global__ void __launch_bounds__(ST_THREADS)
   }
 }
 
+// The coordinate push fused with the sort's first pass: one block per tile
+// of ST_TILE particles pushes them (the arithmetic of k_push_x, or of
+// k_push_x_comp when COMP, 16-byte vectors when every array is 16-byte
+// aligned), and writes the cell keys of the coordinates it has just formed,
+// the per-cell counts and the tile's overflow count exactly as k_keys does
+// from those coordinates -- without reading them back.
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(ST_THREADS)
+    k_push_keys(long np, T *__restrict__ x, T *__restrict__ y, T *__restrict__ z,
+                T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ zl,
+                const T *__restrict__ px, const T *__restrict__ py, const T *__restrict__ pz,
+                const T *__restrict__ g_inv, T dt, int vec, GridP<T> g,
+                u32 *__restrict__ keys, u32 *__restrict__ counts,
+                u32 *__restrict__ tile_ovf) {
+  constexpr int VW = 16 / sizeof(T);
+  constexpr int NVT = ST_TILE / VW / ST_THREADS;  // vectors per thread
+  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  __shared__ u32 sh[32];
+  const int lane = threadIdx.x & 31;
+  const u32 C = (u32)(g.Nx - 1) * (u32)(g.Nr - 1);
+  u32 novf = 0;
+#pragma unroll
+  for (int it = 0; it < NVT; it++) {
+    const long v = (long)blockIdx.x * (ST_TILE / VW) + it * ST_THREADS + threadIdx.x;
+    const long i0 = v * VW;
+    u32 k[VW];
+    if (vec && i0 + VW <= np) {
+      V gx = ((const V *)g_inv)[v], ux = ((const V *)px)[v], uy = ((const V *)py)[v],
+        uz = ((const V *)pz)[v];
+      V xx = ((V *)x)[v], yy = ((V *)y)[v], zz = ((V *)z)[v];
+      T *gg = (T *)&gx, *a = (T *)&ux, *b = (T *)&uy, *c = (T *)&uz;
+      T *xo = (T *)&xx, *yo = (T *)&yy, *zo = (T *)&zz;
+      if constexpr (COMP) {
+        V xe = ((V *)xl)[v], ye = ((V *)yl)[v], ze = ((V *)zl)[v];
+        T *xs = (T *)&xe, *ys = (T *)&ye, *zs = (T *)&ze;
+#pragma unroll
+        for (int q = 0; q < VW; q++)
+          push_one_comp(xo[q], yo[q], zo[q], xs[q], ys[q], zs[q], a[q], b[q], c[q], gg[q], dt);
+        ((V *)xl)[v] = xe;
+        ((V *)yl)[v] = ye;
+        ((V *)zl)[v] = ze;
+      } else {
+#pragma unroll
+        for (int q = 0; q < VW; q++) push_one(xo[q], yo[q], zo[q], a[q], b[q], c[q], gg[q], dt);
+      }
+      ((V *)x)[v] = xx;
+      ((V *)y)[v] = yy;
+      ((V *)z)[v] = zz;
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        k[q] = cell_key<T>(xo[q], yo[q], zo[q], g);
+        keys[i0 + q] = k[q];
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        const long i = i0 + q;
+        k[q] = 0xffffffffu;
+        if (i < np) {
+          T xo = x[i], yo = y[i], zo = z[i];
+          if constexpr (COMP) {
+            T xs = xl[i], ys = yl[i], zs = zl[i];
+            push_one_comp(xo, yo, zo, xs, ys, zs, px[i], py[i], pz[i], g_inv[i], dt);
+            xl[i] = xs;
+            yl[i] = ys;
+            zl[i] = zs;
+          } else {
+            push_one(xo, yo, zo, px[i], py[i], pz[i], g_inv[i], dt);
+          }
+          x[i] = xo;
+          y[i] = yo;
+          z[i] = zo;
+          k[q] = cell_key<T>(xo, yo, zo, g);
+          keys[i] = k[q];
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      const bool valid = k[q] != 0xffffffffu;
+      novf += (valid && k[q] == C) ? 1u : 0u;
+      const unsigned peers = __match_any_sync(0xffffffffu, k[q]);
+      if (valid && k[q] != C && lane == __ffs(peers) - 1) atomicAdd(&counts[k[q]], __popc(peers));
+    }
+  }
+  u32 tot;
+  block_exclusive_scan(novf, sh, &tot);
+  if (threadIdx.x == 0) {
+    tile_ovf[blockIdx.x] = tot;
+    if (tot) atomicAdd(&counts[C], tot);
+  }
+}
+
 static inline long scan_ws_words(long L) {
   long w = 0;
   while (L > SCAN_TILE) {
@@ -642,6 +740,42 @@ static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
   return s;
 }
 
+// The sort after its first pass (keys in indx, counts in counts, the tiles'
+// overflow counts in the workspace): offsets, scatter, fix-up.
+inline int index_sort_keyed(long np, long C, const u32 *indx, u32 *counts, u32 *cell_offset,
+                            u32 *sort_indx, u32 *np_stay, void *ws, size_t ws_bytes,
+                            cudaStream_t s) {
+  CCL_REQUIRE(ws_bytes >= sort_ws_bytes(np, C), CCL_ERR_WORKSPACE,
+              "index_sort: workspace %zu < %zu bytes", ws_bytes, sort_ws_bytes(np, C));
+  SortWs w = carve_sort_ws(ws, np, C);
+  const long ntiles = (np + ST_TILE - 1) / ST_TILE;
+  // offsets, total, and np_stay = cell_offset[C] from the scan's own tap
+  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1, w.scan, s, np_stay,
+                          C);
+  if (rc) return rc;
+  if (np == 0) return CCL_OK;
+  // few tiles: each scatter block adds up the overflow counts before it
+  const int ovf_scanned = ntiles > SCAN_FUSE;
+  if (ovf_scanned) {
+    rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
+    if (rc) return rc;
+  }
+  // cursors and multi-claim bits are adjacent: one memset clears both
+  cudaError_t me = cudaMemsetAsync(
+      w.cursor, 0, (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32), s);
+  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the cursors: %s",
+              cudaGetErrorString(me));
+  k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
+                                                    w.cursor, w.multi, w.tile_ovf, ovf_scanned,
+                                                    sort_indx);
+  CCL_LAUNCH_CHECK("scatter");
+  if (C > 0)
+    k_cell_fixup<<<grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s>>>((u32)C, cell_offset,
+                                                                       w.multi, sort_indx);
+  CCL_LAUNCH_CHECK("cell_fixup");
+  return CCL_OK;
+}
+
 template <typename T>
 int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
                u32 *indx, u32 *counts, u32 *cell_offset, u32 *sort_indx,
@@ -660,30 +794,38 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
                                                       w.tile_ovf);
     CCL_LAUNCH_CHECK("keys");
   }
-  // offsets, total, and np_stay = cell_offset[C] from the scan's own tap
-  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1, w.scan, s, np_stay,
-                          C);
-  if (rc) return rc;
-  if (np == 0) return CCL_OK;
-  // few tiles: each scatter block adds up the overflow counts before it
-  const int ovf_scanned = ntiles > SCAN_FUSE;
-  if (ovf_scanned) {
-    rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
-    if (rc) return rc;
-  }
-  // cursors and multi-claim bits are adjacent: one memset clears both
-  me = cudaMemsetAsync(w.cursor, 0,
-                       (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32), s);
-  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the cursors: %s",
+  return index_sort_keyed(np, C, indx, counts, cell_offset, sort_indx, np_stay, ws, ws_bytes,
+                          s);
+}
+
+// push_xyz (compensated when xl != nullptr) + the sort's first pass; the
+// sort then completes with index_sort_keyed on the same workspace
+template <typename T>
+int push_keys(long np, T *x, T *y, T *z, T *xl, T *yl, T *zl, const T *px, const T *py,
+              const T *pz, const T *g_inv, double dt, GridP<T> g, u32 *indx, u32 *counts,
+              void *ws, size_t ws_bytes, cudaStream_t s) {
+  long C = (long)(g.Nx - 1) * (g.Nr - 1);
+  CCL_REQUIRE(ws_bytes >= sort_ws_bytes(np, C), CCL_ERR_WORKSPACE,
+              "push_x_keys: workspace %zu < %zu bytes", ws_bytes, sort_ws_bytes(np, C));
+  SortWs w = carve_sort_ws(ws, np, C);
+  const long ntiles = (np + ST_TILE - 1) / ST_TILE;
+  cudaError_t me = cudaMemsetAsync(counts, 0, (C + 1) * sizeof(u32), s);
+  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "push_x_keys: clearing the counts: %s",
               cudaGetErrorString(me));
-  k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
-                                                    w.cursor, w.multi, w.tile_ovf, ovf_scanned,
-                                                    sort_indx);
-  CCL_LAUNCH_CHECK("scatter");
-  if (C > 0)
-    k_cell_fixup<<<grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s>>>((u32)C, cell_offset,
-                                                                       w.multi, sort_indx);
-  CCL_LAUNCH_CHECK("cell_fixup");
+  if (np == 0) return CCL_OK;
+  uintptr_t mis = ((uintptr_t)x | (uintptr_t)y | (uintptr_t)z | (uintptr_t)px |
+                   (uintptr_t)py | (uintptr_t)pz | (uintptr_t)g_inv) & 15;
+  if (xl) {
+    mis |= ((uintptr_t)xl | (uintptr_t)yl | (uintptr_t)zl) & 15;
+    k_push_keys<T, true><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(
+        np, x, y, z, xl, yl, zl, px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts,
+        w.tile_ovf);
+  } else {
+    k_push_keys<T, false><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(
+        np, x, y, z, nullptr, nullptr, nullptr, px, py, pz, g_inv, (T)dt, mis == 0, g, indx,
+        counts, w.tile_ovf);
+  }
+  CCL_LAUNCH_CHECK("push_x_keys");
   return CCL_OK;
 }
 

@@ -2,8 +2,10 @@
 // 5th-generation tensor cores (tcgen05.mma, FP32 accumulation in TMEM):
 //   Y = beta*Y + alpha * (A X),  A ~ A_hi + A_lo,  X ~ X_hi + X_lo  (bf16),
 //   A X ~ A_hi X_hi + A_hi X_lo + A_lo X_hi,
-// A real (m x k, m, k <= 256), X FP32 (k x ncols real columns, interleaved
-// complex allowed), Y FP32.
+// A real (m x k, m, k <= 512), X FP32 (k x ncols real columns, interleaved
+// complex allowed), Y FP32.  One MMA covers at most 256 rows of A (its N):
+// for m > 256 the rows are taken in two halves of 256, each a work item of
+// its own over the same X tile.
 //
 // A is split once into bf16 hi/lo (k_umma_split_a); X is split on the fly.
 // Every mbarrier wait is bounded; a wait that gives up records an error code
@@ -21,7 +23,7 @@
 
 namespace ccl {
 
-constexpr int UM_MAXK = 256, UM_MAXBATCH = 32;
+constexpr int UM_MAXK = 512, UM_MAXBATCH = 32;
 constexpr long UM_SPIN_LIMIT = 20000000L;  // ~ a second of try_wait polls
 
 __device__ int g_umma_error = 0;
@@ -119,28 +121,33 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo_k, __nv_bfloat16 
 }
 
 // ------------------------------------------------------------- A split
-// The matrix A (m x k, row-major, lda = k, m <= 256) is stored for the MMA's
-// B operand, streamed per 32-deep K chunk: chunk c holds a hi block then a lo
-// block of NP x 32 bf16 (NP = 128 or 256 padded rows), K-major no-swizzle
-// core matrices, core matrix (g = row/8, j = (col%32)/8) at (g*4 + j)*128
-// bytes, each 8 rows x 8 consecutive k values.  Zero outside m x k.
+// The matrix A (m x k, row-major, lda = k, m <= 512) is stored for the MMA's
+// B operand, in row halves of NP rows (one half when m <= 256), each
+// streamed per 32-deep K chunk: chunk c of half h (at (h*nchunk + c) chunk
+// sizes) holds a hi block then a lo block of NP x 32 bf16 (NP = 128 or 256
+// padded rows), K-major no-swizzle core matrices, core matrix (g = row/8,
+// j = (col%32)/8) at (g*4 + j)*128 bytes, each 8 rows x 8 consecutive k
+// values.  Zero outside m x k.
 constexpr int UM_KC = 32;  // K depth of one stage
 __host__ __device__ constexpr int umma_np(int m) { return m <= 128 ? 128 : 256; }
+__host__ __device__ constexpr int umma_halves(int m) { return m <= 256 ? 1 : 2; }
 __host__ __device__ constexpr uint32_t umma_chunk_bytes(int np) { return 2u * np * UM_KC * 2; }
 
 template <typename TA>
 __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int np, int nchunk,
-                               uint4 *__restrict__ out) {
+                               int nh, uint4 *__restrict__ out) {
   const long per_block = (long)np * (UM_KC / 8);  // 16-B rows of one hi or lo block
-  const long total = (long)nchunk * 2 * per_block;
+  const long per_half = (long)nchunk * 2 * per_block;
+  const long total = nh * per_half;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < total;
        q += (long)gridDim.x * blockDim.x) {
-    const long c = q / (2 * per_block), rem = q - c * 2 * per_block;
+    const long h = q / per_half, qh = q - h * per_half;
+    const long c = qh / (2 * per_block), rem = qh - c * 2 * per_block;
     const int lo = rem >= per_block;
     const long w = rem - lo * per_block;
     const long cm = w / 8, i8 = w - cm * 8;
     const long g = cm / (UM_KC / 8), j = cm - g * (UM_KC / 8);
-    const long row = g * 8 + i8;
+    const long row = h * np + g * 8 + i8;
     __nv_bfloat16 e[8];
 #pragma unroll
     for (int t = 0; t < 8; t++) {
@@ -161,9 +168,10 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int np, i
 // ---------------------------------------------------------------- GEMM
 // Persistent, warp-specialised kernel computing the transpose on the tensor
 // cores, Y^T = X^T A^T: the MMA's M = 128 columns of X (one work item = one
-// 128-column tile of one batch entry), its N = NP rows of A, K = 16 per
-// instruction.  Each X tile is therefore read and converted once for all
-// output rows; A streams per K chunk from L2 (it is shared by every CTA).
+// 128-column tile of one batch entry and one row half of A), its N = NP rows
+// of A, K = 16 per instruction.  Each X tile is therefore read and converted
+// once for all output rows of a half (m <= 256: for all of them); A streams
+// per K chunk from L2 (it is shared by every CTA).
 //   warps 0-3  epilogue: TMEM lane = X column n, TMEM column = output row i;
 //              alpha (complex pairs are adjacent columns n, n+1: one shuffle),
 //              optional +Y, stores of 32 consecutive columns of one row per
@@ -194,6 +202,7 @@ struct UmmaWork {
   int base[UM_MAXBATCH];   // first item of the entry
   long ldy[UM_MAXBATCH];
   int batch, items;
+  int nh;  // row halves of A: items of an entry are (column tile, half), half fastest
 };
 
 // X of every entry as a 2-D tensor map (inner dim = columns, box 128 x 32)
@@ -244,10 +253,13 @@ __device__ __forceinline__ void um_fail(volatile int *abort, int code) {
   *abort = 1;
 }
 
-__device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, int &nt) {
+__device__ __forceinline__ void um_decode(const UmmaWork &w, int item, int &e, int &nt,
+                                          int &h) {
   e = 0;
   while (e + 1 < w.batch && w.base[e + 1] <= item) e++;
-  nt = item - w.base[e];
+  const int local = item - w.base[e];  // nh is 1 or 2
+  nt = w.nh == 2 ? local >> 1 : local;
+  h = local & (w.nh - 1);
 }
 
 // converter: k rows kb*8 .. +7, columns n, n+1 of a raw stage -> one core
@@ -348,8 +360,8 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
     // tcgen05.ld is warp-collective: every exit decision is taken warp-wide
     for (int j = 0, item = i0; item < i1; j++, item++) {
       if (__any_sync(0xffffffffu, *abort)) break;
-      int e, nt;
-      um_decode(w, item, e, nt);
+      int e, nt, h;
+      um_decode(w, item, e, nt, h);
       const int b = j & 1;
       const bool got = mbar_wait_ab(&tfull[b], (j >> 1) & 1, abort);
       if (!__all_sync(0xffffffffu, got)) {
@@ -360,10 +372,11 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       const int N = w.ncols[e];
       const int n = nt * UM_TN + warp * 32 + lane;  // this lane's column of X and Y
       const bool nin = n < N;
-      float *__restrict__ ycol = w.Y[e] + n;
       const long ldy = w.ldy[e];
+      float *__restrict__ ycol = w.Y[e] + n;
+      if (h) ycol += (long)NP * ldy;  // first row of the half
       const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * NP);
-      const int mrow = M < NP ? M : NP;
+      const int mrow = M - h * NP < NP ? M - h * NP : NP;  // rows of this half
       float *yp = ycol;  // row i of this lane's column
 #pragma unroll 1
       for (int i0c = 0; i0c < mrow; i0c += 32) {
@@ -380,7 +393,7 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
           } else {
             r = are * v[t];
           }
-          if (nin && i0c + t < M) {
+          if (nin && i0c + t < mrow) {
             if (ACC) r += *yp;
             *yp = r;
           }
@@ -442,8 +455,8 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
           um_fail(abort, 8);
           break;
         }
-        int e, nt;
-        um_decode(w, i0 + s / nkc, e, nt);
+        int e, nt, h;
+        um_decode(w, i0 + s / nkc, e, nt, h);
         const int kc = s % nkc;
         mbar_expect_tx(&rfull[r], UM_RAW);
         tma_load_2d(sR + r * UM_RAW, &args.tx[e], nt * UM_TN, kc * UM_KC, &rfull[r]);
@@ -453,7 +466,8 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
           break;
         }
         mbar_expect_tx(&afull[a], ACH);
-        bulk_g2s(sA + a * ACH, (const unsigned char *)w.A[e] + (long)kc * ACH, ACH, &afull[a]);
+        bulk_g2s(sA + a * ACH, (const unsigned char *)w.A[e] + ((long)h * nkc + kc) * ACH, ACH,
+                 &afull[a]);
         issued_a = s + 1;
       }
       // every copy this lane issued has landed before the CTA may exit
@@ -524,7 +538,7 @@ static size_t umma_smem(int np) {
 size_t umma_split_bytes(int m, int k) {
   if (k > UM_MAXK || m > UM_MAXK || m <= 0 || k <= 0) return 0;
   const int nchunk = (k + UM_KC - 1) / UM_KC;
-  return (size_t)nchunk * umma_chunk_bytes(umma_np(m));
+  return (size_t)umma_halves(m) * nchunk * umma_chunk_bytes(umma_np(m));
 }
 
 template <typename TA>
@@ -534,9 +548,10 @@ int umma_split_a(const TA *A, int m, int k, void *out, size_t bytes, cudaStream_
   CCL_REQUIRE(bytes >= umma_split_bytes(m, k), CCL_ERR_WORKSPACE,
               "umma split: %zu < %zu bytes", bytes, umma_split_bytes(m, k));
   CCL_REQUIRE(((uintptr_t)out & 15) == 0, CCL_ERR_ARG, "umma split: output not 16-B aligned");
-  const int np = umma_np(m), nchunk = (k + UM_KC - 1) / UM_KC;
-  const long total = (long)nchunk * 2 * np * (UM_KC / 8);
-  k_umma_split_a<TA><<<grid_for(total, 256), 256, 0, s>>>(A, m, k, np, nchunk, (uint4 *)out);
+  const int np = umma_np(m), nchunk = (k + UM_KC - 1) / UM_KC, nh = umma_halves(m);
+  const long total = (long)nh * nchunk * 2 * np * (UM_KC / 8);
+  k_umma_split_a<TA><<<grid_for(total, 256), 256, 0, s>>>(A, m, k, np, nchunk, nh,
+                                                          (uint4 *)out);
   CCL_LAUNCH_CHECK("umma_split_a");
   return CCL_OK;
 }
@@ -619,11 +634,12 @@ int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const v
     w.ncols[i] = ncols[i];
     w.base[i] = (int)items;
     w.ldy[i] = ldy[i];
-    items += (ncols[i] + UM_TN - 1) / UM_TN;
+    items += (long)umma_halves(m) * ((ncols[i] + UM_TN - 1) / UM_TN);
   }
   CCL_REQUIRE(items < (1L << 30), CCL_ERR_ARG, "umma: %ld work items", items);
   w.batch = batch;
   w.items = (int)items;
+  w.nh = umma_halves(m);
   static int sms = 0;
   if (!sms) sms = device_sm_count();
   const int grid = (int)(items < sms ? items : sms);

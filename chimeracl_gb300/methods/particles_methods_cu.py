@@ -166,32 +166,50 @@ class ParticleMethodsCU(GenericMethodsCU):
              D[weight].data_ptr(), xl.data_ptr(), fl.data_ptr(), dl.data_ptr(), x_loc.size,
              stream())
 
-    def push_coords(self, mode="half"):
-        """particles_methods_cl.py:206-223"""
+    def push_coords(self, mode="half", sort_grid=None):
+        """particles_methods_cl.py:206-223.  With ``sort_grid`` the push
+        also forms the cell keys and counts of the sort on that grid from the
+        coordinates it has just computed (one kernel); the next
+        ``index_sort`` on the same grid then only completes the sort."""
+        self._keys_for = None
         if self.Args["Np"] == 0 or "Immobile" in self.Args:
             return
         D = self.DataDev
         dt = self.Args["dt_2"] if mode == "half" else self.Args["dt"]
-        if "x_lo" in D:
+        lo = [D[k].data_ptr() for k in ("x_lo", "y_lo", "z_lo")] if "x_lo" in D else None
+        if sort_grid is not None:
+            bufs, G = self._sort_buffers(sort_grid), sort_grid.Args
+            call("ccl_push_x_keys", self._dt, self.Args["Np"], D["x"].data_ptr(),
+                 D["y"].data_ptr(), D["z"].data_ptr(), *(lo or [None] * 3),
+                 *[D[k].data_ptr() for k in ("px", "py", "pz", "g_inv")], float(dt),
+                 G["Nx"], float(G["Xmin"]), float(G["dx_inv"]), G["Nr"], float(G["Rmin"]),
+                 float(G["dr_inv"]), D["indx_in_cell"].data_ptr(),
+                 D["sum_in_cell"].data_ptr(), bufs[5].data_ptr(), bufs[6], stream())
+            self._keys_for = self._sort_token(sort_grid)
+        elif lo is not None:
             call("ccl_push_x_compensated", self._dt, self.Args["Np"],
-                 *[D[k].data_ptr() for k in ("x", "y", "z", "x_lo", "y_lo", "z_lo", "px", "py",
-                                             "pz", "g_inv")], float(dt), stream())
-            self.flag_sorted = False
-            return
-        call("ccl_push_x", self._dt, self.Args["Np"], D["x"].data_ptr(), D["y"].data_ptr(),
-             D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(), D["pz"].data_ptr(),
-             D["g_inv"].data_ptr(), float(dt), stream())
+                 *[D[k].data_ptr() for k in ("x", "y", "z")], *lo,
+                 *[D[k].data_ptr() for k in ("px", "py", "pz", "g_inv")], float(dt), stream())
+        else:
+            call("ccl_push_x", self._dt, self.Args["Np"], D["x"].data_ptr(), D["y"].data_ptr(),
+                 D["z"].data_ptr(), D["px"].data_ptr(), D["py"].data_ptr(), D["pz"].data_ptr(),
+                 D["g_inv"].data_ptr(), float(dt), stream())
         self.flag_sorted = False
 
-    def index_sort(self, grid):
-        """particles_methods_cl.py:225-261: keys, counts, exclusive prefix
-        (cell_offset), stable sort -- one C-ABI call.  Np_stay stays on the
-        device (read lazily through Args)."""
+    def _sort_token(self, grid):
+        """What the keys depend on besides the coordinates: the particle
+        arrays, their count and the grid."""
+        G, D = grid.Args, self.DataDev
+        return (self.Args["Np"], D["x"].data_ptr(), G["Nx"], G["Nr"], float(G["Xmin"]),
+                float(G["dx_inv"]), float(G["Rmin"]), float(G["dr_inv"]))
+
+    def _sort_buffers(self, grid):
+        """The sort's outputs and workspace; they persist while Np and the
+        grid are unchanged, so a step between window shifts allocates nothing
+        (and can be graph-captured)."""
         Np = self.Args["Np"]
         C = grid.Args["Nxm1Nrm1"]
         dev, D = self.comm.device, self.DataDev
-        # buffers persist while Np and the grid are unchanged, so a step
-        # between window shifts allocates nothing (and can be graph-captured)
         key = (Np, C)
         bufs = getattr(self, "_sort_bufs", None)
         if bufs is None or bufs[0] != key:
@@ -203,14 +221,30 @@ class ParticleMethodsCU(GenericMethodsCU):
                     torch.empty(max(Np, 1), dtype=i32, device=dev)[:Np],
                     torch.empty(ws_bytes, dtype=torch.uint8, device=dev), ws_bytes)
             self._sort_bufs = bufs
-        _, D["indx_in_cell"], D["sum_in_cell"], D["cell_offset"], D["sort_indx"], ws, ws_bytes = bufs
-        G = grid.Args
-        call("ccl_index_sort", self._dt, Np, D["x"].data_ptr(), D["y"].data_ptr(),
-             D["z"].data_ptr(), G["Nx"], float(G["Xmin"]), float(G["dx_inv"]), G["Nr"],
-             float(G["Rmin"]), float(G["dr_inv"]), D["indx_in_cell"].data_ptr(),
-             D["sum_in_cell"].data_ptr(), D["cell_offset"].data_ptr(),
-             D["sort_indx"].data_ptr(), D["Np_stay_dev"].data_ptr(), ws.data_ptr(), ws_bytes,
-             stream())
+        _, D["indx_in_cell"], D["sum_in_cell"], D["cell_offset"], D["sort_indx"] = bufs[:5]
+        return bufs
+
+    def index_sort(self, grid):
+        """particles_methods_cl.py:225-261: keys, counts, exclusive prefix
+        (cell_offset), stable sort -- one C-ABI call, or the completion of
+        the sort whose keys the coordinate push formed.  Np_stay stays on
+        the device (read lazily through Args)."""
+        bufs = self._sort_buffers(grid)
+        D, G, Np = self.DataDev, grid.Args, self.Args["Np"]
+        ws, ws_bytes = bufs[5], bufs[6]
+        if getattr(self, "_keys_for", None) == self._sort_token(grid):
+            call("ccl_index_sort_keyed", Np, G["Nx"], G["Nr"], D["indx_in_cell"].data_ptr(),
+                 D["sum_in_cell"].data_ptr(), D["cell_offset"].data_ptr(),
+                 D["sort_indx"].data_ptr(), D["Np_stay_dev"].data_ptr(), ws.data_ptr(),
+                 ws_bytes, stream())
+        else:
+            call("ccl_index_sort", self._dt, Np, D["x"].data_ptr(), D["y"].data_ptr(),
+                 D["z"].data_ptr(), G["Nx"], float(G["Xmin"]), float(G["dx_inv"]), G["Nr"],
+                 float(G["Rmin"]), float(G["dr_inv"]), D["indx_in_cell"].data_ptr(),
+                 D["sum_in_cell"].data_ptr(), D["cell_offset"].data_ptr(),
+                 D["sort_indx"].data_ptr(), D["Np_stay_dev"].data_ptr(), ws.data_ptr(),
+                 ws_bytes, stream())
+        self._keys_for = None
         dict.__setitem__(self.Args, "Np_stay", LazyScalar(D["Np_stay_dev"], self.comm))
 
     def align_and_damp(self, comps_align):

@@ -68,12 +68,12 @@ class TransformerMethodsCU(GenericMethodsCU):
     def _gemm(self, names, X, ldx, Y, ldy, ncols, cplx=False, alpha=1.0, beta=0.0):
         """Y[i] = beta Y[i] + alpha (A[i] X[i]) for the matrices `names`
         (pointers X, Y as ints), one launch: the BF16x3 tensor-core kernel in
-        the mixed form when k <= 256 and the rows are 16-byte aligned, else
-        the SIMT kernel in the compute precision (m, k <= 256 for the former)."""
+        the mixed form when m, k <= 512 and the rows are 16-byte aligned,
+        else the SIMT kernel in the compute precision."""
         a = complex(alpha)
         m, k = self.DataDev[names[0]].shape
         b = len(names)
-        if (self.comm.dht_impl == "bf16x3" and k <= 256 and m <= 256
+        if (self.comm.dht_impl == "bf16x3" and k <= 512 and m <= 512
                 and all(p % 16 == 0 for p in X) and all(l % 4 == 0 for l in ldx)):
             mats = [self._bf16x3(n) for n in names]
             call("ccl_dht_bf16x3_gemm_batch", b, m, k, ints(ncols), int(cplx), PP(mats), PP(X),

@@ -196,10 +196,11 @@ class PIC_loop:
 
     def _particles_before(self, graph_mode):
         """Half push + sort, current deposit, half push + sort, charge
-        deposit (pic_loop.py:73-98)."""
+        deposit (pic_loop.py:73-98).  Each push also forms the sort's cell
+        keys from the coordinates it computes (one kernel, no re-read)."""
         for parts in self.species:
             self.timer_start()
-            parts.push_coords(mode="half")
+            parts.push_coords(mode="half", sort_grid=self.mainsolver)
             self.timer_record("push-x")
             self.timer_start()
             parts.sort_parts(grid=self.mainsolver)
@@ -212,7 +213,7 @@ class PIC_loop:
 
         for parts in self.species:
             self.timer_start()
-            parts.push_coords(mode="half")
+            parts.push_coords(mode="half", sort_grid=self.mainsolver)
             self.timer_record("push-x")
             self.timer_start()
             parts.sort_parts(grid=self.mainsolver)

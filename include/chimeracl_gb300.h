@@ -92,6 +92,26 @@ int ccl_index_sort(int dtype, long np, const void *x, const void *y,
                    uint32_t *sort_indx, uint32_t *np_stay, void *workspace,
                    size_t workspace_bytes, void *stream);
 
+/* The same sort in two calls around the coordinate push, so that the keys
+ * are formed from the coordinates the push has just computed instead of
+ * being read back: ccl_push_x_keys runs push_xyz (ccl_push_x, or with
+ * x_lo, y_lo, z_lo non-null ccl_push_x_compensated) and the first pass of
+ * ccl_index_sort (indx_in_cell, sum_in_cell, and per-tile counts kept in the
+ * workspace); ccl_index_sort_keyed, on the same workspace before any other
+ * use of it, completes the sort (cell_offset, sort_indx, np_stay).  The
+ * outputs are those of ccl_push_x followed by ccl_index_sort.  Replaces the
+ * pair push_coords + sort_parts of the reference's loop (pic_loop.py:74-98,
+ * particles_methods_cl.py:206-261) with no counterpart of its own. */
+int ccl_push_x_keys(int dtype, long np, void *x, void *y, void *z, void *x_lo, void *y_lo,
+                    void *z_lo, const void *px, const void *py, const void *pz,
+                    const void *g_inv, double dt, int Nx, double xmin, double dx_inv, int Nr,
+                    double rmin, double dr_inv, uint32_t *indx_in_cell, uint32_t *sum_in_cell,
+                    void *workspace, size_t workspace_bytes, void *stream);
+int ccl_index_sort_keyed(long np, int Nx, int Nr, const uint32_t *indx_in_cell,
+                         uint32_t *sum_in_cell, uint32_t *cell_offset, uint32_t *sort_indx,
+                         uint32_t *np_stay, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
 /* ccl_index_sort without a caller-owned workspace.  No counterpart in the
  * reference: it is for callers that cannot allocate device memory for the
  * sort (a host binding that owns no device allocator, or a process whose
@@ -329,7 +349,7 @@ int ccl_dht_gemm_batch(int dtype, int batch, int m, int k, const int *ncols,
  * accumulation), for FP32 operands: A = A_hi + A_lo and X = X_hi + X_lo in
  * bf16, A X ~ A_hi X_hi + A_hi X_lo + A_lo X_hi (relative error ~1e-5).
  * The constant matrix is split once: ccl_dht_bf16x3_prepare writes the
- * split, tiled form of A (m x k, row-major, m, k <= 256, dtype CCL_F64 or
+ * split, tiled form of A (m x k, row-major, m, k <= 512, dtype CCL_F64 or
  * CCL_F32) into `out` (ccl_dht_bf16x3_prepare_bytes bytes, 16-byte aligned).
  * ccl_dht_bf16x3_gemm_batch then takes prepared matrices and the arguments
  * of ccl_dht_gemm_batch (X rows 16-byte aligned: ldx % 4 == 0).

@@ -53,3 +53,14 @@ def test_invalid_arguments_rejected_without_launch():
     assert lib.ccl_push_x(0, 0, None, None, None, None, None, None, None, 0.1, None) == 0
     assert lib.ccl_deposit_scalar(0, 9, None, None, None, None, None, None, -1, 64, 0.0, 1.0, 16,
                                   0.0, 1.0, None, None) == 3
+    # the fused push + sort keys: dtype, grid, low parts all or none, NULLs
+    args = [None] * 10 + [0.1, 64, 0.0, 1.0, 16, 0.0, 1.0, None, None, None, 0, None]
+    assert lib.ccl_push_x_keys(7, 10, *args) == 1 and b"dtype" in lib.ccl_last_error()
+    bad_grid = args[:11] + [2] + args[12:]
+    assert lib.ccl_push_x_keys(0, 10, *bad_grid) == 1 and b"grid" in lib.ccl_last_error()
+    one_lo = args[:3] + [8] + args[4:18] + [8, 8] + args[20:]
+    assert lib.ccl_push_x_keys(0, 10, *one_lo) == 1 and b"low parts" in lib.ccl_last_error()
+    assert lib.ccl_push_x_keys(0, 10, *args) == 1 and b"NULL" in lib.ccl_last_error()
+    assert lib.ccl_index_sort_keyed(10, 64, 2, None, None, None, None, None, None, 0, None) == 1
+    assert b"grid" in lib.ccl_last_error()
+    assert lib.ccl_index_sort_keyed(-1, 64, 16, None, None, None, None, None, None, 0, None) == 1

@@ -29,7 +29,10 @@ def prepare(A64, dtype=CCL_F64):
 @pytest.mark.parametrize("m,k,ncols,ldx,cplx_,beta", [
     (255, 255, 4096, 4096, 1, 0.0), (255, 255, 2048, 2048, 0, 0.0), (63, 63, 1024, 1024, 1, 0.0),
     (100, 37, 130, 136, 0, 1.0), (255, 255, 512, 512, 1, 1.0), (128, 256, 64, 64, 0, 0.0),
-    (129, 129, 200, 200, 1, 0.0)])
+    (129, 129, 200, 200, 1, 0.0),
+    # m > 256: two row halves of A, each a work item over the same X tile
+    (511, 511, 4096, 4096, 1, 0.0), (511, 511, 1024, 1024, 0, 1.0), (300, 400, 200, 200, 1, 0.0),
+    (257, 129, 130, 136, 0, 1.0), (511, 300, 512, 512, 1, 1.0), (200, 511, 256, 256, 0, 0.0)])
 def test_bf16x3_gemm(cuda, m, k, ncols, ldx, cplx_, beta):
     rng = np.random.default_rng(m * 7 + ncols)
     A = rng.normal(size=(m, k))
@@ -83,7 +86,10 @@ def test_bf16x3_rejects_large_k_and_misaligned(cuda):
     import ctypes
     lib = _lib.load()
     nb = ctypes.c_size_t(0)
-    assert lib.ccl_dht_bf16x3_prepare_bytes(511, 511, ctypes.byref(nb)) == 3
+    assert lib.ccl_dht_bf16x3_prepare_bytes(511, 511, ctypes.byref(nb)) == 0
+    assert nb.value == 2 * 16 * 2 * 256 * 32 * 2  # two halves of 16 chunks, hi + lo
+    assert lib.ccl_dht_bf16x3_prepare_bytes(513, 64, ctypes.byref(nb)) == 3
+    assert lib.ccl_dht_bf16x3_prepare_bytes(64, 513, ctypes.byref(nb)) == 3
     t = torch.zeros(1 << 20, dtype=torch.float32, device="cuda")
     p = t.data_ptr()
     rc = lib.ccl_dht_bf16x3_gemm_batch(1, 64, 64, ints([64]), 0, PP([p]), PP([p + 4]),
@@ -117,6 +123,31 @@ def test_bf16x3_batch_many_items(cuda):
         Rc = (Y0[i][:, 0::2] + 1j * Y0[i][:, 1::2]) + al * (T[:, 0::2] + 1j * T[:, 1::2])
         ref = np.empty_like(T)
         ref[:, 0::2], ref[:, 1::2] = Rc.real, Rc.imag
+        err = np.abs(Yd[i].cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err < TOL, (i, err)
+
+
+def test_bf16x3_batch_large_modes(cuda):
+    """The 4096 x 512 grid's transforms: m = k = 511, a batch of complex
+    and real entries with different matrices, accumulation into Y."""
+    rng = np.random.default_rng(17)
+    m = k = 511
+    mats = [rng.normal(size=(m, k)) for _ in range(2)]
+    preps = [prepare(a, CCL_F32) for a in mats]
+    ncols = [8192, 4096, 8192, 1000]
+    which = [0, 1, 1, 0]
+    Xs = [rng.normal(size=(k, n)).astype(np.float32) for n in ncols]
+    Y0 = [rng.normal(size=(m, n)).astype(np.float32) for n in ncols]
+    Xd = [torch.from_numpy(x).cuda() for x in Xs]
+    Yd = [torch.from_numpy(y.copy()).cuda() for y in Y0]
+    call("ccl_dht_bf16x3_gemm_batch", len(ncols), m, k, ints(ncols), 0,
+         PP([preps[w] for w in which]), PP(Xd), longs(ncols), PP(Yd), longs(ncols),
+         -0.5, 0.0, 1.0, _lib.stream())
+    torch.cuda.synchronize()
+    assert _lib.load().ccl_dht_bf16x3_status(1) == 0
+    for i in range(len(ncols)):
+        A32 = mats[which[i]].astype(np.float32).astype(np.float64)
+        ref = Y0[i] - 0.5 * (A32 @ Xs[i].astype(np.float64))
         err = np.abs(Yd[i].cpu().numpy() - ref).max() / np.abs(ref).max()
         assert err < TOL, (i, err)
 
