@@ -343,17 +343,23 @@ __global__ void k_postproc(ptrs<32> f, int Mp1, int Nx, int Nr,
       a[i] = a[i] * dv[ir];
     }
   } else {
+    // complex values as one 8- or 16-byte vector each (same arithmetic)
+    using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+    V2 *c = (V2 *)a;
     long i = (long)ir * Nx + ix;
+    V2 v = c[i];
     if (ir == 1) {
-      T r0 = a[2 * ix], i0 = a[2 * ix + 1];
-      a[2 * i] = (a[2 * i] - r0) * dv[1];
-      a[2 * i + 1] = (a[2 * i + 1] - i0) * dv[1];
-      a[2 * ix] = r0 * dv[0];
-      a[2 * ix + 1] = i0 * dv[0];
+      V2 z = c[ix];
+      v.x = (v.x - z.x) * dv[1];
+      v.y = (v.y - z.y) * dv[1];
+      z.x = z.x * dv[0];
+      z.y = z.y * dv[0];
+      c[ix] = z;
     } else {
-      a[2 * i] = a[2 * i] * dv[ir];
-      a[2 * i + 1] = a[2 * i + 1] * dv[ir];
+      v.x = v.x * dv[ir];
+      v.y = v.y * dv[ir];
     }
+    c[i] = v;
   }
 }
 
