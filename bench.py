@@ -352,11 +352,31 @@ def algorithmic(name, args):
         C = (Nx - 1) * (Nr - 1)
         # x, y, z read; key and sort index written; counts and offsets written
         return n * (3 * b + 4 + 4) + (C + 1) * 4 + (C + 2) * 4, 0.0
-    if name == "ccl_gather_push":
-        dtype, M, n, Nx, Nr = args[0], args[1], args[2], args[13], args[16]
+    if name in ("ccl_gather_push", "ccl_gather_push_cells", "ccl_gather_push_cells_lo"):
+        dtype, M, n = args[0], args[1], args[2]
+        Nx, Nr = (args[13], args[16]) if name == "ccl_gather_push" else (args[14], args[17])
         b = 8 if dtype == 0 else 4
-        # x, y, z, u, g_inv read, u, g_inv written, sort index; E, B read once
-        return n * (7 * b + 4 * b + 4) + 6 * (2 * M + 1) * Nx * Nr * b, 0.0
+        lo = 3 * b if name.endswith("_lo") else 0
+        # x, y, z (+ low parts), u, g_inv read, u, g_inv written, sort index;
+        # E, B read once
+        return n * (7 * b + lo + 4 * b + 4) + 6 * (2 * M + 1) * Nx * Nr * b, 0.0
+    if name == "ccl_push_x_keys":
+        dtype, n, Nx, Nr = args[0], args[1], args[13], args[16]
+        b = 8 if dtype == 0 else 4
+        lo = 6 * b if args[5] else 0  # low parts read and written
+        C = (Nx - 1) * (Nr - 1)
+        # x, y, z, px, py, pz, g_inv read, x, y, z and the key written; counts
+        return n * (10 * b + lo + 4) + (C + 1) * 4, 0.0
+    if name == "ccl_index_sort_keyed":
+        n, Nx, Nr = args[0], args[1], args[2]
+        C = (Nx - 1) * (Nr - 1)
+        # key read, sort index written; counts read, offsets written
+        return n * (4 + 4) + (C + 1) * 4 + (C + 2) * 4, 0.0
+    if name == "ccl_psatd_advance_split":
+        dtype, n = args[0], args[1]
+        b = 8 if dtype == 0 else 4
+        # 8 coefficients + 6 complex fields + 3 sources read, 6 complex written
+        return n * (8 + (6 + 3) * 2 + 6 * 2) * b, 0.0
     if name == "ccl_psatd_advance":
         dtype, n = args[0], args[1]
         b = 8 if dtype == 0 else 4
@@ -609,8 +629,10 @@ def run_ours(args):
     probe = Probe(["ccl_dht_bf16x3_gemm_batch", "ccl_grad_combine", "ccl_rot_combine",
                    "ccl_dht_gemm_batch", "ccl_dht_gemm", "ccl_fft_forward_batch",
                    "ccl_fft_backward_batch", "ccl_damp_batch", "ccl_index_sort",
-                   "ccl_deposit_vector", "ccl_deposit_scalar", "ccl_gather_push",
-                   "ccl_psatd_advance"])
+                   "ccl_push_x_keys", "ccl_index_sort_keyed", "ccl_deposit_vector",
+                   "ccl_deposit_scalar", "ccl_gather_push", "ccl_gather_push_cells",
+                   "ccl_gather_push_cells_lo", "ccl_psatd_advance",
+                   "ccl_psatd_advance_split"])
     orig = install_probe(probe)
     r32["loop"].graphs = False  # the probe times each launch: run the steps eagerly
     for _ in range(min(args.steps, 5)):

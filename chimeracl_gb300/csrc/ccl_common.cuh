@@ -53,6 +53,34 @@ static inline int grid_for(long n, int threads, int per_sm = 8) {
 
 static inline cudaStream_t S(void *stream) { return (cudaStream_t)stream; }
 
+// Programmatic dependent launch.  A kernel started by launch_pdl may be
+// placed on the SMs while the kernel before it in the stream is finishing
+// (the launch and set-up of the next grid overlap the last CTAs of this
+// one).  Such a kernel calls pdl_wait() before it touches any memory an
+// earlier kernel reads or writes: it returns once those kernels have
+// completed and their writes are visible (in a kernel launched the ordinary
+// way it returns at once).  In a CUDA graph the dependency becomes a
+// programmatic edge.  (Releasing the next grid early, before this one's
+// CTAs have all exited, measured slower on the step: its waiting CTAs take
+// SM slots from this grid's last wave.)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                     cudaStream_t s, Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // Complex number of real type T, laid out as (re, im).
 template <typename T> struct cplx {
   T re, im;

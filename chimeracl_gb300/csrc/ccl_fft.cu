@@ -429,6 +429,7 @@ __device__ __forceinline__ void fft_reg(cplx<T> (&v)[8], cplx<T> *sm,
 template <typename T, int N>
 __global__ void __launch_bounds__(N / 8)
     k_fft_fwd_reg(FftBatch b, const T *__restrict__ phs, const cplx<T> *__restrict__ tw) {
+  pdl_wait();
   __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
   constexpr int TH = N / 8;
   const int j = threadIdx.x, e = blockIdx.y;
@@ -461,6 +462,7 @@ __global__ void __launch_bounds__(N / 8)
 template <typename T, int N>
 __global__ void __launch_bounds__(N / 8)
     k_fft_bwd_reg(FftBatch b, const T *__restrict__ phs, const cplx<T> *__restrict__ tw) {
+  pdl_wait();
   __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
   constexpr int TH = N / 8;
   const int j = threadIdx.x, e = blockIdx.y;
@@ -489,6 +491,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(N / 8, sizeof(T) == 4 && N <= 2048 ? 6144 / N : 1)
     k_damp_reg(FftBatch b, const T *__restrict__ phs_p, const T *__restrict__ phs_m,
                const T *__restrict__ prof, u32 nf, const cplx<T> *__restrict__ tw) {
+  pdl_wait();
   __shared__ cplx<T> sm[RegFft<N>::SMEM_PTS];
   constexpr int TH = N / 8;
   const int j = threadIdx.x, e = blockIdx.y;
@@ -672,7 +675,8 @@ int fft_forward_batch(int batch, int nrows, int nx, const void *const *in,
   const cplx<T> *tw = twiddles<T>(nx, s, &why);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
-#define CCL_L(NN) k_fft_fwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
+#define CCL_L(NN) \
+  launch_pdl(k_fft_fwd_reg<T, NN>, dim3(nrows, batch), NN / 8, 0, s, b, (const T *)phs, tw)
     CCL_REG_DISPATCH(nx, CCL_L)
 #undef CCL_L
   } else {
@@ -709,7 +713,8 @@ int fft_backward_batch(int batch, int nrows, int nx, const void *const *in,
   const cplx<T> *tw = twiddles<T>(nx, s, &why);
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
-#define CCL_L(NN) k_fft_bwd_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs, tw)
+#define CCL_L(NN) \
+  launch_pdl(k_fft_bwd_reg<T, NN>, dim3(nrows, batch), NN / 8, 0, s, b, (const T *)phs, tw)
     CCL_REG_DISPATCH(nx, CCL_L)
 #undef CCL_L
   } else {
@@ -746,8 +751,8 @@ int damp_batch(int batch, int nrows, int nx, void *const *spec,
   CCL_REQUIRE(tw, CCL_ERR_CUDA, "fft: twiddle table for nx=%d: %s", nx, why);
   if (reg_size<T>(nx)) {
 #define CCL_L(NN)                                                                           \
-  k_damp_reg<T, NN><<<dim3(nrows, batch), NN / 8, 0, s>>>(b, (const T *)phs_p, (const T *)phs_m, \
-                                                          (const T *)prof, (u32)nf, tw)
+  launch_pdl(k_damp_reg<T, NN>, dim3(nrows, batch), NN / 8, 0, s, b, (const T *)phs_p,        \
+             (const T *)phs_m, (const T *)prof, (u32)nf, tw)
     CCL_REG_DISPATCH(nx, CCL_L)
 #undef CCL_L
   } else {

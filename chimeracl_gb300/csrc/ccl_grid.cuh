@@ -155,6 +155,7 @@ __global__ void __launch_bounds__(DEP_THREADS)
               const T *__restrict__ w, T q, GridP<T> g, ptrs<12> f,
               const T *__restrict__ xl = nullptr, const T *__restrict__ yl = nullptr,
               const T *__restrict__ zl = nullptr) {
+  pdl_wait();
   constexpr int NK = VEC ? 3 : 1;       // vector components
   constexpr int NQ = NK * (1 + 2 * M);  // reals per node
   __shared__ T acc[NQ][DEP_NTR][DEP_NTX];
@@ -264,9 +265,9 @@ void deposit_launch(dim3 grid, const u32 *sort_indx, const u32 *cell_off, const 
                          cudaFuncAttributePreferredSharedMemoryCarveout, DEP_CARVEOUT);
     set = true;
   }
-  k_deposit<T, M, VEC, LO><<<grid, DEP_THREADS, 0, s>>>(
-      sort_indx, cell_off, x, y, z, ux, uy, uz, g_inv, w, q, g, f, LO ? lo[0] : nullptr,
-      LO ? lo[1] : nullptr, LO ? lo[2] : nullptr);
+  launch_pdl(k_deposit<T, M, VEC, LO>, grid, DEP_THREADS, 0, s, sort_indx, cell_off, x, y, z, ux,
+             uy, uz, g_inv, w, q, g, f, LO ? lo[0] : nullptr, LO ? lo[1] : nullptr,
+             LO ? lo[2] : nullptr);
 }
 
 // lo: nullptr, or the low parts {x_lo, y_lo, z_lo} of compensated FP32
@@ -328,6 +329,7 @@ int deposit(int M, const u32 *sort_indx, const u32 *cell_off, const T *x,
 template <typename T>
 __global__ void k_postproc(ptrs<32> f, int Mp1, int Nx, int Nr,
                            const T *__restrict__ dv) {
+  pdl_wait();
   const int pidx = blockIdx.z, m = pidx % Mp1;
   const int ir = blockIdx.y + 1;
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,6 +368,7 @@ __global__ void k_postproc(ptrs<32> f, int Mp1, int Nx, int Nr,
 // warp_axis_m0_d / warp_axis_m1plus_c (grid_generic.cl:63-86)
 template <typename T>
 __global__ void k_warp_axis(ptrs<32> f, int Mp1, int Nx) {
+  pdl_wait();
   const int pidx = blockIdx.y, m = pidx % Mp1;
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
   if (ix >= Nx) return;
@@ -390,6 +393,7 @@ __global__ void __launch_bounds__(256)
                   T *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
                   const u32 *__restrict__ np_stay_p, T dt, GridP<T> g,
                   ptrs<24> f) {
+  pdl_wait();
   const u32 np_stay = *np_stay_p;
   const int Nx = g.Nx, nxc = Nx - 1, nrc = g.Nr - 1;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
@@ -479,6 +483,7 @@ __global__ void __launch_bounds__(256)
                       float *__restrict__ g_inv, const u32 *__restrict__ sort_indx,
                       const u32 *__restrict__ np_stay_p, float dt, GridP<float> g,
                       ptrs<24> f) {
+  pdl_wait();
   const u32 np_stay = *np_stay_p;
   const int Nx = g.Nx, nxc = Nx - 1, nrc = g.Nr - 1;
   const float dt_2 = 0.5f * dt;
@@ -583,6 +588,7 @@ __global__ void __launch_bounds__(GT_THREADS)
                         const float *__restrict__ xl = nullptr,
                         const float *__restrict__ yl = nullptr,
                         const float *__restrict__ zl = nullptr) {
+  pdl_wait();
   constexpr int NS = gt_stride(M);
   extern __shared__ __align__(16) float gsm[];  // [GT_NR][GT_NX][NS]
   __shared__ u32 row_a[GT_TR], row_pre[GT_TR + 1];
@@ -752,10 +758,10 @@ int gather_push(int M, long np, const T *x, const T *y, const T *z, T *px,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 0);         \
       set = true;                                                                      \
     }                                                                                  \
-    k_gather_push_f32<MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx, \
+    launch_pdl(k_gather_push_f32<MM>, nb, 256, 0, s, np, x, y, z, px, py, pz, g_inv, sort_indx, \
                                              np_stay, dt, g, f);                       \
   } else                                                                               \
-    k_gather_push<T, MM><<<nb, 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv, sort_indx,  \
+    launch_pdl(k_gather_push<T, MM>, nb, 256, 0, s, np, x, y, z, px, py, pz, g_inv, sort_indx,  \
                                             np_stay, dt, g, f)
   switch (M) {
     case 0: CCL_GP(0); break;
@@ -801,9 +807,9 @@ int gather_push_cells(int M, long np, const T *x, const T *y, const T *z, T *px,
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
       set[lo != nullptr] = true;                                                           \
     }                                                                                      \
-    kern<<<grid, GT_THREADS, smem, s>>>(x, y, z, px, py, pz, g_inv, sort_indx, cell_off,    \
-                                        np_stay, dt, g, f, lo ? lo[0] : nullptr,           \
-                                        lo ? lo[1] : nullptr, lo ? lo[2] : nullptr);       \
+    launch_pdl(kern, grid, GT_THREADS, smem, s, x, y, z, px, py, pz, g_inv, sort_indx,      \
+               cell_off, np_stay, dt, g, f, lo ? lo[0] : nullptr, lo ? lo[1] : nullptr,    \
+               lo ? lo[2] : nullptr);                                                      \
   }
     switch (M) {
       case 0: CCL_GT(0); break;

@@ -127,7 +127,7 @@ int Ops<T>::postproc(int M, int nfld, void *const *flds, int Nx, int Nr,
   }
   if (Nr < 2) return CCL_OK;
   dim3 grid((Nx + 127) / 128, Nr - 1, n);
-  k_postproc<T><<<grid, 128, 0, s>>>(f, M + 1, Nx, Nr, (const T *)dv);
+  launch_pdl(k_postproc<T>, grid, 128, 0, s, f, M + 1, Nx, Nr, (const T *)dv);
   CCL_LAUNCH_CHECK("postproc");
   return CCL_OK;
 }
@@ -143,7 +143,7 @@ int Ops<T>::warp_axis(int M, int nfld, void *const *flds, int Nx,
     f.p[i] = flds[i];
   }
   dim3 grid((Nx + 127) / 128, n);
-  k_warp_axis<T><<<grid, 128, 0, s>>>(f, M + 1, Nx);
+  launch_pdl(k_warp_axis<T>, grid, 128, 0, s, f, M + 1, Nx);
   CCL_LAUNCH_CHECK("warp_axis");
   return CCL_OK;
 }
@@ -187,8 +187,8 @@ int Ops<T>::psatd(long n, double dt_inv, const void *c1, const void *c2,
     f.p[i] = flds[i];
   }
   if (n == 0) return CCL_OK;
-  k_psatd<T><<<grid_for(n, 256), 256, 0, s>>>(n, (T)dt_inv, (const T *)c1,
-                                               (const T *)c2, (const T *)c3, f);
+  launch_pdl(k_psatd<T>, grid_for(n, 256), 256, 0, s, n, (T)dt_inv, (const T *)c1, (const T *)c2,
+             (const T *)c3, f);
   CCL_LAUNCH_CHECK("psatd");
   return CCL_OK;
 }
@@ -203,7 +203,7 @@ int Ops<T>::psatd_split(long n, const void *coef, void *const *flds, cudaStream_
   CCL_REQUIRE(((uintptr_t)coef & 15) == 0, CCL_ERR_ARG,
               "psatd_split: coefficient array not 16-byte aligned");
   if (n == 0) return CCL_OK;
-  k_psatd_split<T><<<grid_for(n, 256), 256, 0, s>>>(n, (const T *)coef, f);
+  launch_pdl(k_psatd_split<T>, grid_for(n, 256), 256, 0, s, n, (const T *)coef, f);
   CCL_LAUNCH_CHECK("psatd_split");
   return CCL_OK;
 }
@@ -248,7 +248,7 @@ int Ops<T>::set_batch(int narr, const int *cplx, const long *n, void *const *a, 
   }
   if (nmax == 0) return CCL_OK;
   dim3 grid((unsigned)((grid_for(nmax, 256) + narr - 1) / narr), (unsigned)narr);
-  k_set_batch<T><<<grid, 256, 0, s>>>(b, (T)re, (T)im);
+  launch_pdl(k_set_batch<T>, grid, 256, 0, s, b, (T)re, (T)im);
   CCL_LAUNCH_CHECK("set_batch");
   return CCL_OK;
 }
@@ -352,7 +352,7 @@ int Ops<T>::grad_combine(int M, int nrows, int nx, const void *kx, const void *c
   long n = (long)nrows * nx;
   if (n == 0) return CCL_OK;
   dim3 grid(grid_for(n, 256, 4), M + 1);
-  k_grad_combine<T><<<grid, 256, 0, s>>>(n, nx, (const T *)kx, r, pm, pp, d);
+  launch_pdl(k_grad_combine<T>, grid, 256, 0, s, n, nx, (const T *)kx, r, pm, pp, d);
   CCL_LAUNCH_CHECK("grad_combine");
   return CCL_OK;
 }
@@ -378,7 +378,7 @@ int Ops<T>::rot_combine(int M, int nrows, int nx, const void *kx, const void *co
   long n = (long)nrows * nx;
   if (n == 0) return CCL_OK;
   dim3 grid(grid_for(n, 256, 4), M + 1);
-  k_rot_combine<T><<<grid, 256, 0, s>>>(n, nx, (const T *)kx, g, qm, qp, po, b);
+  launch_pdl(k_rot_combine<T>, grid, 256, 0, s, n, nx, (const T *)kx, g, qm, qp, po, b);
   CCL_LAUNCH_CHECK("rot_combine");
   return CCL_OK;
 }

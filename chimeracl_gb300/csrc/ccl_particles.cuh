@@ -24,6 +24,7 @@ __global__ void k_push_x(long np, T *__restrict__ x, T *__restrict__ y,
                          T *__restrict__ z, const T *__restrict__ px,
                          const T *__restrict__ py, const T *__restrict__ pz,
                          const T *__restrict__ g_inv, T dt, int vec) {
+  pdl_wait();
   // 16-byte vectors of VW particles when every array is 16-byte aligned, the
   // per-particle arithmetic of push_xyz unchanged; the tail one by one
   constexpr int VW = 16 / sizeof(T);
@@ -59,8 +60,8 @@ int push_x(long np, T *x, T *y, T *z, const T *px, const T *py, const T *pz,
   const uintptr_t mis = ((uintptr_t)x | (uintptr_t)y | (uintptr_t)z | (uintptr_t)px |
                          (uintptr_t)py | (uintptr_t)pz | (uintptr_t)g_inv) & 15;
   if (np == 0) return CCL_OK;
-  k_push_x<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, px, py, pz, g_inv,
-                                                 (T)dt, mis == 0);
+  launch_pdl(k_push_x<T>, grid_for(np, 256), 256, 0, s, np, x, y, z, px, py, pz, g_inv, (T)dt,
+             mis == 0);
   CCL_LAUNCH_CHECK("push_x");
   return CCL_OK;
 }
@@ -110,6 +111,7 @@ __global__ void k_push_x_comp(long np, T *__restrict__ x, T *__restrict__ y,
                               T *__restrict__ zl, const T *__restrict__ px,
                               const T *__restrict__ py, const T *__restrict__ pz,
                               const T *__restrict__ g_inv, T dt, int vec) {
+  pdl_wait();
   constexpr int VW = 16 / sizeof(T);
   using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
   const long nv = vec ? np / VW : 0;
@@ -152,8 +154,8 @@ int push_x_comp(long np, T *x, T *y, T *z, T *xl, T *yl, T *zl, const T *px, con
                          (uintptr_t)yl | (uintptr_t)zl | (uintptr_t)px | (uintptr_t)py |
                          (uintptr_t)pz | (uintptr_t)g_inv) & 15;
   if (np == 0) return CCL_OK;
-  k_push_x_comp<T><<<grid_for(np, 256), 256, 0, s>>>(np, x, y, z, xl, yl, zl, px, py, pz,
-                                                      g_inv, (T)dt, mis == 0);
+  launch_pdl(k_push_x_comp<T>, grid_for(np, 256), 256, 0, s, np, x, y, z, xl, yl, zl, px, py, pz,
+             g_inv, (T)dt, mis == 0);
   CCL_LAUNCH_CHECK("push_x_compensated");
   return CCL_OK;
 }
@@ -306,6 +308,7 @@ __device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32 *sh,
 
 static __global__ void k_scan_reduce(const u32 *__restrict__ in, long L,
                               u32 *__restrict__ part) {
+  pdl_wait();
   __shared__ u32 sh[32];
   long base = (long)blockIdx.x * SCAN_TILE;
   u32 s = 0;
@@ -327,6 +330,7 @@ static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
                             const u32 *__restrict__ part, int sum_parts,
                             u32 *__restrict__ out, u32 *__restrict__ total_out,
                             u32 *__restrict__ tap, long tap_i) {
+  pdl_wait();
   __shared__ u32 sh[32];
   __shared__ u32 tile_pre;
   if (threadIdx.x == 0) tile_pre = 0;
@@ -374,6 +378,7 @@ __global__ void __launch_bounds__(ST_THREADS)
     k_keys(long np, const T *__restrict__ x, const T *__restrict__ y,
            const T *__restrict__ z, GridP<T> g, u32 *__restrict__ keys,
            u32 *__restrict__ counts, u32 *__restrict__ tile_ovf) {
+  pdl_wait();
   __shared__ u32 sh[32];
   const int lane = threadIdx.x & 31;
   const u32 C = (u32)(g.Nx - 1) * (u32)(g.Nr - 1);
@@ -414,6 +419,7 @@ __global__ void __launch_bounds__(ST_THREADS)
                 const T *__restrict__ g_inv, T dt, int vec, GridP<T> g,
                 u32 *__restrict__ keys, u32 *__restrict__ counts,
                 u32 *__restrict__ tile_ovf) {
+  pdl_wait();
   constexpr int VW = 16 / sizeof(T);
   constexpr int NVT = ST_TILE / VW / ST_THREADS;  // vectors per thread
   using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
@@ -512,20 +518,20 @@ static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
   if (L <= 0) return CCL_OK;
   long nb = (L + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 1) {
-    k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, L, nullptr, 0, out, total_out, tap, tap_i);
+    launch_pdl(k_scan_tile, 1, SCAN_THREADS, 0, s, in, L, nullptr, 0, out, total_out, tap, tap_i);
     CCL_LAUNCH_CHECK("scan_tile");
     return CCL_OK;
   }
   u32 *part = ws;
-  k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part);
+  launch_pdl(k_scan_reduce, (unsigned)nb, SCAN_THREADS, 0, s, in, L, part);
   CCL_LAUNCH_CHECK("scan_reduce");
   int fused = nb <= SCAN_FUSE;
   if (!fused) {
     int rc = scan_exclusive(part, nb, part, nullptr, ws + nb, s);
     if (rc) return rc;
   }
-  k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, L, part, fused, out, total_out, tap,
-                                                     tap_i);
+  launch_pdl(k_scan_tile, (unsigned)nb, SCAN_THREADS, 0, s, in, L, part, fused, out, total_out, tap,
+             tap_i);
   CCL_LAUNCH_CHECK("scan_tile");
   return CCL_OK;
 }
@@ -545,6 +551,7 @@ static __global__ void __launch_bounds__(ST_THREADS)
               const u32 *__restrict__ cell_offset, u32 *__restrict__ cursor,
               u32 *__restrict__ multi, const u32 *__restrict__ ovf_off, int ovf_scanned,
               u32 *__restrict__ sort_indx) {
+  pdl_wait();
   __shared__ u32 sh[32];
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -676,6 +683,7 @@ __device__ __forceinline__ void warp_bitonic_sort(u32 *__restrict__ g, u32 n, u3
 static __global__ void __launch_bounds__(FX_WARPS * 32)
     k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, const u32 *__restrict__ multi,
                  u32 *__restrict__ sort_indx) {
+  pdl_wait();
   __shared__ u32 buf[FX_WARPS][FX_BUF];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long stride = (long)gridDim.x * FX_WARPS * 32;
@@ -765,13 +773,12 @@ inline int index_sort_keyed(long np, long C, const u32 *indx, u32 *counts, u32 *
       w.cursor, 0, (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32), s);
   CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the cursors: %s",
               cudaGetErrorString(me));
-  k_scatter<<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, indx, (u32)C, cell_offset,
-                                                    w.cursor, w.multi, w.tile_ovf, ovf_scanned,
-                                                    sort_indx);
+  launch_pdl(k_scatter, (unsigned)ntiles, ST_THREADS, 0, s, np, indx, (u32)C, cell_offset, w.cursor,
+             w.multi, w.tile_ovf, ovf_scanned, sort_indx);
   CCL_LAUNCH_CHECK("scatter");
   if (C > 0)
-    k_cell_fixup<<<grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s>>>((u32)C, cell_offset,
-                                                                       w.multi, sort_indx);
+    launch_pdl(k_cell_fixup, grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s, (u32)C, cell_offset,
+               w.multi, sort_indx);
   CCL_LAUNCH_CHECK("cell_fixup");
   return CCL_OK;
 }
@@ -790,8 +797,8 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
   CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the counts: %s",
               cudaGetErrorString(me));
   if (np > 0) {
-    k_keys<T><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(np, x, y, z, g, indx, counts,
-                                                      w.tile_ovf);
+    launch_pdl(k_keys<T>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, g, indx, counts,
+               w.tile_ovf);
     CCL_LAUNCH_CHECK("keys");
   }
   return index_sort_keyed(np, C, indx, counts, cell_offset, sort_indx, np_stay, ws, ws_bytes,
@@ -817,13 +824,11 @@ int push_keys(long np, T *x, T *y, T *z, T *xl, T *yl, T *zl, const T *px, const
                    (uintptr_t)py | (uintptr_t)pz | (uintptr_t)g_inv) & 15;
   if (xl) {
     mis |= ((uintptr_t)xl | (uintptr_t)yl | (uintptr_t)zl) & 15;
-    k_push_keys<T, true><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(
-        np, x, y, z, xl, yl, zl, px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts,
-        w.tile_ovf);
+    launch_pdl(k_push_keys<T, true>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, xl, yl, zl,
+               px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf);
   } else {
-    k_push_keys<T, false><<<(unsigned)ntiles, ST_THREADS, 0, s>>>(
-        np, x, y, z, nullptr, nullptr, nullptr, px, py, pz, g_inv, (T)dt, mis == 0, g, indx,
-        counts, w.tile_ovf);
+    launch_pdl(k_push_keys<T, false>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, nullptr,
+               nullptr, nullptr, px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf);
   }
   CCL_LAUNCH_CHECK("push_x_keys");
   return CCL_OK;

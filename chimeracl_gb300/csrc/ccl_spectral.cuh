@@ -19,6 +19,7 @@ __global__ void __launch_bounds__(256)
     k_psatd(long n, T dt_inv, const T *__restrict__ c1m,
             const T *__restrict__ c2m, const T *__restrict__ c3m,
             ptrs<15> f) {
+  pdl_wait();
   const T pi2 = T(2) * T(M_PI);
   CCL_GRID_STRIDE(i, n) {
     const T c1 = c1m[i], c2 = c2m[i], c3 = c3m[i];
@@ -61,6 +62,7 @@ __global__ void __launch_bounds__(256)
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_psatd_split(long n, const T *__restrict__ coef, ptrs<15> f) {
+  pdl_wait();
   CCL_GRID_STRIDE(i, n) {
     T c[8];
     if constexpr (sizeof(T) == 4) {  // two 16-byte loads (the array is 32-byte aligned)
@@ -162,6 +164,7 @@ struct SetBatch {
 };
 template <typename T>
 __global__ void k_set_batch(SetBatch b, T re, T im) {
+  pdl_wait();
   const int e = blockIdx.y;
   T *a = (T *)b.a[e];
   const long n = b.n[e];
@@ -263,6 +266,7 @@ __device__ __forceinline__ cplx<T> ld_mode(const T *p, long i, long ir, long ix,
 template <typename T>
 __global__ void k_grad_combine(long n, int nx, const T *__restrict__ kx, ptrs<4> rho,
                                ptrs<4> Pm, ptrs<4> Pp, ptrs<12> dN) {
+  pdl_wait();
   const int m = blockIdx.y;
   CCL_GRID_STRIDE(i, n) {
     const long ir = i / nx, ix = i - ir * nx;
@@ -288,6 +292,7 @@ __global__ void k_grad_combine(long n, int nx, const T *__restrict__ kx, ptrs<4>
 template <typename T>
 __global__ void k_rot_combine(long n, int nx, const T *__restrict__ kx, ptrs<12> G,
                               ptrs<12> Qm, ptrs<12> Qp, ptrs<4> poiss, ptrs<12> B) {
+  pdl_wait();
   const int m = blockIdx.y;
   CCL_GRID_STRIDE(i, n) {
     const long ir = i / nx, ix = i - ir * nx;

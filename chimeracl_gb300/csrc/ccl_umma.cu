@@ -354,6 +354,9 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // the set-up above touches only this CTA's shared and tensor memory: the
+  // operands written by earlier kernels are read after this point
+  pdl_wait();
 
   if (warp < UM_EPI_WARPS) {
     // ------------------------------------------------------------ epilogue
@@ -589,7 +592,7 @@ static void umma_launch(int grid, size_t smem, const UmmaArgs &args, int m, int 
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     set_smem = smem;
   }
-  kern<<<grid, UM_THREADS2, smem, s>>>(args, m, k, ar, ai);
+  launch_pdl(kern, grid, UM_THREADS2, smem, s, args, m, k, ar, ai);
 }
 
 int umma_gemm_batch(int batch, int m, int k, const int *ncols, int cplx, const void *const *Ap,
