@@ -637,96 +637,139 @@ __global__ void __launch_bounds__(GT_THREADS)
   __syncthreads();
   const u32 total = row_pre[GT_TR];
   const float dt_2 = 0.5f * dt;
-  for (u32 idx = threadIdx.x; idx < total; idx += GT_THREADS) {
-    int r = 0;
+  // two particles per thread and pass: both particles' loads are issued
+  // before either's results are stored (a store to px[p] would otherwise
+  // keep the next particle's loads from being hoisted above it)
+  constexpr int GP = 2;
+  for (u32 i0 = threadIdx.x; i0 < total; i0 += GP * GT_THREADS) {
+    u32 pp[GP];
+    int rr_[GP];
+    bool ok[GP];
 #pragma unroll
-    for (int q = 1; q < GT_TR; q++) r += idx >= row_pre[q];
-    const u32 pos = row_a[r] + (idx - row_pre[r]);
-    const u32 p = __ldg(sort_indx + pos);
-    if (p >= np_stay) continue;  // grid_deposit_m1.cl:367-368
-    const float xp = x[p], yp = y[p], zp = z[p];
-    const float r2 = yp * yp + zp * zp;
-    const float rp = sqrtf(r2);
-    const float rinv = r2 > 0.f ? 1.f / rp : __int_as_float(0x7f800000);
-    const float fx = (xp - g.xmin) * g.dx_inv;
-    int ix = (int)floorf(fx);
-    ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
-    float sX1, sR1;
-    if constexpr (LO) {
-      float rr, rrl;
-      radius_pair(yp, zp, yl[p], zl[p], rinv, rr, rrl);
-      const float xlp = xl[p];
-      sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
-      // the index from hi can be one off within an FP32 spacing of a face:
-      // the cell of the full coordinate (within the tile's cells)
-      if (sX1 < 0.f && ix > ixl) {
-        ix--;
-        sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
-      } else if (sX1 >= 1.f && ix < ixh) {
-        ix++;
-        sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+    for (int j = 0; j < GP; j++) {
+      const u32 idx = i0 + (u32)j * GT_THREADS;
+      ok[j] = idx < total;
+      pp[j] = 0;
+      rr_[j] = 0;
+      if (ok[j]) {
+        int r = 0;
+#pragma unroll
+        for (int q = 1; q < GT_TR; q++) r += idx >= row_pre[q];
+        pp[j] = __ldg(sort_indx + row_a[r] + (idx - row_pre[r]));
+        rr_[j] = r;
+        ok[j] = pp[j] < np_stay;  // grid_deposit_m1.cl:367-368
       }
-      sR1 = edge_frac_lo(rr, rrl, redge[r], g.dr_inv);
-    } else {
-      sX1 = edge_frac(xp, xedge[ix - nx0], g.dx_inv);
-      sR1 = edge_frac(rp, redge[r], g.dr_inv);
     }
-    const float sX0 = 1.f - sX1, sR0 = 1.f - sR1;
-    const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
-    const int l0 = (r * GT_NX + (ix - nx0)) * NS;
-    const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};
-    float e[M + 1][2];
-    if (M >= 1) {
-      e[1][0] = yp * rinv;
-      e[1][1] = -zp * rinv;
-    }
+    float vx[GP], vy[GP], vz[GP], vpx[GP], vpy[GP], vpz[GP], vxl[GP], vyl[GP], vzl[GP];
 #pragma unroll
-    for (int m = 2; m <= M; m++) {
-      e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
-      e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
-    }
-    float fld[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      float a = 0.f;
-#pragma unroll
-      for (int c = 0; c < 4; c++) a = fmaf(C[c], gsm[loff[c] + k], a);
-#pragma unroll
-      for (int m = 1; m <= M; m++) {
-        float re = 0.f, im = 0.f;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          re = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k], re);
-          im = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k + 1], im);
+    for (int j = 0; j < GP; j++) {
+      vxl[j] = vyl[j] = vzl[j] = 0.f;
+      if (ok[j]) {
+        const u32 p = pp[j];
+        vx[j] = x[p];
+        vy[j] = y[p];
+        vz[j] = z[p];
+        vpx[j] = px[p];
+        vpy[j] = py[p];
+        vpz[j] = pz[p];
+        if constexpr (LO) {
+          vxl[j] = xl[p];
+          vyl[j] = yl[p];
+          vzl[j] = zl[p];
         }
-        a = fmaf(re, e[m][0], a);
-        a = fmaf(-im, e[m][1], a);
       }
-      fld[k] = a;
     }
-    // Boris push (grid_deposit_m1.cl:440-505)
-    float um[3];
-    um[0] = px[p] + dt_2 * fld[0];
-    um[1] = py[p] + dt_2 * fld[1];
-    um[2] = pz[p] + dt_2 * fld[2];
-    const float gi0 = rsqrtf(1.f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
-    float t[3], sv[3], u0[3], up[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) t[k] = dt_2 * fld[3 + k] * gi0;
-    const float f2 = __fdividef(2.f, 1.f + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-#pragma unroll
-    for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
-    u0[0] = um[0] + um[1] * t[2] - um[2] * t[1];
-    u0[1] = um[1] - um[0] * t[2] + um[2] * t[0];
-    u0[2] = um[2] + um[0] * t[1] - um[1] * t[0];
-    up[0] = um[0] + u0[1] * sv[2] - u0[2] * sv[1];
-    up[1] = um[1] - u0[0] * sv[2] + u0[2] * sv[0];
-    up[2] = um[2] + u0[0] * sv[1] - u0[1] * sv[0];
-    const float u[3] = {up[0] + dt_2 * fld[0], up[1] + dt_2 * fld[1], up[2] + dt_2 * fld[2]};
-    px[p] = u[0];
-    py[p] = u[1];
-    pz[p] = u[2];
-    g_inv[p] = rsqrtf(1.f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    for (int j = 0; j < GP; j++) {
+      if (!ok[j]) continue;
+      const u32 p = pp[j];
+      const int r = rr_[j];
+      const float xp = vx[j], yp = vy[j], zp = vz[j];
+      const float pxp = vpx[j], pyp = vpy[j], pzp = vpz[j];
+      const float xlp = vxl[j], ylp = vyl[j], zlp = vzl[j];
+      const float r2 = yp * yp + zp * zp;
+      const float rp = sqrtf(r2);
+      const float rinv = r2 > 0.f ? 1.f / rp : __int_as_float(0x7f800000);
+      const float fx = (xp - g.xmin) * g.dx_inv;
+      int ix = (int)floorf(fx);
+      ix = ix < ixl ? ixl : (ix > ixh ? ixh : ix);
+      float sX1, sR1;
+      if constexpr (LO) {
+        float rr, rrl;
+        radius_pair(yp, zp, ylp, zlp, rinv, rr, rrl);
+        sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+        // the index from hi can be one off within an FP32 spacing of a face:
+        // the cell of the full coordinate (within the tile's cells)
+        if (sX1 < 0.f && ix > ixl) {
+          ix--;
+          sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+        } else if (sX1 >= 1.f && ix < ixh) {
+          ix++;
+          sX1 = edge_frac_lo(xp, xlp, xedge[ix - nx0], g.dx_inv);
+        }
+        sR1 = edge_frac_lo(rr, rrl, redge[r], g.dr_inv);
+      } else {
+        sX1 = edge_frac(xp, xedge[ix - nx0], g.dx_inv);
+        sR1 = edge_frac(rp, redge[r], g.dr_inv);
+      }
+      const float sX0 = 1.f - sX1, sR0 = 1.f - sR1;
+      const float C[4] = {sR0 * sX0, sR0 * sX1, sR1 * sX0, sR1 * sX1};
+      const int l0 = (r * GT_NX + (ix - nx0)) * NS;
+      const int loff[4] = {l0, l0 + NS, l0 + GT_NX * NS, l0 + (GT_NX + 1) * NS};
+      float e[M + 1][2];
+      if (M >= 1) {
+        e[1][0] = yp * rinv;
+        e[1][1] = -zp * rinv;
+      }
+  #pragma unroll
+      for (int m = 2; m <= M; m++) {
+        e[m][0] = e[m - 1][0] * e[1][0] - e[m - 1][1] * e[1][1];
+        e[m][1] = e[m - 1][0] * e[1][1] + e[m - 1][1] * e[1][0];
+      }
+      float fld[6];
+  #pragma unroll
+      for (int k = 0; k < 6; k++) {
+        float a = 0.f;
+  #pragma unroll
+        for (int c = 0; c < 4; c++) a = fmaf(C[c], gsm[loff[c] + k], a);
+  #pragma unroll
+        for (int m = 1; m <= M; m++) {
+          float re = 0.f, im = 0.f;
+  #pragma unroll
+          for (int c = 0; c < 4; c++) {
+            re = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k], re);
+            im = fmaf(C[c], gsm[loff[c] + 6 + 12 * (m - 1) + 2 * k + 1], im);
+          }
+          a = fmaf(re, e[m][0], a);
+          a = fmaf(-im, e[m][1], a);
+        }
+        fld[k] = a;
+      }
+      // Boris push (grid_deposit_m1.cl:440-505)
+      float um[3];
+      um[0] = pxp + dt_2 * fld[0];
+      um[1] = pyp + dt_2 * fld[1];
+      um[2] = pzp + dt_2 * fld[2];
+      const float gi0 = rsqrtf(1.f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+      float t[3], sv[3], u0[3], up[3];
+  #pragma unroll
+      for (int k = 0; k < 3; k++) t[k] = dt_2 * fld[3 + k] * gi0;
+      const float f2 = __fdividef(2.f, 1.f + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+  #pragma unroll
+      for (int k = 0; k < 3; k++) sv[k] = t[k] * f2;
+      u0[0] = um[0] + um[1] * t[2] - um[2] * t[1];
+      u0[1] = um[1] - um[0] * t[2] + um[2] * t[0];
+      u0[2] = um[2] + um[0] * t[1] - um[1] * t[0];
+      up[0] = um[0] + u0[1] * sv[2] - u0[2] * sv[1];
+      up[1] = um[1] - u0[0] * sv[2] + u0[2] * sv[0];
+      up[2] = um[2] + u0[0] * sv[1] - u0[1] * sv[0];
+      const float u[3] = {up[0] + dt_2 * fld[0], up[1] + dt_2 * fld[1], up[2] + dt_2 * fld[2]};
+      px[p] = u[0];
+      py[p] = u[1];
+      pz[p] = u[2];
+      g_inv[p] = rsqrtf(1.f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+
+    }
   }
 }
 
