@@ -172,22 +172,24 @@ __global__ void k_umma_split_a(const TA *__restrict__ A, int m, int k, int np, i
 // of A, K = 16 per instruction.  Each X tile is therefore read and converted
 // once for all output rows of a half (m <= 256: for all of them); A streams
 // per K chunk from L2 (it is shared by every CTA).
-//   warps 0-3  epilogue: TMEM lane = X column n, TMEM column = output row i;
-//              alpha (complex pairs are adjacent columns n, n+1: one shuffle),
-//              optional +Y, stores of 32 consecutive columns of one row per
-//              instruction (128 contiguous bytes)
-//   warps 4-11 converters: raw FP32 stage (32 k x 128 n) -> K-major bf16
+//   warps 0-7  epilogue: TMEM lane = X column n, TMEM column = output row i;
+//              warps w and w + 4 share lanes 32(w % 4) .. + 31 (the lanes a
+//              warp may read) and take the first and the second half of the
+//              rows; alpha (complex pairs are adjacent columns n, n+1: one
+//              shuffle), optional +Y, stores of 32 consecutive columns of one
+//              row per instruction (128 contiguous bytes)
+//   warps 8-15 converters: raw FP32 stage (32 k x 128 n) -> K-major bf16
 //              hi/lo core matrices in a ring of UM_NS slots
-//   warp 12    lane 0: producer -- per stage one 2-D tensor copy of X into a
+//   warp 16    lane 0: producer -- per stage one 2-D tensor copy of X into a
 //              ring of UM_NR raw slots (out-of-range rows/columns read as 0)
 //              and one bulk copy of A's K chunk into a ring of UM_NA slots
-//   warp 13    lane 0: the MMAs (X_hi A_hi, X_lo A_hi, X_hi A_lo per 16-deep k
+//   warp 17    lane 0: the MMAs (X_hi A_hi, X_lo A_hi, X_hi A_lo per 16-deep k
 //              step) into double-buffered 128 x NP FP32 accumulators in TMEM
 // Every wait is bounded (and gives up early once another role has aborted);
 // the MMA thread drains its MMAs and the producer its copies before the CTA
 // releases TMEM and exits.
-constexpr int UM_EPI_WARPS = 4, UM_CVT_WARPS = 8;
-constexpr int UM_THREADS2 = (UM_EPI_WARPS + UM_CVT_WARPS + 2) * 32;  // 448
+constexpr int UM_EPI_WARPS = 8, UM_CVT_WARPS = 8;
+constexpr int UM_THREADS2 = (UM_EPI_WARPS + UM_CVT_WARPS + 2) * 32;  // 576
 constexpr int UM_TN = 128;        // X columns per work item (the MMA's M)
 constexpr int UM_NS = 3;          // bf16 X slots
 constexpr int UM_NR = 4;          // raw FP32 X slots
@@ -373,16 +375,19 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
       }
       tc_fence_after();
       const int N = w.ncols[e];
-      const int n = nt * UM_TN + warp * 32 + lane;  // this lane's column of X and Y
+      const int quarter = warp & 3, part = warp >> 2;  // TMEM lanes, row part
+      const int n = nt * UM_TN + quarter * 32 + lane;  // this lane's column of X and Y
       const bool nin = n < N;
       const long ldy = w.ldy[e];
       float *__restrict__ ycol = w.Y[e] + n;
       if (h) ycol += (long)NP * ldy;  // first row of the half
-      const uint32_t tb = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * NP);
+      const uint32_t tb = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * NP);
       const int mrow = M - h * NP < NP ? M - h * NP : NP;  // rows of this half
-      float *yp = ycol;  // row i of this lane's column
+      const int r0 = part * (NP / 2);                     // this warp's rows r0 ..
+      const int r1 = mrow < r0 + NP / 2 ? mrow : r0 + NP / 2;
+      float *yp = ycol + (long)r0 * ldy;  // row i of this lane's column
 #pragma unroll 1
-      for (int i0c = 0; i0c < mrow; i0c += 32) {
+      for (int i0c = r0; i0c < r1; i0c += 32) {
         float v[32];
         tmem_ld16(tb + i0c, v);  // two loads in flight per wait
         tmem_ld16(tb + i0c + 16, v + 16);
@@ -396,7 +401,7 @@ __global__ void __launch_bounds__(UM_THREADS2, 1)
           } else {
             r = are * v[t];
           }
-          if (nin && i0c + t < mrow) {
+          if (nin && i0c + t < r1) {
             if (ACC) r += *yp;
             *yp = r;
           }
