@@ -175,9 +175,9 @@ def advance_to(run, n):
         run["loop"].step()
 
 
-def full_run_accuracy(cfg, r32, r64, device_index=0):
+def full_run_accuracy(cfg, device_index=0):
     """The mixed run against the FP64 run on the same seed at the end of the
-    full-length run (FULL_RUN_STEPS, or later if both are past it), beside
+    full-length run (FULL_RUN_STEPS, fresh runs of the workload), beside
     (a) the FP64 run's own sensitivity there -- the FP64 run with its
     injected coordinates and weights rounded to FP32 (2^-24 relative),
     against the FP64 run: with 2x1x4 particles per cell every radial
@@ -185,30 +185,30 @@ def full_run_accuracy(cfg, r32, r64, device_index=0):
     outermost rows are rounding ties -- and (b) the same comparison with
     2x2x4 particles per cell (no ties)."""
     import torch
-    n = max(FULL_RUN_STEPS, r32["loop"].it, r64["loop"].it)
-    advance_to(r32, n)
-    advance_to(r64, n)
-    torch.cuda.synchronize()
+    n = FULL_RUN_STEPS
+
+    def fresh(c, prec, particles_cls=None):
+        run = dict(zip(("solver", "eons", "ions", "loop"),
+                       build_run(c, prec, device_index, particles_cls=particles_cls)))
+        advance_to(run, n)
+        torch.cuda.synchronize()
+        return run
+
+    keys = ("field_energy_rel_err", "wake_ex_rel_err", "kinetic_rel_err", "field_l2_rel_err")
+    r64 = fresh(cfg, "fp64")
+    r32 = fresh(cfg, "mixed")
     acc = compare_runs(cfg, r32, r64)
     acc["layout"] = "x".join(map(str, cfg["eons_in"]["Nppc"]))
     acc["electrons"] = {"mixed": int(r32["eons"].Args["Np"]), "fp64": int(r64["eons"].Args["Np"])}
-    keys = ("field_energy_rel_err", "wake_ex_rel_err", "kinetic_rel_err", "field_l2_rel_err")
-    alt = dict(zip(("solver", "eons", "ions", "loop"),
-                   build_run(cfg, "fp64", device_index, particles_cls=fp32_injected_particles())))
-    advance_to(alt, n)
-    torch.cuda.synchronize()
+    del r32
+    alt = fresh(cfg, "fp64", fp32_injected_particles())
     se = compare_runs(cfg, alt, r64)
     acc["fp64_self_sensitivity"] = {k: se[k] for k in keys}
-    del alt
+    del alt, r64
     torch.cuda.empty_cache()
     cfg2 = copy.deepcopy(cfg)
     cfg2["eons_in"]["Nppc"] = (2, 2, 4)
-    pair = {}
-    for prec in ("fp64", "mixed"):
-        pair[prec] = dict(zip(("solver", "eons", "ions", "loop"),
-                              build_run(cfg2, prec, device_index)))
-        advance_to(pair[prec], n)
-    torch.cuda.synchronize()
+    pair = {prec: fresh(cfg2, prec) for prec in ("fp64", "mixed")}
     a2 = compare_runs(cfg2, pair["mixed"], pair["fp64"])
     acc2 = {k: a2[k] for k in keys + ("at_step",)}
     acc2["layout"] = "2x2x4"
@@ -666,7 +666,7 @@ def run_ours(args):
     r64 = time_arm(cfg, "fp64", args.steps, args.warmup, local, dist)
     # accuracy of the mixed run vs the FP64 run at the end of the full run
     # (untimed: both runs are stepped on to the workload's 500 steps)
-    acc, acc2 = ({}, {}) if args.no_accuracy else full_run_accuracy(cfg, r32, r64, local)
+    acc, acc2 = ({}, {}) if args.no_accuracy else full_run_accuracy(cfg, local)
     ms32 = reduce_max(dist, r32["ms"], dev)
     ms64 = reduce_max(dist, r64["ms"], dev)
     np32 = reduce_sum(dist, r32["np_sum"], dev)

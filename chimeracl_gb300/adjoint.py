@@ -47,6 +47,7 @@ import torch
 from ._lib import PP, call, ints, longs, stream
 from .checkpoint import restore_checkpoint, save_checkpoint
 from .methods.solver_methods_cu import psatd_split_coefficients
+from .pic_loop import capture_guard
 
 VEC = ("x", "y", "z")
 
@@ -496,7 +497,7 @@ class PICAdjoint:
                 self._cap_stream = torch.cuda.Stream()
             now = torch.cuda.current_stream()
             self._cap_stream.wait_stream(now)
-            with torch.cuda.stream(self._cap_stream):
+            with torch.cuda.stream(self._cap_stream), capture_guard():
                 g.capture_begin()
                 try:
                     self._reverse_body(cur)

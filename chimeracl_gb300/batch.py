@@ -57,6 +57,8 @@ import time
 
 import torch
 
+from .pic_loop import capture_guard
+
 
 class PIC_batch:
     def __init__(self, loops, lanes=None, candidates=None, tune_steps=3, one_graph=False):
@@ -158,7 +160,7 @@ class PIC_batch:
         g = torch.cuda.CUDAGraph()
         cur = torch.cuda.current_stream()
         cap.wait_stream(cur)
-        with torch.cuda.stream(cap):
+        with torch.cuda.stream(cap), capture_guard():
             g.capture_begin()
             try:
                 for i, (lp, s) in enumerate(zip(self.loops, streams)):

@@ -17,9 +17,12 @@ following steps read:
   next window shifts);
 * the loop's step count.
 
-``restore_checkpoint`` puts that state back, rebinding each ``DataDev``
-entry to a fresh copy (so the checkpoint can be restored again), and drops
-the loop's CUDA graphs, whose launches name the replaced buffers.  A run
+``restore_checkpoint`` puts that state back: into each ``DataDev`` tensor in
+place where the run's tensor has the saved shape and type (the loop's CUDA
+graphs, whose launches name those buffers, then stay valid: a restored step
+between the same window shifts replays instead of capturing again), else by
+rebinding the entry to a fresh copy; the checkpoint itself is never handed
+out, so it can be restored again.  A run
 restored to step n and stepped to step m reproduces, bit for bit, the run
 that went from n to m before (the kernels are deterministic), which is
 what a recompute-from-checkpoint scheme needs.
@@ -35,6 +38,9 @@ import torch
 from .methods.generic_methods_cu import LazyScalar
 
 SCRATCH_PREFIXES = ("_", "buff_fb", "fld_buff")
+# entries that only name another entry's buffer (the solver's current phase
+# factors): not saved, and set again by the code that uses them
+ALIASES = ("phs_shft",)
 # host values a checkpoint stores; anything else in Args (an object such as
 # the ions' InjectorSource species) is a link the run keeps: marked, not
 # copied, and left as it is on restore
@@ -95,7 +101,7 @@ def save_checkpoint(loop):
     objs = {}
     for kind, i, obj in _objects(loop):
         dev = {k: v.clone() for k, v in obj.DataDev.items()
-               if isinstance(v, torch.Tensor) and not _is_scratch(k)}
+               if isinstance(v, torch.Tensor) and not _is_scratch(k) and k not in ALIASES}
         entry = {"dev": dev, "args": _args_copy(obj.Args)}
         rng = getattr(obj, "_rng", None)
         if rng is not None:
@@ -106,12 +112,48 @@ def save_checkpoint(loop):
     return Checkpoint(loop.it, objs)
 
 
+def _copy_into(pairs):
+    """dst <- src for (dst, src) tensor pairs: the library's batched copy
+    (32 per launch) for contiguous device tensors of whole 4-byte words,
+    torch's copy for the rest."""
+    dev = [(d, s_) for d, s_ in pairs if d.is_cuda and d.is_contiguous() and s_.is_contiguous()
+           and (s_.numel() * s_.element_size()) % 4 == 0 and s_.numel()]
+    ids = {id(d) for d, _ in dev}
+    for d, s_ in pairs:
+        if id(d) not in ids:
+            d.copy_(s_)
+    if dev:
+        from ._lib import PP, call, longs, stream
+        for k in range(0, len(dev), 32):
+            part = dev[k:k + 32]
+            call("ccl_copy_batch", len(part), longs([s_.numel() * s_.element_size()
+                                                     for _, s_ in part]),
+                 PP([d for d, _ in part]), PP([s_ for _, s_ in part]), stream())
+
+
 def restore_checkpoint(loop, ckpt):
     """Put the run back to the checkpoint's step."""
+    pairs = []
     for kind, i, obj in _objects(loop):
         entry = ckpt.objs[(kind, i)]
+        # buffers that two entries name now are rebound, never written
+        # through (the named aliases aside)
+        ptrs = {}
+        for k, t in obj.DataDev.items():
+            if isinstance(t, torch.Tensor) and t.numel() and k not in ALIASES:
+                ptrs.setdefault(t.data_ptr(), []).append(k)
+        shared = {k for ks in ptrs.values() if len(ks) > 1 for k in ks}
         for k, v in entry["dev"].items():
-            obj.DataDev[k] = v.clone()
+            if k in ALIASES:
+                continue
+            cur = obj.DataDev.get(k)
+            if (isinstance(cur, torch.Tensor) and k not in shared and cur.shape == v.shape
+                    and cur.dtype == v.dtype and cur.device == v.device):
+                pairs.append((cur, v))  # the same buffer: captured launches stay valid
+            else:
+                obj.DataDev[k] = v.clone()
+        if hasattr(obj, "_phs_cache"):
+            obj._phs_cache = {}  # phase factors: recomputed for the restored origin
         args = obj.Args
         for k in list(args.keys()):
             if k not in entry["args"]:
@@ -125,10 +167,10 @@ def restore_checkpoint(loop, ckpt):
             obj._rng.bit_generator.state = copy.deepcopy(entry["rng"])
         if "flag_sorted" in entry:
             obj.flag_sorted = entry["flag_sorted"]
+    _copy_into(pairs)
     loop.it = ckpt.it
-    # captured launches name the replaced buffers; signatures would force
-    # new captures, dropping the graphs frees their memory now
-    loop._graphs = {}
+    # a graph whose buffers were rebound, or whose particle counts or grid
+    # origin differ, fails its signature check and is captured again
 
 
 def state_dict(ckpt):

@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(AT_THREADS)
                   T *__restrict__ lx, T *__restrict__ ly, T *__restrict__ lz,
                   T *__restrict__ lw, T *__restrict__ lux, T *__restrict__ luy,
                   T *__restrict__ luz, T *__restrict__ lg) {
+  pdl_wait();
   constexpr int NK = VEC ? 3 : 1, B = 1 + 2 * M, NS = NK * B;
   extern __shared__ __align__(16) unsigned char adj_sm[];
   T *nsm = (T *)adj_sm;  // [AT_NR][AT_NX][NS]
@@ -294,6 +295,7 @@ __global__ void __launch_bounds__(AT_THREADS)
                       ptrs<24> lF, T *__restrict__ lx, T *__restrict__ ly, T *__restrict__ lz,
                       T *__restrict__ lux, T *__restrict__ luy, T *__restrict__ luz,
                       T *__restrict__ lg) {
+  pdl_wait();
   constexpr int NS = 6 * (1 + 2 * M);
   extern __shared__ __align__(16) unsigned char adj_sm[];
   T *fsm = (T *)adj_sm;                     // [AT_NR][AT_NX][NS] fields (m >= 1 doubled)
@@ -504,6 +506,7 @@ __global__ void k_push_x_adj(long np, const T *__restrict__ ux, const T *__restr
                              const T *__restrict__ lz, T *__restrict__ lux,
                              T *__restrict__ luy, T *__restrict__ luz, T *__restrict__ lg,
                              T dt) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np;
        i += (long)gridDim.x * blockDim.x) {
     const T gd = g_inv[i] * dt;
@@ -529,6 +532,7 @@ __global__ void k_push_x_adj(long np, const T *__restrict__ ux, const T *__restr
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_psatd_adj(long n, const T *__restrict__ coef, const T *__restrict__ filt, ptrs<15> f) {
+  pdl_wait();
   CCL_GS(i, n) {
     const T fj = filt ? filt[i] : T(1);
     T c[8];
@@ -568,6 +572,7 @@ __device__ __forceinline__ cplx<T> mirror_at(const T *p, long ir, long ix, int n
 template <typename T>
 __global__ void k_grad_adj_pre(long n, int nx, int M, const T *__restrict__ kx, ptrs<12> ldN,
                                ptrs<4> lrho, ptrs<4> Pm, ptrs<4> Pp) {
+  pdl_wait();
   const int m = blockIdx.y;
   CCL_GS(i, n) {
     const long ir = i / nx, ix = i - ir * nx;
@@ -604,6 +609,7 @@ __global__ void k_grad_adj_pre(long n, int nx, int M, const T *__restrict__ kx, 
 template <typename T>
 __global__ void k_modes_adj_post(long n, int M, int ncomp, ptrs<12> lo, ptrs<12> Rm,
                                  ptrs<12> Rp, ptrs<4> filt) {
+  pdl_wait();
   const int j = blockIdx.y / ncomp, c = blockIdx.y - j * ncomp;
   const T *fl = (const T *)filt.p[j];
   CCL_GS(i, n) {
@@ -634,6 +640,7 @@ __global__ void k_modes_adj_post(long n, int M, int ncomp, ptrs<12> lo, ptrs<12>
 template <typename T>
 __global__ void k_rot_adj_pre(long n, int nx, int M, const T *__restrict__ kx, ptrs<4> poiss,
                               ptrs<12> lB, ptrs<12> lG, ptrs<12> Qm, ptrs<12> Qp) {
+  pdl_wait();
   const int m = blockIdx.y;
   CCL_GS(i, n) {
     const long ir = i / nx, ix = i - ir * nx;
@@ -688,6 +695,7 @@ __global__ void k_rot_adj_pre(long n, int nx, int M, const T *__restrict__ kx, p
 // x dv[ir].
 template <typename T>
 __global__ void k_postproc_adj(ptrs<32> f, int Mp1, int Nx, int Nr, const T *__restrict__ dv) {
+  pdl_wait();
   const int pidx = blockIdx.z, m = pidx % Mp1;
   const int ir = blockIdx.y + 1;
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -710,6 +718,7 @@ __global__ void k_postproc_adj(ptrs<32> f, int Mp1, int Nx, int Nr, const T *__r
 // ghost rows transposed: row 0 = +row 1 (m = 0) or -row 1 (m >= 1)
 template <typename T>
 __global__ void k_warp_axis_adj(ptrs<32> f, int Mp1, int Nx) {
+  pdl_wait();
   const int pidx = blockIdx.y, m = pidx % Mp1;
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
   if (ix >= Nx) return;
@@ -733,6 +742,7 @@ struct AddBatch {
 };
 template <typename T>
 __global__ void k_add_batch(AddBatch b) {
+  pdl_wait();
   const int a = blockIdx.y;
   T *d = (T *)b.dst[a];
   const T *s = (const T *)b.src[a];
@@ -742,6 +752,7 @@ __global__ void k_add_batch(AddBatch b) {
 // dst[a][i] = src[a][i] for i < n[a] 32-bit words, a < narr (blockIdx.y)
 template <typename W>
 __global__ void k_copy_batch(AddBatch b) {
+  pdl_wait();
   const int a = blockIdx.y;
   W *d = (W *)b.dst[a];
   const W *s = (const W *)b.src[a];
@@ -752,6 +763,7 @@ __global__ void k_copy_batch(AddBatch b) {
 template <typename T>
 __global__ void k_scatter(long n, int ncomp, ptrs<16> src, ptrs<16> dst,
                           const u32 *__restrict__ idx) {
+  pdl_wait();
   CCL_GS(i, n) {
     const u32 j = idx[i];
     for (int c = 0; c < ncomp; c++) ((T *)dst.p[c])[j] = ((const T *)src.p[c])[i];
@@ -768,6 +780,7 @@ __global__ void k_dens_profile_adj(long np, const T *__restrict__ x, const T *__
                                    const double *__restrict__ ff,
                                    const double *__restrict__ dxm1, u32 nloc,
                                    double *__restrict__ lff) {
+  pdl_wait();
   __shared__ double acc[DP_MAXK];
   for (u32 k = threadIdx.x; k < nloc; k += blockDim.x) acc[k] = 0.0;
   __syncthreads();
@@ -813,9 +826,8 @@ static int deposit_adj_m(const u32 *si, const u32 *co, const T *x, const T *y, c
     set = true;
   }
   dim3 grid((g.Nx + AT_TX - 1) / AT_TX, (g.Nr + AT_TR - 1) / AT_TR);
-  kern<<<grid, AT_THREADS, smem, s>>>(si, co, x, y, z, ux, uy, uz, gi, w,
-                                      (T)(signed char)q, g, L, lx, ly, lz, lw, lux, luy, luz,
-                                      lg);
+  launch_pdl(kern, grid, AT_THREADS, smem, s, si, co, x, y, z, ux, uy, uz, gi, w, (T)(signed char)q,
+             g, L, lx, ly, lz, lw, lux, luy, luz, lg);
   CCL_LAUNCH_CHECK("deposit_adjoint");
   return CCL_OK;
 }
@@ -840,8 +852,8 @@ static int gather_push_adj_m(const T *x, const T *y, const T *z, const T *ux, co
     set = true;
   }
   dim3 grid((g.Nx + AT_TX - 1) / AT_TX, (g.Nr + AT_TR - 1) / AT_TR);
-  kern<<<grid, AT_THREADS, smem, s>>>(x, y, z, ux, uy, uz, si, co, np_stay, (T)factor, g, f, lf,
-                                      lx, ly, lz, lux, luy, luz, lg);
+  launch_pdl(kern, grid, AT_THREADS, smem, s, x, y, z, ux, uy, uz, si, co, np_stay, (T)factor, g, f,
+             lf, lx, ly, lz, lux, luy, luz, lg);
   CCL_LAUNCH_CHECK("gather_push_adjoint");
   return CCL_OK;
 }
@@ -969,15 +981,14 @@ int ccl_push_x_adjoint(int dtype, long np, const void *ux, const void *uy, const
   ADJ_NONNULL(lg);
   const int nb = grid_for(np, 256);
   if (dtype == CCL_F64)
-    k_push_x_adj<double><<<nb, 256, 0, S(stream)>>>(
-        np, (const double *)ux, (const double *)uy, (const double *)uz, (const double *)g_inv,
-        (const double *)lx, (const double *)ly, (const double *)lz, (double *)lux,
-        (double *)luy, (double *)luz, (double *)lg, dt);
+    launch_pdl(k_push_x_adj<double>, nb, 256, 0, S(stream), np, (const double *)ux,
+               (const double *)uy, (const double *)uz, (const double *)g_inv, (const double *)lx,
+               (const double *)ly, (const double *)lz, (double *)lux, (double *)luy, (double *)luz,
+               (double *)lg, dt);
   else
-    k_push_x_adj<float><<<nb, 256, 0, S(stream)>>>(
-        np, (const float *)ux, (const float *)uy, (const float *)uz, (const float *)g_inv,
-        (const float *)lx, (const float *)ly, (const float *)lz, (float *)lux, (float *)luy,
-        (float *)luz, (float *)lg, (float)dt);
+    launch_pdl(k_push_x_adj<float>, nb, 256, 0, S(stream), np, (const float *)ux, (const float *)uy,
+               (const float *)uz, (const float *)g_inv, (const float *)lx, (const float *)ly,
+               (const float *)lz, (float *)lux, (float *)luy, (float *)luz, (float *)lg, (float)dt);
   CCL_LAUNCH_CHECK("push_x_adjoint");
   return CCL_OK;
 }
@@ -995,11 +1006,11 @@ int ccl_psatd_adjoint(int dtype, long ncells, const void *coef, const void *filt
   }
   const int nb = grid_for(ncells, 256);
   if (dtype == CCL_F64)
-    k_psatd_adj<double><<<nb, 256, 0, S(stream)>>>(ncells, (const double *)coef,
-                                                    (const double *)filter, f);
+    launch_pdl(k_psatd_adj<double>, nb, 256, 0, S(stream), ncells, (const double *)coef,
+               (const double *)filter, f);
   else
-    k_psatd_adj<float><<<nb, 256, 0, S(stream)>>>(ncells, (const float *)coef,
-                                                   (const float *)filter, f);
+    launch_pdl(k_psatd_adj<float>, nb, 256, 0, S(stream), ncells, (const float *)coef,
+               (const float *)filter, f);
   CCL_LAUNCH_CHECK("psatd_adjoint");
   return CCL_OK;
 }
@@ -1026,11 +1037,11 @@ int ccl_grad_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx
   if (n == 0) return CCL_OK;
   dim3 grid(grid_for(n, 256, 4), M + 1);
   if (dtype == CCL_F64)
-    k_grad_adj_pre<double><<<grid, 256, 0, S(stream)>>>(n, nx, M, (const double *)kx, a, r, pm,
-                                                         pp);
+    launch_pdl(k_grad_adj_pre<double>, grid, 256, 0, S(stream), n, nx, M, (const double *)kx, a, r,
+               pm, pp);
   else
-    k_grad_adj_pre<float><<<grid, 256, 0, S(stream)>>>(n, nx, M, (const float *)kx, a, r, pm,
-                                                        pp);
+    launch_pdl(k_grad_adj_pre<float>, grid, 256, 0, S(stream), n, nx, M, (const float *)kx, a, r,
+               pm, pp);
   CCL_LAUNCH_CHECK("grad_combine_adjoint");
   return CCL_OK;
 }
@@ -1064,11 +1075,11 @@ int ccl_rot_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx,
   if (n == 0) return CCL_OK;
   dim3 grid(grid_for(n, 256, 4), M + 1);
   if (dtype == CCL_F64)
-    k_rot_adj_pre<double><<<grid, 256, 0, S(stream)>>>(n, nx, M, (const double *)kx, po, b, g,
-                                                        qm, qp);
+    launch_pdl(k_rot_adj_pre<double>, grid, 256, 0, S(stream), n, nx, M, (const double *)kx, po, b,
+               g, qm, qp);
   else
-    k_rot_adj_pre<float><<<grid, 256, 0, S(stream)>>>(n, nx, M, (const float *)kx, po, b, g,
-                                                       qm, qp);
+    launch_pdl(k_rot_adj_pre<float>, grid, 256, 0, S(stream), n, nx, M, (const float *)kx, po, b, g,
+               qm, qp);
   CCL_LAUNCH_CHECK("rot_combine_adjoint");
   return CCL_OK;
 }
@@ -1094,9 +1105,9 @@ int ccl_modes_adjoint_accumulate(int dtype, int M, int ncomp, int nrows, int nx,
   if (n == 0) return CCL_OK;
   dim3 grid(grid_for(n, 256, 2), ncomp * (M + 1));
   if (dtype == CCL_F64)
-    k_modes_adj_post<double><<<grid, 256, 0, S(stream)>>>(n, M, ncomp, o, rm, rp, fl);
+    launch_pdl(k_modes_adj_post<double>, grid, 256, 0, S(stream), n, M, ncomp, o, rm, rp, fl);
   else
-    k_modes_adj_post<float><<<grid, 256, 0, S(stream)>>>(n, M, ncomp, o, rm, rp, fl);
+    launch_pdl(k_modes_adj_post<float>, grid, 256, 0, S(stream), n, M, ncomp, o, rm, rp, fl);
   CCL_LAUNCH_CHECK("modes_adjoint_accumulate");
   return CCL_OK;
 }
@@ -1121,9 +1132,9 @@ int ccl_add_batch(int dtype, int narr, const long *n, void *const *dst, const vo
   if (nmax == 0) return CCL_OK;
   dim3 grid(grid_for(nmax, 256, 2), narr);
   if (dtype == CCL_F64)
-    k_add_batch<double><<<grid, 256, 0, S(stream)>>>(b);
+    launch_pdl(k_add_batch<double>, grid, 256, 0, S(stream), b);
   else
-    k_add_batch<float><<<grid, 256, 0, S(stream)>>>(b);
+    launch_pdl(k_add_batch<float>, grid, 256, 0, S(stream), b);
   CCL_LAUNCH_CHECK("add_batch");
   return CCL_OK;
 }
@@ -1149,7 +1160,7 @@ int ccl_copy_batch(int narr, const long *nbytes, void *const *dst, const void *c
   }
   if (nmax == 0) return CCL_OK;
   dim3 grid(grid_for(nmax, 256, 4), narr);
-  k_copy_batch<uint32_t><<<grid, 256, 0, S(stream)>>>(b);
+  launch_pdl(k_copy_batch<uint32_t>, grid, 256, 0, S(stream), b);
   CCL_LAUNCH_CHECK("copy_batch");
   return CCL_OK;
 }
@@ -1167,9 +1178,11 @@ int ccl_deposit_postproc_adjoint(int dtype, int M, int nfld, void *const *flds, 
   }
   dim3 grid((Nx + 127) / 128, Nr - 1, nfld * (M + 1));
   if (dtype == CCL_F64)
-    k_postproc_adj<double><<<grid, 128, 0, S(stream)>>>(f, M + 1, Nx, Nr, (const double *)dV_inv);
+    launch_pdl(k_postproc_adj<double>, grid, 128, 0, S(stream), f, M + 1, Nx, Nr,
+               (const double *)dV_inv);
   else
-    k_postproc_adj<float><<<grid, 128, 0, S(stream)>>>(f, M + 1, Nx, Nr, (const float *)dV_inv);
+    launch_pdl(k_postproc_adj<float>, grid, 128, 0, S(stream), f, M + 1, Nx, Nr,
+               (const float *)dV_inv);
   CCL_LAUNCH_CHECK("postproc_adjoint");
   return CCL_OK;
 }
@@ -1186,9 +1199,9 @@ int ccl_warp_axis_adjoint(int dtype, int M, int nfld, void *const *flds, int Nx,
   }
   dim3 grid((Nx + 127) / 128, nfld * (M + 1));
   if (dtype == CCL_F64)
-    k_warp_axis_adj<double><<<grid, 128, 0, S(stream)>>>(f, M + 1, Nx);
+    launch_pdl(k_warp_axis_adj<double>, grid, 128, 0, S(stream), f, M + 1, Nx);
   else
-    k_warp_axis_adj<float><<<grid, 128, 0, S(stream)>>>(f, M + 1, Nx);
+    launch_pdl(k_warp_axis_adj<float>, grid, 128, 0, S(stream), f, M + 1, Nx);
   CCL_LAUNCH_CHECK("warp_axis_adjoint");
   return CCL_OK;
 }
@@ -1208,9 +1221,9 @@ int ccl_align_adjoint(int dtype, long n, int ncomp, void *const *src, void *cons
   }
   const int nb = grid_for(n, 256);
   if (dtype == CCL_F64)
-    k_scatter<double><<<nb, 256, 0, S(stream)>>>(n, ncomp, a, b, sort_indx);
+    launch_pdl(k_scatter<double>, nb, 256, 0, S(stream), n, ncomp, a, b, sort_indx);
   else
-    k_scatter<float><<<nb, 256, 0, S(stream)>>>(n, ncomp, a, b, sort_indx);
+    launch_pdl(k_scatter<float>, nb, 256, 0, S(stream), n, ncomp, a, b, sort_indx);
   CCL_LAUNCH_CHECK("align_adjoint");
   return CCL_OK;
 }
@@ -1227,14 +1240,11 @@ int ccl_dens_profile_adjoint(int dtype, long np, const void *x, const void *w, c
   ADJ_NONNULL(dxm1); ADJ_NONNULL(lff);
   const int nb = grid_for(np, 256, 2);
   if (dtype == CCL_F64)
-    k_dens_profile_adj<double><<<nb, 256, 0, S(stream)>>>(np, (const double *)x,
-                                                          (const double *)w,
-                                                          (const double *)lw, xx, ff, dxm1,
-                                                          nloc, lff);
+    launch_pdl(k_dens_profile_adj<double>, nb, 256, 0, S(stream), np, (const double *)x,
+               (const double *)w, (const double *)lw, xx, ff, dxm1, nloc, lff);
   else
-    k_dens_profile_adj<float><<<nb, 256, 0, S(stream)>>>(np, (const float *)x, (const float *)w,
-                                                         (const float *)lw, xx, ff, dxm1, nloc,
-                                                         lff);
+    launch_pdl(k_dens_profile_adj<float>, nb, 256, 0, S(stream), np, (const float *)x,
+               (const float *)w, (const float *)lw, xx, ff, dxm1, nloc, lff);
   CCL_LAUNCH_CHECK("dens_profile_adjoint");
   return CCL_OK;
 }

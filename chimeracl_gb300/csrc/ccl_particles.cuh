@@ -572,26 +572,31 @@ static __global__ void __launch_bounds__(ST_THREADS)
                                                                  : (u32)np - cell_offset[C])
                                    : ovf_before + ovf_off[blockIdx.x];
   const bool tile_has_ovf = ovf_next != ovf_before;
-  u32 kk[ST_ITEMS];
-#pragma unroll
-  for (int it = 0; it < ST_ITEMS; it++) {
-    const long i = base + it * ST_THREADS + threadIdx.x;
-    kk[it] = i < np ? keys[i] : 0xffffffffu;
-  }
   if (tile_has_ovf) {
-    // overflow: block-ordered rank within each round of ST_THREADS items
+    // overflow: block-ordered rank within each round of ST_THREADS
+    // consecutive items
 #pragma unroll
     for (int it = 0; it < ST_ITEMS; it++) {
       const long i = base + it * ST_THREADS + threadIdx.x;
-      const bool ovf = kk[it] == C;  // invalid items hold 0xffffffff != C
+      const bool ovf = i < np && keys[i] == C;
       u32 rtot;
       const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
       if (ovf) sort_indx[tile_run + r] = (u32)i;
       tile_run += rtot;
     }
   }
-  // in-window: one cursor atomic per distinct cell per warp and round, all
-  // of the thread's atomics issued before any result is used
+  // in-window: each warp takes ST_ITEMS rounds of 32 consecutive items of
+  // its own 32 * ST_ITEMS (a cell split between rounds is claimed by the
+  // same warp, in order); one cursor atomic per distinct cell per warp and
+  // round (lanes keep index order), all of the thread's atomics issued
+  // before any result is used
+  const long wbase = base + (long)(threadIdx.x >> 5) * (32 * ST_ITEMS) + lane;
+  u32 kk[ST_ITEMS];
+#pragma unroll
+  for (int it = 0; it < ST_ITEMS; it++) {
+    const long i = wbase + it * 32;
+    kk[it] = i < np ? keys[i] : 0xffffffffu;
+  }
   unsigned peers[ST_ITEMS];
   u32 b0[ST_ITEMS];
 #pragma unroll
@@ -604,7 +609,7 @@ static __global__ void __launch_bounds__(ST_THREADS)
   }
 #pragma unroll
   for (int it = 0; it < ST_ITEMS; it++) {
-    const long i = base + it * ST_THREADS + threadIdx.x;
+    const long i = wbase + it * 32;
     const u32 k = kk[it];
     const bool win = k < C;
     const int leader = __ffs(peers[it]) - 1;
@@ -640,6 +645,11 @@ __device__ __forceinline__ void reg_sort(u32 *__restrict__ g, u32 n) {
   u32 v[N];
 #pragma unroll
   for (int i = 0; i < N; i++) v[i] = (u32)i < n ? g[i] : 0xffffffffu;
+  // a segment whose claims landed in order is left as it is
+  bool sorted = true;
+#pragma unroll
+  for (int i = 1; i < N; i++) sorted = sorted && ((u32)i >= n || v[i - 1] < v[i]);
+  if (sorted) return;
 #pragma unroll
   for (int p = 1; p < N; p <<= 1)
 #pragma unroll

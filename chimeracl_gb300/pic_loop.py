@@ -21,11 +21,33 @@ pieces; the solver's buffers alone for the field piece.  A window shift
 the particle pieces eagerly and captures them again -- the field solve,
 ~65 of the step's library calls, is replayed through the shift (its phase
 factors are refreshed in place first)."""
+import collections
+import contextlib
+import gc
+
 import numpy as np
 import torch
 
+# captures kept per piece (the signatures of the last few window positions)
+GRAPH_CACHE = 4
+
 loop_steps = ["frame", "push-x", "sort", "depose", "transform", "smooth", "data_copy",
               "grad", "push-eb", "damp-eb", "restore_B", "gather + push-p"]
+
+
+@contextlib.contextmanager
+def capture_guard():
+    """Around a CUDA graph capture: no cyclic garbage collection inside it.
+    A collection there could free an unreachable graph of an earlier run,
+    and freeing a graph (its memory pool) is not allowed while a capture is
+    open -- the capture would be invalidated."""
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 
 def timer_plot(Timer):
@@ -55,8 +77,12 @@ class PIC_loop:
         self.Timer = {k: 0.0 for k in loop_steps}
         self._events = []
         self.graphs = graphs
-        # piece name -> [graph, signature, library kernels in it]
+        # piece name -> [graph, signature, library kernels in it] (the one in
+        # use), and per piece the last GRAPH_CACHE captures by signature: a
+        # run restored to an earlier step (a recompute from a checkpoint)
+        # finds the graphs of that stretch of the window again
         self._graphs = {}
+        self._graph_cache = {}
         self.graph_replays = 0  # steps served by graph replays
         self.graph_captures = 0  # pieces captured
         self._cap_stream = None
@@ -114,6 +140,7 @@ class PIC_loop:
         use_graph = self.graphs and not self.timit and not self.diags and self.it > 0
         if not use_graph:
             self._graphs = {}
+            self._graph_cache = {}
             self._body(graph_mode=False)
         elif self._frame_due():
             # a window shift: host-driven injection, new particle counts and
@@ -127,8 +154,10 @@ class PIC_loop:
             self._particles_before(graph_mode=True)
             self._run_piece("f")
             self._particles_after(graph_mode=True)
+            full = self._signature("pa")
             for piece in ("pa", "pb"):
-                self._capture(piece)
+                if not self._from_cache(piece, full):
+                    self._capture(piece)
             self.graph_replays += 1
         else:
             full = self._signature("pa")  # the same for both particle pieces
@@ -140,11 +169,24 @@ class PIC_loop:
 
     def _run_piece(self, piece, sig=None):
         g = self._graphs.get(piece)
-        if g is None or (sig or self._signature(piece))[0] != g[1][0]:
-            self._capture(piece)
+        sig = sig or self._signature(piece)
+        if g is None or sig[0] != g[1][0]:
+            if not self._from_cache(piece, sig):
+                self._capture(piece)
             g = self._graphs[piece]
         g[0].replay()
         self.graph_kernels_replayed += g[2]
+
+    def _from_cache(self, piece, sig):
+        """Make a cached capture of `piece` with this signature the one in
+        use; False when there is none."""
+        cache = self._graph_cache.get(piece)
+        g = cache.get(sig[0]) if cache else None
+        if g is None:
+            return False
+        cache.move_to_end(sig[0])
+        self._graphs[piece] = g
+        return True
 
     def _capture(self, piece):
         """Capture one piece of the step into a CUDA graph, on a persistent
@@ -165,7 +207,7 @@ class PIC_loop:
             self._cap_stream = torch.cuda.Stream()
         cur = torch.cuda.current_stream()
         self._cap_stream.wait_stream(cur)
-        with torch.cuda.stream(self._cap_stream):
+        with torch.cuda.stream(self._cap_stream), capture_guard():
             g.capture_begin()
             try:
                 self._piece_fn(piece)(graph_mode=True)
@@ -173,7 +215,11 @@ class PIC_loop:
                 g.capture_end()
         cur.wait_stream(self._cap_stream)
         nk = _lib.launch_count() - n0
-        self._graphs[piece] = [g, self._signature(piece), nk]
+        entry = self._graphs[piece] = [g, self._signature(piece), nk]
+        cache = self._graph_cache.setdefault(piece, collections.OrderedDict())
+        cache[entry[1][0]] = entry
+        while len(cache) > GRAPH_CACHE:
+            cache.popitem(last=False)
         self.graph_captures += 1
         self.graph_kernels_captured += nk
 
