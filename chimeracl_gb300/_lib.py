@@ -70,6 +70,8 @@ SIGNATURES = {
     "ccl_dht_bf16x3_gemm_batch": [_i, _i, _i, _vp, _i, _pp, _pp, _vp, _pp, _vp, _d, _d, _d, _vp],
     "ccl_dht_bf16x3_status": [_i],
     "ccl_wait_probe": [_l, _i, _vp, _vp],
+    "ccl_sort_status": [_i],
+    "ccl_scan_wait_probe": [_l, _i, _vp, _vp, _vp],
     "ccl_get_m1": [_i, _i, _i, _vp, _vp, _vp],
     "ccl_grad_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _vp],
     "ccl_rot_combine": [_i, _i, _i, _i, _vp, _pp, _pp, _pp, _pp, _pp, _vp],

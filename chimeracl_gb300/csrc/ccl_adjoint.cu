@@ -570,16 +570,24 @@ __device__ __forceinline__ cplx<T> mirror_at(const T *p, long ir, long ix, int n
 // term), Pm[m] = -ldN_y + i ldN_z (mirrored for m = 0) and
 // Pp[m] = ldN_y + i ldN_z, for the radial products' transposes.
 template <typename T>
-__global__ void k_grad_adj_pre(long n, int nx, int M, const T *__restrict__ kx, ptrs<12> ldN,
-                               ptrs<4> lrho, ptrs<4> Pm, ptrs<4> Pp) {
+__global__ void __launch_bounds__(RC_THREADS)
+    k_grad_adj_pre(int nx, int M, const T *__restrict__ kx, ptrs<12> ldN, ptrs<4> lrho,
+                   ptrs<4> Pm, ptrs<4> Pp) {
   pdl_wait();
   const int m = blockIdx.y;
-  CCL_GS(i, n) {
-    const long ir = i / nx, ix = i - ir * nx;
+  const RowChunk<T> rc(nx);
+  const T *lx = (const T *)pick(ldN, 3 * m), *ly = (const T *)pick(ldN, 3 * m + 1),
+          *lz = (const T *)pick(ldN, 3 * m + 2);
+  T *lr = (T *)pick(lrho, m), *pmp = (T *)pick(Pm, m), *ppp = (T *)pick(Pp, m);
+#pragma unroll
+  for (int q = 0; q < RcPer<T>; q++) {
+    const long ir = rc.ir, ix = rc.col(q);
+    if (ix >= nx) continue;
+    const long i = ir * nx + ix;
     const T k = kx[ix];
-    const cplx<T> ax = ld_c((const T *)ldN.p[3 * m], i);
-    st_c((T *)lrho.p[m], i, cplx<T>{k * ax.im, -k * ax.re});
-    if (Pm.p[m]) {
+    const cplx<T> ax = ld_c(lx, i);
+    st_c(lr, i, cplx<T>{k * ax.im, -k * ax.re});
+    if (pmp) {
       // -ly + i lz, at the mirrored column for m = 0
       cplx<T> ay, az;
       if (m == 0) {
@@ -587,17 +595,17 @@ __global__ void k_grad_adj_pre(long n, int nx, int M, const T *__restrict__ kx, 
         ay = ld_c((const T *)ldN.p[1], ir * nx + io);
         az = ld_c((const T *)ldN.p[2], ir * nx + io);
         const cplx<T> v = {-ay.re - az.im, -ay.im + az.re};
-        st_c((T *)Pm.p[m], i, cplx<T>{-v.re, v.im});
+        st_c(pmp, i, cplx<T>{-v.re, v.im});
       } else {
-        ay = ld_c((const T *)ldN.p[3 * m + 1], i);
-        az = ld_c((const T *)ldN.p[3 * m + 2], i);
-        st_c((T *)Pm.p[m], i, cplx<T>{-ay.re - az.im, -ay.im + az.re});
+        ay = ld_c(ly, i);
+        az = ld_c(lz, i);
+        st_c(pmp, i, cplx<T>{-ay.re - az.im, -ay.im + az.re});
       }
     }
-    if (Pp.p[m]) {
-      const cplx<T> ay = ld_c((const T *)ldN.p[3 * m + 1], i);
-      const cplx<T> az = ld_c((const T *)ldN.p[3 * m + 2], i);
-      st_c((T *)Pp.p[m], i, cplx<T>{ay.re - az.im, ay.im + az.re});
+    if (ppp) {
+      const cplx<T> ay = ld_c(ly, i);
+      const cplx<T> az = ld_c(lz, i);
+      st_c(ppp, i, cplx<T>{ay.re - az.im, ay.im + az.re});
     }
   }
 }
@@ -611,12 +619,13 @@ __global__ void k_modes_adj_post(long n, int M, int ncomp, ptrs<12> lo, ptrs<12>
                                  ptrs<12> Rp, ptrs<4> filt) {
   pdl_wait();
   const int j = blockIdx.y / ncomp, c = blockIdx.y - j * ncomp;
-  const T *fl = (const T *)filt.p[j];
+  const T *fl = (const T *)pick(filt, j);
+  T *lop = (T *)pick(lo, j * ncomp + c);
+  const T *srcs[3] = {j + 1 <= M ? (const T *)pick(Rm, (j + 1) * ncomp + c) : nullptr,
+                      j >= 1 ? (const T *)pick(Rp, (j - 1) * ncomp + c) : nullptr,
+                      j == 1 ? (const T *)pick(Rm, c) : nullptr};
   CCL_GS(i, n) {
-    cplx<T> v = ld_c((const T *)lo.p[j * ncomp + c], i);
-    const T *srcs[3] = {j + 1 <= M ? (const T *)Rm.p[(j + 1) * ncomp + c] : nullptr,
-                        j >= 1 ? (const T *)Rp.p[(j - 1) * ncomp + c] : nullptr,
-                        j == 1 ? (const T *)Rm.p[c] : nullptr};
+    cplx<T> v = ld_c(lop, i);
 #pragma unroll
     for (int q = 0; q < 3; q++)
       if (srcs[q]) {
@@ -628,7 +637,7 @@ __global__ void k_modes_adj_post(long n, int M, int ncomp, ptrs<12> lo, ptrs<12>
       v.re *= fl[i];
       v.im *= fl[i];
     }
-    st_c((T *)lo.p[j * ncomp + c], i, v);
+    st_c(lop, i, v);
   }
 }
 
@@ -638,31 +647,46 @@ __global__ void k_modes_adj_post(long n, int M, int ncomp, ptrs<12> lo, ptrs<12>
 //   Qm_x = i lBy + lBz, Qm_y = -i lBx, Qm_z = -lBx  (mirrored for m = 0),
 //   Qp_x = i lBy - lBz, Qp_y = -i lBx, Qp_z = lBx.
 template <typename T>
-__global__ void k_rot_adj_pre(long n, int nx, int M, const T *__restrict__ kx, ptrs<4> poiss,
-                              ptrs<12> lB, ptrs<12> lG, ptrs<12> Qm, ptrs<12> Qp) {
+__global__ void __launch_bounds__(RC_THREADS)
+    k_rot_adj_pre(int nx, int M, const T *__restrict__ kx, ptrs<4> poiss, ptrs<12> lB,
+                  ptrs<12> lG, ptrs<12> Qm, ptrs<12> Qp) {
   pdl_wait();
   const int m = blockIdx.y;
-  CCL_GS(i, n) {
-    const long ir = i / nx, ix = i - ir * nx;
+  const RowChunk<T> rc(nx);
+  const T *pf = (const T *)pick(poiss, m);
+  const T *lbp[3];
+  T *qmp[3], *qpp[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    lbp[c] = (const T *)pick(lB, 3 * m + c);
+    qmp[c] = (T *)pick(Qm, 3 * m + c);
+    qpp[c] = (T *)pick(Qp, 3 * m + c);
+  }
+  T *lgy = (T *)pick(lG, 3 * m + 1), *lgz = (T *)pick(lG, 3 * m + 2);
+#pragma unroll
+  for (int q = 0; q < RcPer<T>; q++) {
+    const long ir = rc.ir, ix = rc.col(q);
+    if (ix >= nx) continue;
+    const long i = ir * nx + ix;
     const T k = kx[ix];
     auto lb = [&](int c, long at) {
-      cplx<T> v = ld_c((const T *)lB.p[3 * m + c], at);
-      if (poiss.p[m]) {
-        const T f = ((const T *)poiss.p[m])[at];
+      cplx<T> v = ld_c(lbp[c], at);
+      if (pf) {
+        const T f = pf[at];
         v.re *= f;
         v.im *= f;
       }
       return v;
     };
     const cplx<T> bx = lb(0, i), by = lb(1, i), bz = lb(2, i);
-    cplx<T> gy = ld_c((const T *)lG.p[3 * m + 1], i), gz = ld_c((const T *)lG.p[3 * m + 2], i);
+    cplx<T> gy = ld_c(lgy, i), gz = ld_c(lgz, i);
     gy.re += k * bz.im;   // -i k bz
     gy.im -= k * bz.re;
     gz.re -= k * by.im;   // +i k by
     gz.im += k * by.re;
-    st_c((T *)lG.p[3 * m + 1], i, gy);
-    st_c((T *)lG.p[3 * m + 2], i, gz);
-    if (Qm.p[3 * m]) {
+    st_c(lgy, i, gy);
+    st_c(lgz, i, gz);
+    if (qmp[0]) {
       cplx<T> ax = bx, ay = by, az = bz;
       if (m == 0) {
         const long io = ix == 0 ? 0 : nx - ix;
@@ -678,14 +702,14 @@ __global__ void k_rot_adj_pre(long n, int nx, int M, const T *__restrict__ kx, p
         qy.re = -qy.re;
         qz.re = -qz.re;
       }
-      st_c((T *)Qm.p[3 * m], i, qx);
-      st_c((T *)Qm.p[3 * m + 1], i, qy);
-      st_c((T *)Qm.p[3 * m + 2], i, qz);
+      st_c(qmp[0], i, qx);
+      st_c(qmp[1], i, qy);
+      st_c(qmp[2], i, qz);
     }
-    if (Qp.p[3 * m]) {
-      st_c((T *)Qp.p[3 * m], i, cplx<T>{-by.im - bz.re, by.re - bz.im});
-      st_c((T *)Qp.p[3 * m + 1], i, cplx<T>{bx.im, -bx.re});
-      st_c((T *)Qp.p[3 * m + 2], i, cplx<T>{bx.re, bx.im});
+    if (qpp[0]) {
+      st_c(qpp[0], i, cplx<T>{-by.im - bz.re, by.re - bz.im});
+      st_c(qpp[1], i, cplx<T>{bx.im, -bx.re});
+      st_c(qpp[2], i, cplx<T>{bx.re, bx.im});
     }
   }
 }
@@ -766,7 +790,9 @@ __global__ void k_scatter(long n, int ncomp, ptrs<16> src, ptrs<16> dst,
   pdl_wait();
   CCL_GS(i, n) {
     const u32 j = idx[i];
-    for (int c = 0; c < ncomp; c++) ((T *)dst.p[c])[j] = ((const T *)src.p[c])[i];
+#pragma unroll
+    for (int c = 0; c < 16; c++)
+      if (c < ncomp) ((T *)dst.p[c])[j] = ((const T *)src.p[c])[i];
   }
 }
 
@@ -1033,15 +1059,13 @@ int ccl_grad_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx
     pm.p[m] = Pm ? Pm[m] : nullptr;
     pp.p[m] = Pp ? Pp[m] : nullptr;
   }
-  const long n = (long)nrows * nx;
-  if (n == 0) return CCL_OK;
-  dim3 grid(grid_for(n, 256, 4), M + 1);
+  if ((long)nrows * nx == 0) return CCL_OK;
   if (dtype == CCL_F64)
-    launch_pdl(k_grad_adj_pre<double>, grid, 256, 0, S(stream), n, nx, M, (const double *)kx, a, r,
-               pm, pp);
+    launch_pdl(k_grad_adj_pre<double>, row_chunk_grid<double>(nrows, nx, M + 1), RC_THREADS, 0,
+               S(stream), nx, M, (const double *)kx, a, r, pm, pp);
   else
-    launch_pdl(k_grad_adj_pre<float>, grid, 256, 0, S(stream), n, nx, M, (const float *)kx, a, r,
-               pm, pp);
+    launch_pdl(k_grad_adj_pre<float>, row_chunk_grid<float>(nrows, nx, M + 1), RC_THREADS, 0,
+               S(stream), nx, M, (const float *)kx, a, r, pm, pp);
   CCL_LAUNCH_CHECK("grad_combine_adjoint");
   return CCL_OK;
 }
@@ -1071,15 +1095,13 @@ int ccl_rot_combine_adjoint(int dtype, int M, int nrows, int nx, const void *kx,
                     (!qp.p[3 * m] && !qp.p[3 * m + 1] && !qp.p[3 * m + 2]),
                 CCL_ERR_ARG, "%s: Qp of mode %d partly NULL", __func__, m);
   }
-  const long n = (long)nrows * nx;
-  if (n == 0) return CCL_OK;
-  dim3 grid(grid_for(n, 256, 4), M + 1);
+  if ((long)nrows * nx == 0) return CCL_OK;
   if (dtype == CCL_F64)
-    launch_pdl(k_rot_adj_pre<double>, grid, 256, 0, S(stream), n, nx, M, (const double *)kx, po, b,
-               g, qm, qp);
+    launch_pdl(k_rot_adj_pre<double>, row_chunk_grid<double>(nrows, nx, M + 1), RC_THREADS, 0,
+               S(stream), nx, M, (const double *)kx, po, b, g, qm, qp);
   else
-    launch_pdl(k_rot_adj_pre<float>, grid, 256, 0, S(stream), n, nx, M, (const float *)kx, po, b, g,
-               qm, qp);
+    launch_pdl(k_rot_adj_pre<float>, row_chunk_grid<float>(nrows, nx, M + 1), RC_THREADS, 0,
+               S(stream), nx, M, (const float *)kx, po, b, g, qm, qp);
   CCL_LAUNCH_CHECK("rot_combine_adjoint");
   return CCL_OK;
 }

@@ -522,6 +522,13 @@ int ccl_wait_probe(long spins, int arrive, int *gave_up, void *stream) {
   return umma_wait_probe(spins, arrive, gave_up, S(stream));
 }
 
+int ccl_sort_status(int reset) { return sort_status(reset); }
+
+int ccl_scan_wait_probe(long spins, int publish, int *gave_up, uint32_t *scratch, void *stream) {
+  NONNULL(gave_up); NONNULL(scratch);
+  return scan_wait_probe(spins, publish, gave_up, scratch, S(stream));
+}
+
 int ccl_psatd_advance(int dtype, long ncells, double dt_inv, const void *c1,
                       const void *c2, const void *c3, void *const *flds,
                       void *stream) {

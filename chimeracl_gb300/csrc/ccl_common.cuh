@@ -81,6 +81,28 @@ static inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 blo
   return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
+// Row-chunked indexing of (nrows x nx) spectral arrays (the spectral
+// combines and their transposes): block blockIdx.x takes row
+// blockIdx.x / nch and RcCols<T> consecutive columns of it, each thread
+// RcPer<T> of them RC_THREADS apart, with no division per element.  (The
+// combines load all of a thread's columns before their first store: the
+// field bundles may alias, so the compiler would not move the loads.)
+constexpr int RC_THREADS = 256;
+template <typename T> constexpr int RcPer = sizeof(T) == 4 ? 4 : 2;
+template <typename T> constexpr int RcCols = RC_THREADS * RcPer<T>;
+template <typename T> inline dim3 row_chunk_grid(int nrows, int nx, int nz) {
+  return dim3((unsigned)nrows * (unsigned)((nx + RcCols<T> - 1) / RcCols<T>), (unsigned)nz);
+}
+template <typename T> struct RowChunk {
+  int ir, c0;
+  __device__ __forceinline__ RowChunk(int nx) {
+    const int nch = (nx + RcCols<T> - 1) / RcCols<T>;
+    ir = blockIdx.x / nch;
+    c0 = (blockIdx.x - ir * nch) * RcCols<T> + threadIdx.x;
+  }
+  __device__ __forceinline__ int col(int q) const { return c0 + q * RC_THREADS; }
+};
+
 // Complex number of real type T, laid out as (re, im).
 template <typename T> struct cplx {
   T re, im;
@@ -108,5 +130,16 @@ template <typename T> __device__ __forceinline__ void st_c(T *p, long i, cplx<T>
 template <int N> struct ptrs {
   void *p[N];
 };
+
+// Element i of a bundle for an index known only at run time (a block
+// coordinate, a count): a chain of selects over constant indices, so the
+// bundle stays in parameter space.  Indexing it directly makes the compiler
+// copy the whole bundle into every thread's local memory first.
+template <int N> __device__ __forceinline__ void *pick(const ptrs<N> &a, int i) {
+  void *r = a.p[0];
+#pragma unroll
+  for (int j = 1; j < N; j++) r = i == j ? a.p[j] : r;
+  return r;
+}
 
 }  // namespace ccl

@@ -12,13 +12,6 @@ size_t index_sort_ws_bytes(long np, long ncells) {
   return sort_ws_bytes(np, ncells);
 }
 
-int index_sort_keyed_launch(long np, long ncells, const uint32_t *indx, uint32_t *counts,
-                            uint32_t *cell_offset, uint32_t *sort_indx, uint32_t *np_stay,
-                            void *ws, size_t ws_bytes, cudaStream_t s) {
-  return index_sort_keyed(np, ncells, indx, counts, cell_offset, sort_indx, np_stay, ws,
-                          ws_bytes, s);
-}
-
 int iota_u32(uint32_t *a, long n, cudaStream_t s) {
   if (n == 0) return CCL_OK;
   k_iota<<<grid_for(n, 256), 256, 0, s>>>(a, n);

@@ -150,5 +150,7 @@ int index_sort_keyed_launch(long np, long ncells, const uint32_t *indx, uint32_t
                             uint32_t *cell_offset, uint32_t *sort_indx, uint32_t *np_stay,
                             void *ws, size_t ws_bytes, cudaStream_t s);
 int iota_u32(uint32_t *a, long n, cudaStream_t s);
+int sort_status(int reset);
+int scan_wait_probe(long spins, int publish, int *gave_up, uint32_t *scratch, cudaStream_t s);
 
 }  // namespace ccl

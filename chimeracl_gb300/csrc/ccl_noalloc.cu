@@ -20,7 +20,7 @@
 
 namespace {
 
-constexpr size_t kSortScratchBytes = (size_t)8 << 20;  // 8 MiB
+constexpr size_t kSortScratchBytes = (size_t)9 << 20;  // 9 MiB
 constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_sort_scratch[kSortScratchBytes];

@@ -349,10 +349,9 @@ int Ops<T>::grad_combine(int M, int nrows, int nx, const void *kx, const void *c
       d.p[3 * m + c] = dN[3 * m + c];
     }
   }
-  long n = (long)nrows * nx;
-  if (n == 0) return CCL_OK;
-  dim3 grid(grid_for(n, 256, 4), M + 1);
-  launch_pdl(k_grad_combine<T>, grid, 256, 0, s, n, nx, (const T *)kx, r, pm, pp, d);
+  if ((long)nrows * nx == 0) return CCL_OK;
+  launch_pdl(k_grad_combine<T>, row_chunk_grid<T>(nrows, nx, M + 1), RC_THREADS, 0, s, nx,
+             (const T *)kx, r, pm, pp, d);
   CCL_LAUNCH_CHECK("grad_combine");
   return CCL_OK;
 }
@@ -375,10 +374,9 @@ int Ops<T>::rot_combine(int M, int nrows, int nx, const void *kx, const void *co
       qp.p[j] = Qp ? (void *)Qp[j] : nullptr;
     }
   }
-  long n = (long)nrows * nx;
-  if (n == 0) return CCL_OK;
-  dim3 grid(grid_for(n, 256, 4), M + 1);
-  launch_pdl(k_rot_combine<T>, grid, 256, 0, s, n, nx, (const T *)kx, g, qm, qp, po, b);
+  if ((long)nrows * nx == 0) return CCL_OK;
+  launch_pdl(k_rot_combine<T>, row_chunk_grid<T>(nrows, nx, M + 1), RC_THREADS, 0, s, nx,
+             (const T *)kx, g, qm, qp, po, b);
   CCL_LAUNCH_CHECK("rot_combine");
   return CCL_OK;
 }

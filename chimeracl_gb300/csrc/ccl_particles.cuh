@@ -306,65 +306,14 @@ __device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32 *sh,
   return wpre + inc - v;
 }
 
-static __global__ void k_scan_reduce(const u32 *__restrict__ in, long L,
-                              u32 *__restrict__ part) {
-  pdl_wait();
-  __shared__ u32 sh[32];
-  long base = (long)blockIdx.x * SCAN_TILE;
-  u32 s = 0;
-#pragma unroll
-  for (int it = 0; it < SCAN_ITEMS; it++) {
-    long i = base + it * SCAN_THREADS + threadIdx.x;
-    if (i < L) s += in[i];
-  }
-  u32 tot;
-  block_exclusive_scan(s, sh, &tot);
-  if (threadIdx.x == 0) part[blockIdx.x] = tot;
-}
-
-// exclusive scan of one tile per block, offset by the tile's prefix: with
-// sum_parts the block adds up the raw tile sums part[0 .. blockIdx) itself
-// (few tiles), else part holds them scanned.  Optionally copies out[tap_i]
-// to *tap (the in-window count of the cell sort).
-static __global__ void k_scan_tile(const u32 *__restrict__ in, long L,
-                            const u32 *__restrict__ part, int sum_parts,
-                            u32 *__restrict__ out, u32 *__restrict__ total_out,
-                            u32 *__restrict__ tap, long tap_i) {
-  pdl_wait();
-  __shared__ u32 sh[32];
-  __shared__ u32 tile_pre;
-  if (threadIdx.x == 0) tile_pre = 0;
-  if (part && sum_parts) {
-    u32 ps = 0;
-    for (long t = threadIdx.x; t < blockIdx.x; t += blockDim.x) ps += part[t];
-    u32 ptot;
-    __syncthreads();
-    block_exclusive_scan(ps, sh, &ptot);
-    if (threadIdx.x == 0) tile_pre = ptot;
-  } else if (part && threadIdx.x == 0) {
-    tile_pre = part[blockIdx.x];
-  }
-  __syncthreads();
-  long base = (long)blockIdx.x * SCAN_TILE + (long)threadIdx.x * SCAN_ITEMS;
-  u32 v[SCAN_ITEMS];
-  u32 s = 0;
-#pragma unroll
-  for (int it = 0; it < SCAN_ITEMS; it++) {
-    long i = base + it;
-    v[it] = i < L ? in[i] : 0;
-    s += v[it];
-  }
-  u32 tot;
-  const u32 tp = tile_pre;
-  u32 pre = block_exclusive_scan(s, sh, &tot) + tp;
-#pragma unroll
-  for (int it = 0; it < SCAN_ITEMS; it++) {
-    long i = base + it;
-    if (i < L) out[i] = pre;
-    if (tap && i == tap_i) *tap = pre;
-    pre += v[it];
-  }
-  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = tp + tot;
+// The sort's first pass also zeroes the workspace region that the rest of
+// the sort expects at zero (scatter cursors, multi-claim bits, the scan's
+// tile status words and ticket), spread over its blocks: the previous sort
+// on the workspace has finished when a dependent launch passes pdl_wait.
+__device__ __forceinline__ void clear_sort_region(uint4 *__restrict__ clr, long n4) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride)
+    clr[q] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // Keys + per-cell counts over tiles of ST_TILE consecutive particles; cell
@@ -377,8 +326,10 @@ template <typename T>
 __global__ void __launch_bounds__(ST_THREADS)
     k_keys(long np, const T *__restrict__ x, const T *__restrict__ y,
            const T *__restrict__ z, GridP<T> g, u32 *__restrict__ keys,
-           u32 *__restrict__ counts, u32 *__restrict__ tile_ovf) {
+           u32 *__restrict__ counts, u32 *__restrict__ tile_ovf, uint4 *__restrict__ clr,
+           long nclr4) {
   pdl_wait();
+  clear_sort_region(clr, nclr4);
   __shared__ u32 sh[32];
   const int lane = threadIdx.x & 31;
   const u32 C = (u32)(g.Nx - 1) * (u32)(g.Nr - 1);
@@ -418,8 +369,9 @@ __global__ void __launch_bounds__(ST_THREADS)
                 const T *__restrict__ px, const T *__restrict__ py, const T *__restrict__ pz,
                 const T *__restrict__ g_inv, T dt, int vec, GridP<T> g,
                 u32 *__restrict__ keys, u32 *__restrict__ counts,
-                u32 *__restrict__ tile_ovf) {
+                u32 *__restrict__ tile_ovf, uint4 *__restrict__ clr, long nclr4) {
   pdl_wait();
+  clear_sort_region(clr, nclr4);
   constexpr int VW = 16 / sizeof(T);
   constexpr int NVT = ST_TILE / VW / ST_THREADS;  // vectors per thread
   using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
@@ -508,241 +460,30 @@ static inline long scan_ws_words(long L) {
   return w + 1;
 }
 
-// out[0..L-1] = exclusive scan of in; *total_out = sum (if non-null);
-// *tap = out[tap_i] (if tap).  Works in place (out == in).  ws:
-// scan_ws_words(L) words.  Up to SCAN_FUSE tiles: two launches (tile sums,
-// then the tile scans, each adding up its own prefix).
-constexpr long SCAN_FUSE = 4096;
-static int scan_exclusive(const u32 *in, long L, u32 *out, u32 *total_out,
-                          u32 *ws, cudaStream_t s, u32 *tap = nullptr, long tap_i = -1) {
-  if (L <= 0) return CCL_OK;
-  long nb = (L + SCAN_TILE - 1) / SCAN_TILE;
-  if (nb == 1) {
-    launch_pdl(k_scan_tile, 1, SCAN_THREADS, 0, s, in, L, nullptr, 0, out, total_out, tap, tap_i);
-    CCL_LAUNCH_CHECK("scan_tile");
-    return CCL_OK;
-  }
-  u32 *part = ws;
-  launch_pdl(k_scan_reduce, (unsigned)nb, SCAN_THREADS, 0, s, in, L, part);
-  CCL_LAUNCH_CHECK("scan_reduce");
-  int fused = nb <= SCAN_FUSE;
-  if (!fused) {
-    int rc = scan_exclusive(part, nb, part, nullptr, ws + nb, s);
-    if (rc) return rc;
-  }
-  launch_pdl(k_scan_tile, (unsigned)nb, SCAN_THREADS, 0, s, in, L, part, fused, out, total_out, tap,
-             tap_i);
-  CCL_LAUNCH_CHECK("scan_tile");
-  return CCL_OK;
-}
-
-// ---------------------------------------------------------------------
-// Counting-sort scatter.  In-window particles take their slot in their
-// cell's segment through a per-cell cursor (one atomic per distinct cell per
-// warp; lanes of a warp keep index order); out-of-window particles take
-// cell_offset[C] + (overflow particles in earlier tiles) + (rank in this
-// tile), so that segment is in index order.  A cell claimed more than once
-// is flagged, and k_cell_fixup sorts just those cells' segments by particle
-// number, which makes the result that of a stable sort: within a cell,
-// ascending particle number -- the order of the reference's sort kernel run
-// serially.
-static __global__ void __launch_bounds__(ST_THREADS)
-    k_scatter(long np, const u32 *__restrict__ keys, u32 C,
-              const u32 *__restrict__ cell_offset, u32 *__restrict__ cursor,
-              u32 *__restrict__ multi, const u32 *__restrict__ ovf_off, int ovf_scanned,
-              u32 *__restrict__ sort_indx) {
-  pdl_wait();
-  __shared__ u32 sh[32];
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  const long base = (long)blockIdx.x * ST_TILE;
-  // overflow items before this tile: the block adds up the per-tile counts
-  // itself (ovf_scanned == 0) or reads their exclusive scan
-  u32 ovf_before;
-  if (!ovf_scanned) {
-    u32 ps = 0;
-    for (long t = threadIdx.x; t < blockIdx.x; t += blockDim.x) ps += ovf_off[t];
-    block_exclusive_scan(ps, sh, &ovf_before);
-  } else {
-    ovf_before = ovf_off[blockIdx.x];
-  }
-  u32 tile_run = ovf_before + cell_offset[C];
-  // overflow items of this tile (block-uniform)
-  const u32 ovf_next = ovf_scanned ? (blockIdx.x + 1 < gridDim.x ? ovf_off[blockIdx.x + 1]
-                                                                 : (u32)np - cell_offset[C])
-                                   : ovf_before + ovf_off[blockIdx.x];
-  const bool tile_has_ovf = ovf_next != ovf_before;
-  if (tile_has_ovf) {
-    // overflow: block-ordered rank within each round of ST_THREADS
-    // consecutive items
-#pragma unroll
-    for (int it = 0; it < ST_ITEMS; it++) {
-      const long i = base + it * ST_THREADS + threadIdx.x;
-      const bool ovf = i < np && keys[i] == C;
-      u32 rtot;
-      const u32 r = block_exclusive_scan(ovf ? 1u : 0u, sh, &rtot);
-      if (ovf) sort_indx[tile_run + r] = (u32)i;
-      tile_run += rtot;
-    }
-  }
-  // in-window: each warp takes ST_ITEMS rounds of 32 consecutive items of
-  // its own 32 * ST_ITEMS (a cell split between rounds is claimed by the
-  // same warp, in order); one cursor atomic per distinct cell per warp and
-  // round (lanes keep index order), all of the thread's atomics issued
-  // before any result is used
-  const long wbase = base + (long)(threadIdx.x >> 5) * (32 * ST_ITEMS) + lane;
-  u32 kk[ST_ITEMS];
-#pragma unroll
-  for (int it = 0; it < ST_ITEMS; it++) {
-    const long i = wbase + it * 32;
-    kk[it] = i < np ? keys[i] : 0xffffffffu;
-  }
-  unsigned peers[ST_ITEMS];
-  u32 b0[ST_ITEMS];
-#pragma unroll
-  for (int it = 0; it < ST_ITEMS; it++) {
-    const u32 k = kk[it];
-    const bool win = k < C;
-    peers[it] = __match_any_sync(0xffffffffu, win ? k : 0xffffffffu);
-    b0[it] = 0;
-    if (win && lane == __ffs(peers[it]) - 1) b0[it] = atomicAdd(&cursor[k], __popc(peers[it]));
-  }
-#pragma unroll
-  for (int it = 0; it < ST_ITEMS; it++) {
-    const long i = wbase + it * 32;
-    const u32 k = kk[it];
-    const bool win = k < C;
-    const int leader = __ffs(peers[it]) - 1;
-    // a second claim on the cell: its order may need the fix-up
-    if (win && lane == leader && b0[it] != 0) atomicOr(&multi[k >> 5], 1u << (k & 31));
-    const u32 b = __shfl_sync(0xffffffffu, b0[it], leader);
-    if (win) sort_indx[cell_offset[k] + b + __popc(peers[it] & lt)] = (u32)i;
-  }
-}
-
-// Fix-up of the cells the scatter flagged (claimed by more than one warp
-// group; a single group writes its items in ascending order).  A warp takes
-// 32 consecutive cells, one per lane: segments of up to FX_REG items are
-// sorted by their lane in registers (Batcher's odd-even merge network over
-// 16 or 32 inputs);
-// longer ones -- a dense bunch of the plasma, or a whole layout of
-// particles on cell faces -- by the whole warp, one at a time, with a
-// bitonic sort in shared memory (up to FX_BUF items; a longer segment, not
-// met in practice, by insertion sort in place).  Every other cell is left
-// untouched without reading it.
-constexpr int FX_REG = 32, FX_WARPS = 4, FX_BUF = 2048;
-
-__device__ __forceinline__ void cswap(u32 &a, u32 &b) {
-  const u32 lo = a < b ? a : b, hi = a < b ? b : a;
-  a = lo;
-  b = hi;
-}
-
-// ascending sort of g[0 .. n), n <= N, by one thread in registers
-// (Batcher's odd-even merge network over N inputs)
-template <int N>
-__device__ __forceinline__ void reg_sort(u32 *__restrict__ g, u32 n) {
-  u32 v[N];
-#pragma unroll
-  for (int i = 0; i < N; i++) v[i] = (u32)i < n ? g[i] : 0xffffffffu;
-  // a segment whose claims landed in order is left as it is
-  bool sorted = true;
-#pragma unroll
-  for (int i = 1; i < N; i++) sorted = sorted && ((u32)i >= n || v[i - 1] < v[i]);
-  if (sorted) return;
-#pragma unroll
-  for (int p = 1; p < N; p <<= 1)
-#pragma unroll
-    for (int k = p; k >= 1; k >>= 1)
-#pragma unroll
-      for (int j = k % p; j <= N - 1 - k; j += 2 * k)
-#pragma unroll
-        for (int i = 0; i <= k - 1 && i + j + k <= N - 1; i++)
-          if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) cswap(v[i + j], v[i + j + k]);
-#pragma unroll
-  for (int i = 0; i < N; i++)
-    if ((u32)i < n) g[i] = v[i];
-}
-
-// ascending sort of g[0 .. n) (distinct values) by the 32 lanes of a warp
-// through buf (FX_BUF words of shared memory)
-__device__ __forceinline__ void warp_bitonic_sort(u32 *__restrict__ g, u32 n, u32 *buf,
-                                                  int lane) {
-  u32 P = 32;
-  while (P < n) P <<= 1;
-  for (u32 i = lane; i < P; i += 32) buf[i] = i < n ? g[i] : 0xffffffffu;
-  __syncwarp();
-  for (u32 k = 2; k <= P; k <<= 1)
-    for (u32 j = k >> 1; j > 0; j >>= 1) {
-      for (u32 i = lane; i < P; i += 32) {
-        const u32 l = i ^ j;
-        if (l > i) {
-          const u32 a = buf[i], b = buf[l];
-          if ((a > b) == ((i & k) == 0)) {
-            buf[i] = b;
-            buf[l] = a;
-          }
-        }
-      }
-      __syncwarp();
-    }
-  for (u32 i = lane; i < n; i += 32) g[i] = buf[i];
-  __syncwarp();
-}
-
-static __global__ void __launch_bounds__(FX_WARPS * 32)
-    k_cell_fixup(u32 C, const u32 *__restrict__ cell_offset, const u32 *__restrict__ multi,
-                 u32 *__restrict__ sort_indx) {
-  pdl_wait();
-  __shared__ u32 buf[FX_WARPS][FX_BUF];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long stride = (long)gridDim.x * FX_WARPS * 32;
-  for (long c0 = ((long)blockIdx.x * FX_WARPS + warp) * 32; c0 < (long)C; c0 += stride) {
-    const long c = c0 + lane;
-    const bool flagged = c < (long)C && (multi[c >> 5] & (1u << (c & 31)));
-    u32 p0 = 0, n = 0;
-    if (flagged) {
-      p0 = cell_offset[c];
-      n = cell_offset[c + 1] - p0;
-    }
-    if (flagged && n <= (u32)FX_REG / 2) reg_sort<FX_REG / 2>(sort_indx + p0, n);
-    else if (flagged && n <= (u32)FX_REG) reg_sort<FX_REG>(sort_indx + p0, n);
-    unsigned big = __ballot_sync(0xffffffffu, flagged && n > (u32)FX_REG);
-    while (big) {
-      const int l = __ffs(big) - 1;
-      big &= big - 1;
-      const u32 q0 = __shfl_sync(0xffffffffu, p0, l), qn = __shfl_sync(0xffffffffu, n, l);
-      if (qn <= (u32)FX_BUF) {
-        warp_bitonic_sort(sort_indx + q0, qn, buf[warp], lane);
-      } else {
-        if (lane == 0)
-          for (u32 a = q0 + 1; a < q0 + qn; a++) {
-            const u32 v = sort_indx[a];
-            u32 b = a;
-            while (b > q0 && sort_indx[b - 1] > v) {
-              sort_indx[b] = sort_indx[b - 1];
-              b--;
-            }
-            sort_indx[b] = v;
-          }
-        __syncwarp();
-      }
-    }
-  }
-}
-
-// workspace: scatter cursors (C + 1 words), multi-claim bits (one per cell),
-// per-tile overflow counts, scan partials
+// workspace: scatter cursors (C + 1 words), multi-claim bits (one per
+// cell), the single-pass scan's tile status words and ticket -- together
+// the region the key pass clears, a whole number of 16-byte words -- then
+// per-tile overflow counts and scan partials
 struct SortWs {
-  u32 *cursor, *multi, *tile_ovf, *scan;
+  u32 *cursor, *multi, *ticket, *tile_ovf, *scan;
+  unsigned long long *status;
+  long nclear4;  // 16-byte words cleared by the key pass, from cursor on
 };
 
 static inline long sort_multi_words(long ncells) { return (ncells + 31) / 32; }
 
+long scan_lookback_tiles(long L);
+
+static inline long sort_clear_words(long ncells) {
+  long w = (ncells + 1 + sort_multi_words(ncells) + 1) & ~1L;  // status: 8-byte aligned
+  w += 2 * scan_lookback_tiles(ncells + 1) + 2;                 // status words, ticket
+  return (w + 3) & ~3L;
+}
+
 static inline size_t sort_ws_bytes(long np, long ncells) {
   long ntiles = (np + ST_TILE - 1) / ST_TILE;
   long scanw = scan_ws_words(ncells + 1 > ntiles ? ncells + 1 : ntiles);
-  long words = ncells + 1 + sort_multi_words(ncells) + ntiles + 1 + scanw + 64;
+  long words = sort_clear_words(ncells) + ntiles + 1 + scanw + 64;
   return (size_t)words * 4 + 256;
 }
 
@@ -753,45 +494,19 @@ static inline SortWs carve_sort_ws(void *ws, long np, long ncells) {
   SortWs s;
   s.cursor = w;
   s.multi = w + ncells + 1;
-  s.tile_ovf = s.multi + sort_multi_words(ncells);
+  const long st = (ncells + 1 + sort_multi_words(ncells) + 1) & ~1L;
+  s.status = (unsigned long long *)(w + st);
+  s.ticket = w + st + 2 * scan_lookback_tiles(ncells + 1);
+  const long cw = sort_clear_words(ncells);
+  s.nclear4 = cw / 4;
+  s.tile_ovf = w + cw;
   s.scan = s.tile_ovf + ntiles + 1;
   return s;
 }
 
-// The sort after its first pass (keys in indx, counts in counts, the tiles'
-// overflow counts in the workspace): offsets, scatter, fix-up.
-inline int index_sort_keyed(long np, long C, const u32 *indx, u32 *counts, u32 *cell_offset,
-                            u32 *sort_indx, u32 *np_stay, void *ws, size_t ws_bytes,
-                            cudaStream_t s) {
-  CCL_REQUIRE(ws_bytes >= sort_ws_bytes(np, C), CCL_ERR_WORKSPACE,
-              "index_sort: workspace %zu < %zu bytes", ws_bytes, sort_ws_bytes(np, C));
-  SortWs w = carve_sort_ws(ws, np, C);
-  const long ntiles = (np + ST_TILE - 1) / ST_TILE;
-  // offsets, total, and np_stay = cell_offset[C] from the scan's own tap
-  int rc = scan_exclusive(counts, C + 1, cell_offset, cell_offset + C + 1, w.scan, s, np_stay,
-                          C);
-  if (rc) return rc;
-  if (np == 0) return CCL_OK;
-  // few tiles: each scatter block adds up the overflow counts before it
-  const int ovf_scanned = ntiles > SCAN_FUSE;
-  if (ovf_scanned) {
-    rc = scan_exclusive(w.tile_ovf, ntiles, w.tile_ovf, nullptr, w.scan, s);
-    if (rc) return rc;
-  }
-  // cursors and multi-claim bits are adjacent: one memset clears both
-  cudaError_t me = cudaMemsetAsync(
-      w.cursor, 0, (size_t)(w.multi + sort_multi_words(C) - w.cursor) * sizeof(u32), s);
-  CCL_REQUIRE(me == cudaSuccess, CCL_ERR_CUDA, "index_sort: clearing the cursors: %s",
-              cudaGetErrorString(me));
-  launch_pdl(k_scatter, (unsigned)ntiles, ST_THREADS, 0, s, np, indx, (u32)C, cell_offset, w.cursor,
-             w.multi, w.tile_ovf, ovf_scanned, sort_indx);
-  CCL_LAUNCH_CHECK("scatter");
-  if (C > 0)
-    launch_pdl(k_cell_fixup, grid_for(C, FX_WARPS * 32), FX_WARPS * 32, 0, s, (u32)C, cell_offset,
-               w.multi, sort_indx);
-  CCL_LAUNCH_CHECK("cell_fixup");
-  return CCL_OK;
-}
+// The sort after its first pass (ccl_sort.cu): offsets, scatter, fix-up.
+int index_sort_keyed(long np, long C, const u32 *indx, u32 *counts, u32 *cell_offset,
+                     u32 *sort_indx, u32 *np_stay, void *ws, size_t ws_bytes, cudaStream_t s);
 
 template <typename T>
 int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
@@ -808,7 +523,7 @@ int index_sort(long np, const T *x, const T *y, const T *z, GridP<T> g,
               cudaGetErrorString(me));
   if (np > 0) {
     launch_pdl(k_keys<T>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, g, indx, counts,
-               w.tile_ovf);
+               w.tile_ovf, (uint4 *)w.cursor, w.nclear4);
     CCL_LAUNCH_CHECK("keys");
   }
   return index_sort_keyed(np, C, indx, counts, cell_offset, sort_indx, np_stay, ws, ws_bytes,
@@ -835,10 +550,12 @@ int push_keys(long np, T *x, T *y, T *z, T *xl, T *yl, T *zl, const T *px, const
   if (xl) {
     mis |= ((uintptr_t)xl | (uintptr_t)yl | (uintptr_t)zl) & 15;
     launch_pdl(k_push_keys<T, true>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, xl, yl, zl,
-               px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf);
+               px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf,
+               (uint4 *)w.cursor, w.nclear4);
   } else {
     launch_pdl(k_push_keys<T, false>, (unsigned)ntiles, ST_THREADS, 0, s, np, x, y, z, nullptr,
-               nullptr, nullptr, px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf);
+               nullptr, nullptr, px, py, pz, g_inv, (T)dt, mis == 0, g, indx, counts, w.tile_ovf,
+               (uint4 *)w.cursor, w.nclear4);
   }
   CCL_LAUNCH_CHECK("push_x_keys");
   return CCL_OK;
@@ -852,8 +569,9 @@ __global__ void k_align(long n, int ncomp, ptrs<16> src, ptrs<16> dst,
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
        i += (long)gridDim.x * blockDim.x) {
     u32 j = idx[i];
-    for (int c = 0; c < ncomp; c++)
-      ((T *)dst.p[c])[i] = ((const T *)src.p[c])[j];
+#pragma unroll
+    for (int c = 0; c < 16; c++)
+      if (c < ncomp) ((T *)dst.p[c])[i] = ((const T *)src.p[c])[j];
   }
 }
 

@@ -264,22 +264,40 @@ __device__ __forceinline__ cplx<T> ld_mode(const T *p, long i, long ir, long ix,
 }
 
 template <typename T>
-__global__ void k_grad_combine(long n, int nx, const T *__restrict__ kx, ptrs<4> rho,
-                               ptrs<4> Pm, ptrs<4> Pp, ptrs<12> dN) {
+__global__ void __launch_bounds__(RC_THREADS)
+    k_grad_combine(int nx, const T *__restrict__ kx, ptrs<4> rho, ptrs<4> Pm, ptrs<4> Pp,
+                   ptrs<12> dN) {
   pdl_wait();
+  constexpr int RP = RcPer<T>;
   const int m = blockIdx.y;
-  CCL_GRID_STRIDE(i, n) {
-    const long ir = i / nx, ix = i - ir * nx;
-    const T k = kx[ix];
-    const cplx<T> r = ld_c((const T *)rho.p[m], i);
-    const cplx<T> tm = ld_mode((const T *)Pm.p[m], i, ir, ix, nx, m == 0);
-    const cplx<T> tp = ld_mode((const T *)Pp.p[m], i, ir, ix, nx, false);
-    const cplx<T> gx = {k * (-r.im), k * r.re};
-    const cplx<T> gy = {-tm.re + tp.re, -tm.im + tp.im};
-    const cplx<T> gz = {tm.im + tp.im, -(tm.re + tp.re)};
-    st_c((T *)dN.p[3 * m], i, gx);
-    st_c((T *)dN.p[3 * m + 1], i, gy);
-    st_c((T *)dN.p[3 * m + 2], i, gz);
+  const RowChunk<T> rc(nx);
+  const T *rh = (const T *)pick(rho, m), *pmm = (const T *)pick(Pm, m),
+          *ppm = (const T *)pick(Pp, m);
+  T *ox = (T *)pick(dN, 3 * m), *oy = (T *)pick(dN, 3 * m + 1), *oz = (T *)pick(dN, 3 * m + 2);
+  cplx<T> r[RP], tm[RP], tp[RP];
+#pragma unroll
+  for (int q = 0; q < RP; q++) {
+    const int ix = rc.col(q);
+    if (ix < nx) {
+      const long i = (long)rc.ir * nx + ix;
+      r[q] = ld_c(rh, i);
+      tm[q] = ld_mode(pmm, i, rc.ir, ix, nx, m == 0);
+      tp[q] = ld_mode(ppm, i, rc.ir, ix, nx, false);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RP; q++) {
+    const int ix = rc.col(q);
+    if (ix < nx) {
+      const long i = (long)rc.ir * nx + ix;
+      const T k = kx[ix];
+      const cplx<T> gx = {k * (-r[q].im), k * r[q].re};
+      const cplx<T> gy = {-tm[q].re + tp[q].re, -tm[q].im + tp[q].im};
+      const cplx<T> gz = {tm[q].im + tp[q].im, -(tm[q].re + tp[q].re)};
+      st_c(ox, i, gx);
+      st_c(oy, i, gy);
+      st_c(oz, i, gz);
+    }
   }
 }
 
@@ -290,35 +308,62 @@ __global__ void k_grad_combine(long n, int nx, const T *__restrict__ kx, ptrs<4>
 //   By = -i (kx Gz + U-_x + U+_x)
 //   Bz = i kx Gy + U-_x - U+_x
 template <typename T>
-__global__ void k_rot_combine(long n, int nx, const T *__restrict__ kx, ptrs<12> G,
-                              ptrs<12> Qm, ptrs<12> Qp, ptrs<4> poiss, ptrs<12> B) {
+__global__ void __launch_bounds__(RC_THREADS)
+    k_rot_combine(int nx, const T *__restrict__ kx, ptrs<12> G, ptrs<12> Qm, ptrs<12> Qp,
+                  ptrs<4> poiss, ptrs<12> B) {
   pdl_wait();
+  constexpr int RP = RcPer<T>;
   const int m = blockIdx.y;
-  CCL_GRID_STRIDE(i, n) {
-    const long ir = i / nx, ix = i - ir * nx;
-    const T k = kx[ix];
-    const cplx<T> gy = ld_c((const T *)G.p[3 * m + 1], i);
-    const cplx<T> gz = ld_c((const T *)G.p[3 * m + 2], i);
-    cplx<T> um[3], up[3];
+  const RowChunk<T> rc(nx);
+  const T *po = (const T *)pick(poiss, m);
+  const T *gyp = (const T *)pick(G, 3 * m + 1), *gzp = (const T *)pick(G, 3 * m + 2);
+  const T *qmp[3], *qpp[3];
+  T *bp[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      um[c] = ld_mode((const T *)Qm.p[3 * m + c], i, ir, ix, nx, m == 0);
-      up[c] = ld_mode((const T *)Qp.p[3 * m + c], i, ir, ix, nx, false);
+  for (int c = 0; c < 3; c++) {
+    qmp[c] = (const T *)pick(Qm, 3 * m + c);
+    qpp[c] = (const T *)pick(Qp, 3 * m + c);
+    bp[c] = (T *)pick(B, 3 * m + c);
+  }
+  cplx<T> gy[RP], gz[RP], um[RP][3], up[RP][3];
+  T f[RP];
+#pragma unroll
+  for (int q = 0; q < RP; q++) {
+    const int ix = rc.col(q);
+    if (ix < nx) {
+      const long i = (long)rc.ir * nx + ix;
+      gy[q] = ld_c(gyp, i);
+      gz[q] = ld_c(gzp, i);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        um[q][c] = ld_mode(qmp[c], i, rc.ir, ix, nx, m == 0);
+        up[q][c] = ld_mode(qpp[c], i, rc.ir, ix, nx, false);
+      }
+      f[q] = po ? po[i] : T(1);
     }
-    cplx<T> bx = {-um[2].re - um[1].im + up[2].re - up[1].im,
-                  -um[2].im + um[1].re + up[2].im + up[1].re};
-    const cplx<T> sy = {k * gz.re + um[0].re + up[0].re, k * gz.im + um[0].im + up[0].im};
-    cplx<T> by = {sy.im, -sy.re};
-    cplx<T> bz = {-k * gy.im + um[0].re - up[0].re, k * gy.re + um[0].im - up[0].im};
-    if (poiss.p[m]) {
-      const T f = ((const T *)poiss.p[m])[i];
-      bx.re *= f; bx.im *= f;
-      by.re *= f; by.im *= f;
-      bz.re *= f; bz.im *= f;
+  }
+#pragma unroll
+  for (int q = 0; q < RP; q++) {
+    const int ix = rc.col(q);
+    if (ix < nx) {
+      const long i = (long)rc.ir * nx + ix;
+      const T k = kx[ix];
+      cplx<T> bx = {-um[q][2].re - um[q][1].im + up[q][2].re - up[q][1].im,
+                    -um[q][2].im + um[q][1].re + up[q][2].im + up[q][1].re};
+      const cplx<T> sy = {k * gz[q].re + um[q][0].re + up[q][0].re,
+                          k * gz[q].im + um[q][0].im + up[q][0].im};
+      cplx<T> by = {sy.im, -sy.re};
+      cplx<T> bz = {-k * gy[q].im + um[q][0].re - up[q][0].re,
+                    k * gy[q].re + um[q][0].im - up[q][0].im};
+      if (po) {
+        bx.re *= f[q]; bx.im *= f[q];
+        by.re *= f[q]; by.im *= f[q];
+        bz.re *= f[q]; bz.im *= f[q];
+      }
+      st_c(bp[0], i, bx);
+      st_c(bp[1], i, by);
+      st_c(bp[2], i, bz);
     }
-    st_c((T *)B.p[3 * m], i, bx);
-    st_c((T *)B.p[3 * m + 1], i, by);
-    st_c((T *)B.p[3 * m + 2], i, bz);
   }
 }
 

@@ -84,7 +84,9 @@ int ccl_index_sort_workspace(long np, long ncells, size_t *bytes);
  *   sort_indx[np]           particle numbers in key order -- the sort is
  *                           stable, so within a cell in ascending order;
  *   np_stay[1] (device)     cell_offset[C], the in-window count.
- * The host reads nothing; np_stay stays on the device. */
+ * The host reads nothing; np_stay stays on the device.  The offsets come
+ * from a single-pass scan whose tiles wait (bounded) on their predecessors'
+ * sums; ccl_sort_status reports a wait that gave up. */
 int ccl_index_sort(int dtype, long np, const void *x, const void *y,
                    const void *z, int Nx, double xmin, double dx_inv, int Nr,
                    double rmin, double dr_inv, uint32_t *indx_in_cell,
@@ -96,9 +98,12 @@ int ccl_index_sort(int dtype, long np, const void *x, const void *y,
  * are formed from the coordinates the push has just computed instead of
  * being read back: ccl_push_x_keys runs push_xyz (ccl_push_x, or with
  * x_lo, y_lo, z_lo non-null ccl_push_x_compensated) and the first pass of
- * ccl_index_sort (indx_in_cell, sum_in_cell, and per-tile counts kept in the
- * workspace); ccl_index_sort_keyed, on the same workspace before any other
- * use of it, completes the sort (cell_offset, sort_indx, np_stay).  The
+ * ccl_index_sort (indx_in_cell, sum_in_cell, per-tile counts kept in the
+ * workspace, and the workspace's cursors and scan flags cleared);
+ * ccl_index_sort_keyed, on the same workspace before any other
+ * use of it, completes the sort (cell_offset, sort_indx, np_stay); run
+ * again with no key pass in between, its scan finds the workspace not
+ * cleared and sets ccl_sort_status (nothing is written out of bounds).  The
  * outputs are those of ccl_push_x followed by ccl_index_sort.  Replaces the
  * pair push_coords + sort_parts of the reference's loop (pic_loop.py:74-98,
  * particles_methods_cl.py:206-261) with no counterpart of its own. */
@@ -116,7 +121,7 @@ int ccl_index_sort_keyed(long np, int Nx, int Nr, const uint32_t *indx_in_cell,
  * reference: it is for callers that cannot allocate device memory for the
  * sort (a host binding that owns no device allocator, or a process whose
  * device memory is reserved up front by another framework).  The workspace is
- * a file-scope 8 MiB device array -- enough for up to 2,000,000 cells with up
+ * a file-scope 9 MiB device array -- enough for up to 2,000,000 cells with up
  * to 2^26 particles; larger inputs return CCL_ERR_WORKSPACE without
  * launching anything.  Each call outside a stream capture looks up the
  * array's device address on the calling device (cudaGetSymbolAddress); a
@@ -373,6 +378,21 @@ int ccl_dht_bf16x3_status(int reset);
  * about a second).  Writes 1 to the device int *gave_up when the wait ran
  * out and 0 when it completed; the context stays usable either way. */
 int ccl_wait_probe(long spins, int arrive, int *gave_up, void *stream);
+
+/* The cell sort's device error flag, no counterpart in the reference: the
+ * single-pass scan of the cell offsets (ccl_index_sort, ccl_index_sort_keyed)
+ * waits, bounded, for the sums of the tiles before its own; 0 = ok, else a
+ * wait gave up (that scan's offsets are then wrong).  reset != 0 clears it.
+ * It synchronises.  ccl_scan_wait_probe runs that bounded wait on its own:
+ * one tile of the scan looks back at a predecessor whose sum is published
+ * (publish != 0) or never written, polling at most `spins` times
+ * (1 <= spins <= 1,048,576); it writes 1 to the device int *gave_up when the
+ * wait ran out, else 0, and the tile's offset to scratch[6] (5 when the
+ * predecessor published, 0 when not); scratch: 8 device words, 8-byte
+ * aligned.  The context stays usable either way. */
+int ccl_sort_status(int reset);
+int ccl_scan_wait_probe(long spins, int publish, int *gave_up, uint32_t *scratch,
+                        void *stream);
 
 /* PSATD update of E and G in one azimuthal mode over ncells spectral cells.
  * flds: 15 complex device pointers E_x,E_y,E_z, G_x,G_y,G_z, J_x,J_y,J_z,

@@ -148,6 +148,23 @@ def test_index_sort_nearly_sorted_full_size(cuda, port):
     p["y"] += rng.uniform(-0.4, 0.4, p["y"].size) * g["dr"]
     for a, b in zip(oracle_sort(port, p, g), gpu_sort(p, g)[:4]):
         np.testing.assert_array_equal(b, a)
+    assert _lib.load().ccl_sort_status(1) == 0  # no bounded wait of the scan gave up
+
+
+def test_index_sort_many_scan_tiles(cuda, port):
+    # 4096 x 512 nodes: 2.09M cells, about a thousand tiles of the offsets'
+    # single-pass scan; random particle order (most cells claimed by many
+    # warps), then the same workspace again on a cell-ordered copy
+    rng = np.random.default_rng(9)
+    g = geom(4096, 512)
+    p = particles(rng, 2_000_000, g)
+    o = oracle_sort(port, p, g)
+    for a, b in zip(o, gpu_sort(p, g)[:4]):
+        np.testing.assert_array_equal(b, a)
+    q = {k: v[o[3]].copy() for k, v in p.items()}
+    for a, b in zip(oracle_sort(port, q, g), gpu_sort(q, g)[:4]):
+        np.testing.assert_array_equal(b, a)
+    assert _lib.load().ccl_sort_status(1) == 0
 
 
 def test_index_sort_workspace_too_small(cuda):

@@ -19,7 +19,7 @@ def _geom(Nx, Nr, Xmin=-20.0, Xmax=0.0, Rmax=8.0):
 
 
 def test_oversize_rejected_without_launch():
-    """Too large for the 8 MiB scratch: an error, before any CUDA call."""
+    """Too large for the 9 MiB scratch: an error, before any CUDA call."""
     if not os.path.exists(_lib.LIB_PATH):
         pytest.skip("library not built")
     lib = _lib.load()
