@@ -88,7 +88,8 @@ static inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 blo
 // combines load all of a thread's columns before their first store: the
 // field bundles may alias, so the compiler would not move the loads.)
 constexpr int RC_THREADS = 256;
-template <typename T> constexpr int RcPer = sizeof(T) == 4 ? 4 : 2;
+// (two columns per thread: four measured slower in FP32, fewer blocks per SM)
+template <typename T> constexpr int RcPer = 2;
 template <typename T> constexpr int RcCols = RC_THREADS * RcPer<T>;
 template <typename T> inline dim3 row_chunk_grid(int nrows, int nx, int nz) {
   return dim3((unsigned)nrows * (unsigned)((nx + RcCols<T> - 1) / RcCols<T>), (unsigned)nz);

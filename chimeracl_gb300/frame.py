@@ -49,9 +49,12 @@ class Frame:
             dom["Rmax"] = grid.Args["Rmax"]
             sp.make_new_domain(dom, density_profiles=self.Args["DensityProfiles"])
             sp.add_new_particles()
+        # every species sorted before any is aligned: the first align reads
+        # the in-window counts of all of them after one wait for the device
         for sp in species:
             sp.free_added()
             sp.sort_parts(grid=grid)
+        for sp in species:
             sp.align_parts()
             # right_lim = max x of the last Nppc+1 particles + ddx/2, kept on
             # the device until the next shift reads it (the value is the
