@@ -56,9 +56,10 @@ class Frame:
             sp.sort_parts(grid=grid)
         for sp in species:
             sp.align_parts()
-            # right_lim = max x of the last Nppc+1 particles + ddx/2, kept on
-            # the device until the next shift reads it (the value is the
-            # same double sum; the read no longer stalls this step).  With
+            # right_lim = max x of the last Nppc+1 particles + ddx/2, formed
+            # on the device and copied to pinned host memory at once (the
+            # value is the same double sum): neither this step nor the next
+            # shift, which reads it, waits for the device.  With
             # compensated coordinates x is x + x_lo: the next slab is then
             # placed where the FP64 run places it (from a rounded x the whole
             # slab would shift by that rounding)
@@ -84,4 +85,5 @@ class Frame:
                     first = torch.argmax(same.to(torch.int32))  # the last column wins
                     x_max = torch.where(same.any(), cand[first], x_max)
                 dict.__setitem__(sp.Args, "right_lim",
-                                 LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float))
+                                 LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float,
+                                            prefetch=True))

@@ -257,7 +257,15 @@ class ParticleMethodsCU(GenericMethodsCU):
             self.reset_num_parts()
             return
         src = [D[c] for c in comps_align]
-        dst = [torch.empty(ns, dtype=D[c].dtype, device=self.comm.device) for c in comps_align]
+        # one allocation for all the components (they share one dtype): the
+        # host part of a window shift is what the device waits for
+        dtypes = {D[c].dtype for c in comps_align}
+        if len(dtypes) == 1:
+            block = torch.empty(len(comps_align) * ns, dtype=dtypes.pop(), device=self.comm.device)
+            dst = list(block.view(len(comps_align), ns).unbind(0))
+        else:
+            dst = [torch.empty(ns, dtype=D[c].dtype, device=self.comm.device)
+                   for c in comps_align]
         call("ccl_align", self._dt, ns, len(src), PP(src), PP(dst), D["sort_indx"].data_ptr(),
              stream())
         for c, t in zip(comps_align, dst):
