@@ -77,6 +77,11 @@ class PIC_batch:
         if not self.candidates:
             raise ValueError("no lane count among the candidates fits the batch")
         self.tune_steps = int(tune_steps)
+        for lp in self.loops:
+            # the batch keeps the host busy with many runs' launches: a run
+            # captures its pieces again right at its window shift
+            if hasattr(lp, "eager_after_shift"):
+                lp.eager_after_shift = 0
         # candidate -> host seconds of its timed steps
         self.tune_log = {c: [] for c in self.candidates}
         self._streams = None
@@ -116,7 +121,8 @@ class PIC_batch:
         (eager) step: the step replays graphs only, unless a signature
         changed (checked after the step through the capture count)."""
         for lp in self.loops:
-            if lp.it == 0 or lp._frame_due() or lp.timit or lp.diags:
+            if (lp.it == 0 or lp._frame_due() or lp.timit or lp.diags
+                    or getattr(lp, "_eager_left", 0)):
                 return False
             if not (lp.graphs or self.one_graph):
                 return False

@@ -17,10 +17,10 @@ transforms) and the gather + push.  Each is captured on first use and
 replayed while a signature of what its launches depend on is unchanged:
 device buffers, particle counts and the grid origin for the particle
 pieces; the solver's buffers alone for the field piece.  A window shift
-(host-driven injection, new particle counts and origin) therefore runs only
-the particle pieces eagerly and captures them again -- the field solve,
-~65 of the step's library calls, is replayed through the shift (its phase
-factors are refreshed in place first)."""
+(host-driven injection, new particle counts and origin) therefore runs the
+particle pieces eagerly for a few steps and then captures them again --
+the field solve, ~65 of the step's library calls, is replayed through the
+shift (its phase factors are refreshed in place first)."""
 import collections
 import contextlib
 import gc
@@ -83,6 +83,10 @@ class PIC_loop:
         # finds the graphs of that stretch of the window again
         self._graphs = {}
         self._graph_cache = {}
+        # steps after a window shift that still launch the particle pieces
+        # eagerly before they are captured again (see step())
+        self.eager_after_shift = 2
+        self._eager_left = 0
         self.graph_replays = 0  # steps served by graph replays
         self.graph_captures = 0  # pieces captured
         self._cap_stream = None
@@ -141,24 +145,31 @@ class PIC_loop:
         if not use_graph:
             self._graphs = {}
             self._graph_cache = {}
+            self._eager_left = 0
             self._body(graph_mode=False)
         elif self._frame_due():
             # a window shift: host-driven injection, new particle counts and
-            # origin.  The particle pieces run eagerly and are captured again
-            # right after, while the device still executes this step; the
-            # field solve replays (its phase factors are moved first)
+            # origin.  The host had to wait for the device (the in-window
+            # counts), so it is no longer ahead: the particle pieces run
+            # eagerly on this step and the next eager_after_shift ones --
+            # each eager step puts the host further ahead, the device being
+            # slower than the launches -- and are captured again after that,
+            # when the capture's host time overlaps the device's queue.  The
+            # field solve replays throughout (its phase factors moved first)
             self._frame_part()
             for sol in self.solvers:
                 sol._phase(0)
                 sol._phase(1)
-            self._particles_before(graph_mode=True)
-            self._run_piece("f")
-            self._particles_after(graph_mode=True)
-            full = self._signature("pa")
-            for piece in ("pa", "pb"):
-                if not self._from_cache(piece, full):
-                    self._capture(piece)
-            self.graph_replays += 1
+            self._eager_left = self.eager_after_shift
+            self._eager_pieces()
+            if self._eager_left == 0:
+                full = self._signature("pa")
+                for piece in ("pa", "pb"):
+                    if not self._from_cache(piece, full):
+                        self._capture(piece)
+        elif self._eager_left > 0:
+            self._eager_left -= 1
+            self._eager_pieces()
         else:
             full = self._signature("pa")  # the same for both particle pieces
             for piece in ("pa", "f", "pb"):
@@ -166,6 +177,13 @@ class PIC_loop:
             self.graph_replays += 1
         self.it += 1
         return self.it
+
+    def _eager_pieces(self):
+        """One graph-mode step with the particle pieces launched eagerly."""
+        self._particles_before(graph_mode=True)
+        self._run_piece("f")
+        self._particles_after(graph_mode=True)
+        self.graph_replays += 1
 
     def _run_piece(self, piece, sig=None):
         g = self._graphs.get(piece)

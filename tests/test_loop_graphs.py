@@ -108,19 +108,41 @@ def test_pieces_captured_replayed_and_kept_through_shifts(loop):
     for _ in range(3):  # it = 2..4: replays only, no library call from Python
         s = _step(lp, log)
         assert s == [("replay", ids["pa"]), ("replay", ids["f"]), ("replay", ids["pb"])]
-    s5 = _step(lp, log)  # it = 5: window shift
-    assert s5.count("capture_begin") == 2  # particle pieces only
+    s5 = _step(lp, log)  # it = 5: window shift, the particle pieces eager
+    assert s5.count("capture_begin") == 0
     assert ("replay", ids["f"]) in s5  # the field solve replays through the shift
     assert "push_fields" not in s5  # ... and is not run eagerly
     assert s5.index("sp.push_coords") < s5.index(("replay", ids["f"])) < s5.index("gather_and_push")
+    assert lp.eager_after_shift == 2
+    for _ in range(lp.eager_after_shift):  # it = 6, 7: still eager (host gets ahead)
+        s = _step(lp, log)
+        assert s.count("capture_begin") == 0 and "sp.push_coords" in s
+        assert ("replay", ids["f"]) in s
+    s8 = _step(lp, log)  # it = 8: the particle pieces captured again, then replayed
+    assert s8.count("capture_begin") == 2
     assert lp._graphs["f"][0] is objs["f"] and lp._graphs["pa"][0] is not objs["pa"]
+    s9 = _step(lp, log)
+    assert s9.count("capture_begin") == 0 and len(s9) == 3
+    assert lp.graph_replays == 9 and lp.graph_captures == 5
+
+
+def test_capture_at_the_shift_when_no_eager_steps(loop):
+    lp, log, sol, sp = loop
+    lp.eager_after_shift = 0  # what a batch of runs uses
+    for _ in range(5):
+        _step(lp, log)
+    f_graph = lp._graphs["f"][0]
+    s5 = _step(lp, log)  # it = 5: shift; pieces eager, then captured right away
+    assert s5.count("capture_begin") == 2
+    assert s5.index("sp.push_coords") < s5.index("capture_begin")
+    assert lp._graphs["f"][0] is f_graph
     s6 = _step(lp, log)
     assert s6.count("capture_begin") == 0 and len(s6) == 3
-    assert lp.graph_replays == 6 and lp.graph_captures == 5
 
 
 def test_rebound_buffers_force_a_capture(loop):
     lp, log, sol, sp = loop
+    lp.eager_after_shift = 0  # the step at it = 5 (a shift) captures at once
     for _ in range(3):
         _step(lp, log)
     sol.DataDev["E"] = torch.zeros(4)  # a solver buffer rebound: all pieces
