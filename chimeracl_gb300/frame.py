@@ -6,6 +6,50 @@ import torch
 from .methods.generic_methods_cu import LazyScalar
 
 
+class TailLimit(LazyScalar):
+    """The injector's right limit (frame.py:56-64 of the reference): the
+    largest x of the last Nppc+1 particles after the align, plus ddx/2.  The
+    tail's few coordinates go to pinned host memory by one asynchronous copy
+    when the limit is formed; the arithmetic -- x (+ x_lo) in double, the
+    maximum, and for plain FP32 coordinates the snap to the injector's own
+    double value of a slab column whose FP32 rounding is that maximum (an
+    FP32 right limit would shift every later slab by its rounding) -- runs
+    on the host when the next window shift reads it, in the same IEEE
+    double operations the device would do.  Forming it costs the shift a
+    copy instead of a dozen small device operations, and reading it waits
+    for nothing."""
+
+    def __init__(self, x, x_lo, nppc, half_ddx, cand, comm=None):
+        tails = [x[-nppc:]] + ([x_lo[-nppc:]] if x_lo is not None else [])
+        self._tails = []
+        for t in tails:
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=t.is_cuda)
+            h.copy_(t, non_blocking=t.is_cuda)
+            self._tails.append(h)
+        super().__init__(self._tails[0], comm, float)  # (holds the tail, not the array)
+        if x.is_cuda:
+            self._event = torch.cuda.Event()
+            self._event.record()
+        self._half_ddx = float(half_ddx)
+        self._cand = None if cand is None else np.asarray(cand, dtype=np.float64)
+
+    def resolve(self):
+        if self.comm is not None:
+            self.comm.d2h_bytes += sum(h.numel() * h.element_size() for h in self._tails)
+        if self._event is not None:
+            self._event.synchronize()
+        xs = self._tails[0].numpy()
+        xt = xs.astype(np.float64)
+        if len(self._tails) > 1:
+            xt = xt + self._tails[1].numpy().astype(np.float64)
+        x_max = xt.max()
+        if self._cand is not None and self._cand.size:
+            same = xs.max() == self._cand.astype(np.float32)
+            if same.any():
+                x_max = self._cand[int(np.argmax(same))]  # the last column wins
+        return float(x_max + self._half_ddx)
+
+
 class Frame:
     def __init__(self, configs_in, comm=None):
         self._process_configs(configs_in)
@@ -56,34 +100,16 @@ class Frame:
             sp.sort_parts(grid=grid)
         for sp in species:
             sp.align_parts()
-            # right_lim = max x of the last Nppc+1 particles + ddx/2, formed
-            # on the device and copied to pinned host memory at once (the
-            # value is the same double sum): neither this step nor the next
-            # shift, which reads it, waits for the device.  With
+            # right_lim = max x of the last Nppc+1 particles + ddx/2 (with
             # compensated coordinates x is x + x_lo: the next slab is then
-            # placed where the FP64 run places it (from a rounded x the whole
-            # slab would shift by that rounding)
+            # placed where the FP64 run places it; from a rounded x the whole
+            # slab would shift by that rounding), formed on the host from a
+            # pinned copy of the tail (TailLimit)
             if sp.Args["Np"] > 0 and "InjectorSource" not in sp.Args:
                 nppc = int(np.prod(sp.Args["Nppc"]) + 1)
                 x = sp.DataDev["x"]
-                x_tail = x[-nppc:].to(torch.float64)
-                if "x_lo" in sp.DataDev:
-                    x_tail = x_tail + sp.DataDev["x_lo"][-nppc:].to(torch.float64)
-                x_max = x_tail.max()
-                if x.dtype == torch.float32 and "x_lo" not in sp.DataDev and \
-                        "_inj_last_x" in sp.Args:
-                    # FP32 coordinates: the last particles are normally the
-                    # fresh slab's last columns; where the maximum is one of
-                    # those columns' FP32 value, take the double value it
-                    # rounds (an FP32 right limit would shift every later
-                    # slab by its rounding)
-                    # (the candidates travel by one asynchronous pinned copy)
-                    cand = torch.tensor(sp.Args["_inj_last_x"], dtype=torch.float64)
-                    if x.is_cuda:
-                        cand = cand.pin_memory().to(x.device, non_blocking=True)
-                    same = x[-nppc:].max() == cand.to(torch.float32)
-                    first = torch.argmax(same.to(torch.int32))  # the last column wins
-                    x_max = torch.where(same.any(), cand[first], x_max)
+                x_lo = sp.DataDev.get("x_lo")
+                cand = (sp.Args["_inj_last_x"] if x.dtype == torch.float32 and x_lo is None
+                        and "_inj_last_x" in sp.Args else None)
                 dict.__setitem__(sp.Args, "right_lim",
-                                 LazyScalar(x_max + 0.5 * sp.Args["ddx"], sp.comm, float,
-                                            prefetch=True))
+                                 TailLimit(x, x_lo, nppc, 0.5 * sp.Args["ddx"], cand, sp.comm))
