@@ -365,16 +365,27 @@ class PICAdjoint:
                     r["source"] = id(source) if source is not None else id(_p)
                     _f(_p, source)
 
-                def alg(_p=p, _f=type(p).align_parts):
+                def rec_align(_p):
                     r = rec_of(_p)
                     r["np_pre"] = int(_p.Args["Np"])
                     ns = int(_p.Args["Np_stay"])
                     r["np_stay"] = ns
                     r["sort_indx"] = _p.DataDev["sort_indx"][:ns].clone()
+
+                def alg(_p=p, _f=type(p).align_parts):
+                    rec_align(_p)
+                    _f(_p)
+
+                def alb(_p=p, _f=getattr(type(p), "align_begin", None)):
+                    # (the window shift aligns in two halves; the record is
+                    # the same, taken before the permutation)
+                    rec_align(_p)
                     _f(_p)
                 pt.wrap(p, "make_new_domain", mnd)
                 pt.wrap(p, "add_new_particles", anp)
                 pt.wrap(p, "align_parts", alg)
+                if hasattr(type(p), "align_begin"):
+                    pt.wrap(p, "align_begin", alb)
             loop._frame_part()
         return fr
 

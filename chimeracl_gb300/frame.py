@@ -93,13 +93,21 @@ class Frame:
             dom["Rmax"] = grid.Args["Rmax"]
             sp.make_new_domain(dom, density_profiles=self.Args["DensityProfiles"])
             sp.add_new_particles()
-        # every species sorted before any is aligned: the first align reads
-        # the in-window counts of all of them after one wait for the device
+        # every species sorted, and its permutation queued, before the first
+        # in-window count is read: one wait for the device, and the host work
+        # after it is only the arrays' cut to their counts
         for sp in species:
             sp.free_added()
             sp.sort_parts(grid=grid)
+        two_halves = all(hasattr(sp, "align_begin") for sp in species)
         for sp in species:
-            sp.align_parts()
+            if two_halves:
+                sp.align_begin()
+        for sp in species:
+            if two_halves:
+                sp.align_end()
+            else:
+                sp.align_parts()
             # right_lim = max x of the last Nppc+1 particles + ddx/2 (with
             # compensated coordinates x is x + x_lo: the next slab is then
             # placed where the FP64 run places it; from a rounded x the whole

@@ -248,30 +248,45 @@ class ParticleMethodsCU(GenericMethodsCU):
         dict.__setitem__(self.Args, "Np_stay", LazyScalar(D["Np_stay_dev"], self.comm))
 
     def align_and_damp(self, comps_align):
-        """particles_methods_cl.py:263-286"""
+        """particles_methods_cl.py:263-286, in two halves (align_queue,
+        align_finish): every particle is permuted into cell order -- the
+        out-of-window ones last, as the sort leaves them -- before the
+        in-window count is read, so the copies are queued while the host
+        still runs ahead of the device; after the read the arrays only become
+        views of their first Np_stay entries."""
+        self.align_finish(self.align_queue(comps_align))
+
+    def align_queue(self, comps_align):
+        D = self.DataDev
+        Np = self.Args["Np"]
+        if Np == 0:
+            return comps_align, None, None
+        src = [D[c] for c in comps_align]
+        # one allocation for all the components (they share one dtype)
+        dtypes = {t.dtype for t in src}
+        if len(dtypes) == 1:
+            block = torch.empty(len(src) * Np, dtype=dtypes.pop(), device=self.comm.device)
+            dst = list(block.view(len(src), Np).unbind(0))
+        else:
+            dst = [torch.empty(Np, dtype=t.dtype, device=self.comm.device) for t in src]
+        call("ccl_align", self._dt, Np, len(src), PP(src), PP(dst), D["sort_indx"].data_ptr(),
+             stream())
+        order = torch.empty(Np, dtype=torch.int32, device=self.comm.device)
+        call("ccl_iota_u32", order.data_ptr(), Np, stream())
+        return comps_align, dst, order
+
+    def align_finish(self, state):
+        comps_align, dst, order = state
         D = self.DataDev
         ns = self.Args["Np_stay"]
-        if ns == 0:
+        if ns == 0 or dst is None:
             for comp in comps_align + ["sort_indx"]:
                 D[comp] = D[comp][:0].clone()
             self.reset_num_parts()
             return
-        src = [D[c] for c in comps_align]
-        # one allocation for all the components (they share one dtype): the
-        # host part of a window shift is what the device waits for
-        dtypes = {D[c].dtype for c in comps_align}
-        if len(dtypes) == 1:
-            block = torch.empty(len(comps_align) * ns, dtype=dtypes.pop(), device=self.comm.device)
-            dst = list(block.view(len(comps_align), ns).unbind(0))
-        else:
-            dst = [torch.empty(ns, dtype=D[c].dtype, device=self.comm.device)
-                   for c in comps_align]
-        call("ccl_align", self._dt, ns, len(src), PP(src), PP(dst), D["sort_indx"].data_ptr(),
-             stream())
         for c, t in zip(comps_align, dst):
-            D[c] = t
-        D["sort_indx"] = torch.empty(ns, dtype=torch.int32, device=self.comm.device)
-        call("ccl_iota_u32", D["sort_indx"].data_ptr(), ns, stream())
+            D[c] = t[:ns]
+        D["sort_indx"] = order[:ns]
         self.reset_num_parts()
 
     def reset_num_parts(self, Np=None):

@@ -46,6 +46,19 @@ class Particles(ParticleMethodsCU):
             return
         self.align_and_damp(comps_align=self._comps())
 
+    def align_begin(self):
+        """align_parts in two halves, for several species at a window shift:
+        this one queues the permutation and reads nothing back ..."""
+        self._align_state = None
+        if self.Args["Np"] != 0:
+            self._align_state = self.align_queue(self._comps())
+
+    def align_end(self):
+        """... this one reads the in-window count and cuts the arrays to it."""
+        state, self._align_state = getattr(self, "_align_state", None), None
+        if state is not None:
+            self.align_finish(state)
+
     def _process_configs(self, configs_in):
         """particles.py:53-100"""
         A = self.Args = configs_in if isinstance(configs_in, ArgsDict) else ArgsDict(configs_in)
