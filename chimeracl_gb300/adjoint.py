@@ -156,7 +156,7 @@ class PICAdjoint:
     def wake_loss(self, width=20.0):
         """mean(Ex_m0[1, ix]^2) over the last `width` of the window at the end
         of run() (float64)."""
-        sel = torch.as_tensor(self.loss_window(width), device=self.dev)
+        sel = self._upload(self.loss_window(width), np.int64)
         row = self._final_state()["ex_row"][sel]
         return (row * row).mean()
 
@@ -278,8 +278,20 @@ class PICAdjoint:
                  PP([d for d, _ in part]), PP([s_ for _, s_ in part]), stream())
 
     def _snapshot(self, tensors):
-        """Fresh copies of `tensors` (one batched launch)."""
-        out = [torch.empty_like(t) for t in tensors]
+        """Fresh copies of `tensors` (one batched launch); one allocation per
+        group of equal shape and dtype (the recording runs on the host's
+        clock: an allocation per tensor cost more than the copies)."""
+        groups = {}
+        for i, t in enumerate(tensors):
+            groups.setdefault((t.dtype, tuple(t.shape)), []).append(i)
+        out = [None] * len(tensors)
+        for (dt, shape), idx in groups.items():
+            if len(idx) == 1:
+                out[idx[0]] = torch.empty(shape, dtype=dt, device=self.dev)
+            else:
+                block = torch.empty((len(idx),) + shape, dtype=dt, device=self.dev)
+                for i, v in zip(idx, block.unbind(0)):
+                    out[i] = v
         self._copies(list(zip(out, tensors)))
         return out
 
@@ -312,7 +324,16 @@ class PICAdjoint:
             rec.mob.append(d)
         rec.imm = [{"x": p.DataDev["x"], "y": p.DataDev["y"], "z": p.DataDev["z"],
                     "w": p.DataDev["w"], "Np": int(p.Args["Np"])} for p in imm]
-        if frame or not self.graphs:
+        if frame and self.graphs:
+            # as the loop's own shift step: particle pieces eager, the field
+            # solve replayed (phase factors moved first)
+            for sol in loop.solvers:
+                sol._phase(0)
+                sol._phase(1)
+            loop._eager_pieces()
+            loop._eager_left = 0  # the next steps replay (their graphs are cached)
+            loop.it += 1
+        elif frame or not self.graphs:
             loop._step_part(graph_mode=False)
             loop.it += 1
         else:
@@ -401,7 +422,7 @@ class PICAdjoint:
         D, A, M = S.DataDev, S.Args, self.M
         final_it = self._final_state()["it"]
         # the loss seed on the final real-space Ex_m0
-        sel = torch.as_tensor(self.loss_window(width), device=self.dev)
+        sel = self._upload(self.loss_window(width), np.int64)
         seed = torch.zeros(self.Nx, dtype=torch.float64, device=self.dev)
         seed[sel] = 2.0 * self._final_state()["ex_row"][sel] / len(sel) * float(grad_output)
         self._seed = seed.to(self.real)
@@ -791,6 +812,15 @@ class PICAdjoint:
                 if inj is not None and self.profile is not None and inj["profiles"]:
                     self._knots(inj["dom"], inj["x_new"], inj["w_new"], pre["w"][n0:].contiguous())
 
+    def _upload(self, a, dtype=np.float64):
+        """A host array on the device, through pinned memory: a copy from
+        pageable memory would wait for the whole reverse sweep queued so
+        far."""
+        h = torch.from_numpy(np.ascontiguousarray(a, dtype=dtype))
+        if torch.device(self.dev).type != "cuda":
+            return h.to(self.dev)
+        return h.pin_memory().to(self.dev, non_blocking=True)
+
     def _knots(self, dom, x, w, lw):
         """Accumulate the profile-knot adjoints of the weights w = w0 f(x) of
         particles placed in the domain `dom` (the knots dens_profile used)."""
@@ -801,9 +831,7 @@ class PICAdjoint:
         i1 = int((xp < dom["Xmax"]).sum() + 1)
         xl, fl = xp[i0:i1], fp[i0:i1]
         dxm1 = 1.0 / (xl[1:] - xl[:-1])
-        t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64,
-                                      device=self.dev)
-        xl_d, fl_d, dx_d = t(xl), t(fl), t(dxm1)
+        xl_d, fl_d, dx_d = (self._upload(a) for a in (xl, fl, dxm1))
         out = torch.zeros(len(xl), dtype=torch.float64, device=self.dev)
         call("ccl_dens_profile_adjoint", self.dt_ccl, x.numel(), x.data_ptr(), w.data_ptr(),
              lw.data_ptr(), xl_d.data_ptr(), fl_d.data_ptr(), dx_d.data_ptr(), len(xl),

@@ -169,6 +169,8 @@ def restore_checkpoint(loop, ckpt):
             obj.flag_sorted = entry["flag_sorted"]
     _copy_into(pairs)
     loop.it = ckpt.it
+    if hasattr(loop, "_eager_left"):
+        loop._eager_left = 0  # no eager steps pending: graphs are found by signature
     # a graph whose buffers were rebound, or whose particle counts or grid
     # origin differ, fails its signature check and is captured again
 

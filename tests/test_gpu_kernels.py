@@ -881,3 +881,25 @@ def test_gemm_batch_per_entry_columns(cuda):
     for i in range(2):
         ref = host(A[i]) @ host(X[i])
         assert np.abs(host(Y[i]) - ref).max() <= FFT_TOL * np.abs(ref).max()
+
+
+def test_copy_batch_aligned_misaligned_and_ragged(cuda):
+    """ccl_copy_batch: 16-byte vector path where both arrays are 16-byte
+    aligned, word by word otherwise; sizes with a ragged tail, empty arrays,
+    and arrays of very different lengths in one launch."""
+    from chimeracl_gb300._lib import longs
+    rng = np.random.default_rng(71)
+    words = [0, 1, 3, 4, 5, 1023, 4096 * 257 + 3, 17]
+    offs = [0, 0, 1, 0, 2, 1, 0, 3]  # word offsets into the buffers (1..3: misaligned)
+    srcs = [torch.from_numpy(rng.integers(0, 2**31, n + 8, dtype=np.int64).astype(np.int32)).cuda()
+            for n in words]
+    dsts = [torch.full((n + 8,), -7, dtype=torch.int32, device="cuda") for n in words]
+    ptr = lambda t, o: t.data_ptr() + 4 * o  # noqa: E731
+    call("ccl_copy_batch", len(words), longs([4 * n for n in words]),
+         (C.c_void_p * len(words))(*[ptr(d, o) for d, o in zip(dsts, offs)]),
+         (C.c_void_p * len(words))(*[ptr(s, o) for s, o in zip(srcs, offs)]), S())
+    torch.cuda.synchronize()
+    for n, o, s, d in zip(words, offs, srcs, dsts):
+        hs, hd = host(s), host(d)
+        np.testing.assert_array_equal(hd[o:o + n], hs[o:o + n])
+        assert (hd[:o] == -7).all() and (hd[o + n:] == -7).all()  # nothing outside
