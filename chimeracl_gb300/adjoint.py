@@ -46,6 +46,7 @@ import torch
 
 from ._lib import PP, call, ints, longs, stream
 from .checkpoint import restore_checkpoint, save_checkpoint
+from .methods.generic_methods_cu import LazyScalar
 from .methods.solver_methods_cu import psatd_split_coefficients
 from .pic_loop import capture_guard
 
@@ -104,6 +105,11 @@ class PICAdjoint:
         self.profile_phases = False
         self.timing = {}
         self.checkpoints = {}
+        # per window-shift step of the forward: each species' in-window count
+        # after the shift's align (the recomputation's align takes it from
+        # here instead of waiting for the device; checked after the sweep)
+        self._shift_counts = {}
+        self._count_checks = []
         self.nsteps = 0
         comm = self.S.comm
         self.dt_ccl = comm.ccl
@@ -118,10 +124,20 @@ class PICAdjoint:
         """Step the run nsteps times, keeping a checkpoint every `every`."""
         loop = self.loop
         self.it0 = loop.it
+        # keep the particle pieces' graphs of every window position of the
+        # run: the reverse sweep's recomputation replays them all (each
+        # holds its position's particle arrays)
+        shifts = [fr.Args["Steps"] for fr in loop.frames]
+        epochs = int(nsteps) // max(1, int(min(shifts))) + 2 if shifts else 1
+        loop.graph_cache_size = max(loop.graph_cache_size, epochs)
         for _ in range(int(nsteps)):
             if (loop.it - self.it0) % self.every == 0:
                 self.checkpoints[loop.it] = save_checkpoint(loop)
+            it, shift = loop.it, loop._frame_due()
             loop.step()
+            if shift:  # the align left Np = the in-window count (a host int)
+                self._shift_counts[it] = {id(p): dict.__getitem__(p.Args, "Np")
+                                          for p in loop.species}
         self.nsteps = loop.it - self.it0
         # the final state the loss reads (the reverse sweep leaves the run at
         # its start; gradients() may be called more than once)
@@ -389,6 +405,14 @@ class PICAdjoint:
                 def rec_align(_p):
                     r = rec_of(_p)
                     r["np_pre"] = int(_p.Args["Np"])
+                    known = self._shift_counts.get(loop.it, {}).get(id(_p))
+                    lazy = dict.__getitem__(_p.Args, "Np_stay")
+                    if isinstance(known, int) and isinstance(lazy, LazyScalar):
+                        # the forward's count for this shift: no wait here
+                        # (the recomputation is the forward's arithmetic;
+                        # gradients() compares the two after the sweep)
+                        self._count_checks.append((lazy, known))
+                        dict.__setitem__(_p.Args, "Np_stay", known)
                     ns = int(_p.Args["Np_stay"])
                     r["np_stay"] = ns
                     r["sort_indx"] = _p.DataDev["sort_indx"][:ns].clone()
@@ -460,6 +484,11 @@ class PICAdjoint:
             tm["reverse"] += t3 - t2
         self._graph = None
         self._cur = None
+        checks, self._count_checks = self._count_checks, []
+        for lazy, known in checks:
+            if lazy.resolve() != known:
+                raise RuntimeError("adjoint: a recomputed window shift kept %d particles where "
+                                   "the forward kept %d" % (lazy.resolve(), known))
         # t = 0: the prefilled particles' weights, the laser
         restore_checkpoint(loop, self.checkpoints[self.it0])
         if self.profile is not None and self.prefill is not None:

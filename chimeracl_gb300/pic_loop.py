@@ -78,11 +78,12 @@ class PIC_loop:
         self._events = []
         self.graphs = graphs
         # piece name -> [graph, signature, library kernels in it] (the one in
-        # use), and per piece the last GRAPH_CACHE captures by signature: a
-        # run restored to an earlier step (a recompute from a checkpoint)
-        # finds the graphs of that stretch of the window again
+        # use), and per piece the last graph_cache_size captures by
+        # signature: a run restored to an earlier step (a recompute from a
+        # checkpoint) finds the graphs of that stretch of the window again
         self._graphs = {}
         self._graph_cache = {}
+        self.graph_cache_size = GRAPH_CACHE
         # steps after a window shift that still launch the particle pieces
         # eagerly before they are captured again (see step())
         self.eager_after_shift = 2
@@ -236,7 +237,7 @@ class PIC_loop:
         entry = self._graphs[piece] = [g, self._signature(piece), nk]
         cache = self._graph_cache.setdefault(piece, collections.OrderedDict())
         cache[entry[1][0]] = entry
-        while len(cache) > GRAPH_CACHE:
+        while len(cache) > self.graph_cache_size:
             cache.popitem(last=False)
         self.graph_captures += 1
         self.graph_kernels_captured += nk
