@@ -209,3 +209,76 @@ def test_fp64_right_limits_are_injector_columns(nppc):
     assert len(seen) == 5
     for x_max, xs in seen:
         assert x_max in xs, (x_max, xs)
+
+
+class _TwoHalfSpecies(_FrameSpecies):
+    """Stub species with the two-half align: logs the order of the calls."""
+
+    def __init__(self, name, log, x):
+        super().__init__(x)
+        self.name, self.log = name, log
+
+    def sort_parts(self, grid):
+        self.log.append(("sort", self.name))
+
+    def align_begin(self):
+        self.log.append(("align_begin", self.name))
+
+    def align_end(self):
+        self.log.append(("align_end", self.name))
+
+    def align_parts(self):
+        raise AssertionError("the shift aligns in two halves when every species can")
+
+
+def test_shift_queues_every_align_before_reading_any_count():
+    """At a window shift every species is sorted and its align queued
+    before the first in-window count is read (align_end)."""
+    from chimeracl_gb300.frame import Frame
+    from chimeracl_gb300.methods.generic_methods_cu import ArgsDict
+    log = []
+    sps = [_TwoHalfSpecies(n, log, np.float32(np.linspace(-3.0, 7.3, 12))) for n in "ei"]
+    for sp in sps:
+        sp.Args = ArgsDict(sp.Args)
+    grid = _Stub()
+    grid.Args = {"Xmax": 8.0, "Rmin": 0.0, "Rmax": 4.0}
+    Frame({"Steps": 2, "Velocity": 1.0, "dt": 0.5}).inject_plasma(sps, grid)
+    kinds = [k for k, _ in log]
+    assert kinds == ["sort", "sort", "align_begin", "align_begin", "align_end", "align_end"]
+    assert [n for k, n in log if k == "align_end"] == ["e", "i"]
+
+
+def test_tail_limit_is_the_device_formula():
+    """TailLimit (host double arithmetic on a copy of the tail) equals the
+    torch formula it replaces: max of x (+ x_lo) in double over the last
+    Nppc+1 particles, for FP32 the snap to a candidate column's double value
+    when the FP32 maximum is that column's rounding, + ddx/2."""
+    import torch
+    from chimeracl_gb300.frame import TailLimit
+    rng = np.random.default_rng(3)
+    for trial in range(200):
+        n = int(rng.integers(1, 30))
+        nppc = int(rng.integers(1, 12))
+        x = np.float32(rng.uniform(-5, 5, n))
+        comp = trial % 3 == 1
+        lo = np.float32(np.spacing(x) * rng.uniform(-0.5, 0.5, n)) if comp else None
+        cand = None
+        if trial % 3 == 2:
+            cand = list(rng.uniform(-5, 5, 4))
+            if trial % 2:  # make the tail's maximum one candidate's FP32 rounding
+                x[-1] = np.float32(max(np.float64(x[-nppc:].max()) + 1.0, cand[1]))
+                cand[1] = float(x[-1]) + 1e-9 * rng.uniform(-1, 1)
+                x[-1] = np.float32(cand[1])
+        half = 0.5 * float(rng.uniform(0.01, 0.5))
+        xt, lt = torch.tensor(x), (torch.tensor(lo) if comp else None)
+        got = TailLimit(xt, lt, nppc, half, cand).resolve()
+        tail = xt[-nppc:].to(torch.float64)
+        if comp:
+            tail = tail + lt[-nppc:].to(torch.float64)
+        want = tail.max()
+        if cand is not None:
+            c = torch.tensor(cand, dtype=torch.float64)
+            same = xt[-nppc:].max() == c.to(torch.float32)
+            first = torch.argmax(same.to(torch.int32))
+            want = torch.where(same.any(), c[first], want)
+        assert got == float(want + half), trial
