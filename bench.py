@@ -543,10 +543,13 @@ def load_peaks():
 
 
 # DRAM bytes (read + write) per call of the 2048 x 256, M = 1 workload, summed
-# over the call's kernels in one ncu capture:
+# over the call's kernels in one ncu capture.  ccl_index_sort:
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
 #       --clock-control none --nvtx --nvtx-include "prof/" <one sort of the workload>
-MEASURED_TRAFFIC = {"ccl_index_sort": 86.7e6}
+# ccl_index_sort_keyed (k_scan_lookback 2.1 MB + k_scatter 20.8 MB +
+# k_cell_fixup 2.0 MB, the sort_indx the scatter writes staying in L2):
+#   profiles/sort_and_combine_kernels_mixed_2048x256_ncu_full.md
+MEASURED_TRAFFIC = {"ccl_index_sort": 86.7e6, "ccl_index_sort_keyed": 24.9e6}
 
 
 def roofline(probe_summary, peaks, src):
