@@ -144,7 +144,7 @@ static __global__ void __launch_bounds__(LB_THREADS)
     k_scan_lookback(const u32 *__restrict__ in, long L, u32 *__restrict__ out,
                     u32 *__restrict__ total_out, u32 *__restrict__ tap, long tap_i,
                     unsigned long long *status, u32 *ticket, long ntiles, long spin_limit,
-                    int *err) {
+                    int *err, long tile0) {
   pdl_wait();
   __shared__ u32 sh[32];
   __shared__ u32 s_tile, s_stop;
@@ -155,7 +155,9 @@ static __global__ void __launch_bounds__(LB_THREADS)
     if (threadIdx.x == 0) atomicExch(err ? err : &g_sort_error, 1);
     return;
   }
-  const long base = t * LB_TILE + (long)threadIdx.x * LB_ITEMS;
+  // (tile0: the tile that in[0] starts -- 0 but for the wait probe, whose
+  // one tile of data is tile 1 of its scan)
+  const long base = (t - tile0) * LB_TILE + (long)threadIdx.x * LB_ITEMS;
   const bool vin = ((uintptr_t)in & 15) == 0 && base + LB_ITEMS <= L;
   u32 v[LB_ITEMS];
   if (vin) {
@@ -231,7 +233,7 @@ int scan_lookback(const u32 *in, long L, u32 *out, u32 *total_out, u32 *tap, lon
   if (L <= 0) return CCL_OK;
   const long nt = scan_lookback_tiles(L);
   launch_pdl(k_scan_lookback, (unsigned)nt, LB_THREADS, 0, s, in, L, out, total_out, tap, tap_i,
-             status, ticket, nt, SORT_SPIN_LIMIT, (int *)nullptr);
+             status, ticket, nt, SORT_SPIN_LIMIT, (int *)nullptr, 0L);
   CCL_LAUNCH_CHECK("scan_lookback");
   return CCL_OK;
 }
@@ -525,9 +527,9 @@ int scan_wait_probe(long spins, int publish, int *gave_up, u32 *scratch, cudaStr
   CCL_REQUIRE(e == cudaSuccess, CCL_ERR_CUDA, "scan wait probe: %s", cudaGetErrorString(e));
   k_scan_probe_setup<<<1, 1, 0, s>>>(status, ticket, in, publish);
   CCL_LAUNCH_CHECK("scan_probe_setup");
-  // one tile of L = 1: tile 1 of a scan whose tile 0 is status[0]
-  k_scan_lookback<<<1, LB_THREADS, 0, s>>>(in - LB_TILE, LB_TILE + 1, out - LB_TILE, nullptr,
-                                           nullptr, -1, status, ticket, 2, spins, gave_up);
+  // one item (L = 1) in tile 1 of a scan whose tile 0 is status[0]
+  k_scan_lookback<<<1, LB_THREADS, 0, s>>>(in, 1, out, nullptr, nullptr, -1, status, ticket, 2,
+                                           spins, gave_up, 1);
   CCL_LAUNCH_CHECK("scan_wait_probe");
   return CCL_OK;
 }
