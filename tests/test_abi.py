@@ -64,3 +64,21 @@ def test_invalid_arguments_rejected_without_launch():
     assert lib.ccl_index_sort_keyed(10, 64, 2, None, None, None, None, None, None, 0, None) == 1
     assert b"grid" in lib.ccl_last_error()
     assert lib.ccl_index_sort_keyed(-1, 64, 16, None, None, None, None, None, None, 0, None) == 1
+
+
+def test_sort_wait_probe_arguments_rejected_without_launch():
+    """The sort's bounded-wait probe checks its arguments before any CUDA
+    call: NULL flag or scratch, a poll count outside [1, 2^20], a scratch
+    not 8-byte aligned."""
+    from chimeracl_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    assert lib.ccl_scan_wait_probe(100, 0, None, 8, None) == 1
+    assert b"NULL" in lib.ccl_last_error()
+    assert lib.ccl_scan_wait_probe(100, 0, 8, None, None) == 1
+    assert lib.ccl_scan_wait_probe(0, 0, 8, 8, None) == 1
+    assert b"spins" in lib.ccl_last_error()
+    assert lib.ccl_scan_wait_probe((1 << 20) + 1, 0, 8, 8, None) == 1
+    assert lib.ccl_scan_wait_probe(100, 0, 8, 12, None) == 1
+    assert b"aligned" in lib.ccl_last_error()
