@@ -40,8 +40,7 @@ class Grid(GridMethodsCU):
     def gather_and_push(self, species=()):
         """Ghost rows of E, B, then gather + Boris push of the mobile species
         (grid.py:56-66)."""
-        for fld in ("E", "B"):
-            self.preproc_project_vec(fld)
+        self.preproc_project_vecs(("E", "B"))  # both fields' ghost rows, one launch
         for parts in species:
             if "Immobile" in parts.Args:
                 continue

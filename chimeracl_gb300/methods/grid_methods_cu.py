@@ -80,8 +80,12 @@ class GridMethodsCU(GenericMethodsCU):
 
     def preproc_project_vec(self, vec_fld):
         """grid_methods_cl.py:153-166"""
+        self.preproc_project_vecs((vec_fld,))
+
+    def preproc_project_vecs(self, vec_flds):
+        """preproc_project_vec of several vector fields in one launch."""
         M = self.Args["M"]
-        names = [vec_fld + c for c in self.Args["vec_comps"]]
+        names = [v + c for v in vec_flds for c in self.Args["vec_comps"]]
         flds = [self.DataDev[f + "_m" + str(m)] for f in names for m in range(M + 1)]
         call("ccl_warp_axis", self._dt, M, len(names), PP(flds), self.Args["Nx"], stream())
 
