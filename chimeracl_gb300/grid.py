@@ -18,18 +18,24 @@ class Grid(GridMethodsCU):
         self._init_grid_data_on_dev()
         self.send_args_to_dev()
 
-    def depose_charge(self, species=()):
+    def depose_charge(self, species=(), zero=True):
         """rho = sum over species of the charge deposit, then axis and 1/dV
-        (grid.py:23-31)."""
-        self.set_many([self.DataDev["rho_m" + str(m)] for m in range(self.Args["M"] + 1)], 0)
+        (grid.py:23-31).  zero=False: rho was cleared already (the loop
+        clears it with J, in one launch)."""
+        if zero:
+            self.set_many([self.DataDev["rho_m" + str(m)] for m in range(self.Args["M"] + 1)], 0)
         for parts in species:
             self.depose_scalar(parts, "w", "rho", charge=parts.Args["charge"])
         self.postproc_depose_scalar("rho")
 
-    def depose_currents(self, species=()):
-        """J from the mobile species (grid.py:33-54)."""
+    def depose_currents(self, species=(), also_zero=()):
+        """J from the mobile species (grid.py:33-54).  also_zero: scalar
+        fields (e.g. "rho") cleared in the same launch as J."""
+        M = self.Args["M"]
         self.set_many([self.DataDev["J" + c + "_m" + str(m)]
-                       for m in range(self.Args["M"] + 1) for c in self.Args["vec_comps"]], 0)
+                       for m in range(M + 1) for c in self.Args["vec_comps"]]
+                      + [self.DataDev[f + "_m" + str(m)] for f in also_zero for m in range(M + 1)],
+                      0)
         mom = ["p" + c for c in self.Args["vec_comps"]]
         for parts in species:
             if "Immobile" in parts.Args:

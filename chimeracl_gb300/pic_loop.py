@@ -273,7 +273,9 @@ class PIC_loop:
 
         self.timer_start()
         for solver in self.solvers:
-            solver.depose_currents(species=self.species)
+            # rho is cleared here with J (one launch); the charge deposit
+            # below then adds onto it
+            solver.depose_currents(species=self.species, also_zero=("rho",))
         self.timer_record("depose")
 
         for parts in self.species:
@@ -286,7 +288,7 @@ class PIC_loop:
 
         for solver in self.solvers:
             self.timer_start()
-            solver.depose_charge(species=self.species)
+            solver.depose_charge(species=self.species, zero=False)
             self.timer_record("depose")
 
     def _fields(self, graph_mode):
