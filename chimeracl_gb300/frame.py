@@ -27,6 +27,7 @@ class TailLimit(LazyScalar):
             h.copy_(t, non_blocking=t.is_cuda)
             self._tails.append(h)
         super().__init__(self._tails[0], comm, float)  # (holds the tail, not the array)
+        self._event = None
         if x.is_cuda:
             self._event = torch.cuda.Event()
             self._event.record()

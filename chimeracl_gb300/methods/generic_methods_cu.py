@@ -36,31 +36,16 @@ def torch_dtype(dtype):
 
 class LazyScalar:
     """A device scalar read back only when the host asks for its value
-    (as an int, or through ``cast``).
+    (as an int, or through ``cast``)."""
 
-    With ``prefetch`` the value starts its way to pinned host memory at once
-    (an asynchronous copy ordered after the kernels that form it, and an
-    event): a read long after -- the injector's right limit, read at the
-    next window shift -- then finds it there instead of waiting for the
-    device to finish everything queued since."""
-
-    def __init__(self, tensor, comm=None, cast=int, prefetch=False):
+    def __init__(self, tensor, comm=None, cast=int):
         self.tensor = tensor
         self.comm = comm
         self.cast = cast
-        self._host = self._event = None
-        if prefetch and tensor.is_cuda:
-            self._host = torch.empty(tensor.shape, dtype=tensor.dtype, pin_memory=True)
-            self._host.copy_(tensor, non_blocking=True)
-            self._event = torch.cuda.Event()
-            self._event.record()
 
     def resolve(self):
         if self.comm is not None:
             self.comm.d2h_bytes += self.tensor.element_size()
-        if self._event is not None:
-            self._event.synchronize()
-            return self.cast(self._host.item())
         return self.cast(self.tensor.item())
 
 
