@@ -232,3 +232,21 @@ def test_one_graph_captures_once_and_replays(fakes, monkeypatch):
     assert all(lp.origin == 2 for lp in loops)
     b.step()  # new signatures: captured again
     assert b.graph_captures == 2 and all(lp.it == 7 for lp in loops)
+
+
+def test_batch_runs_capture_at_their_window_shift(fakes):
+    """A batch keeps the host busy with all its runs' launches: its loops
+    capture their particle pieces right at a window shift (no eager steps
+    after it), and a run with eager steps pending makes a batch step
+    ineligible for one graph / autotuning."""
+    log = fakes
+    loops = [FakeLoop(i, log) for i in range(3)]
+    for lp in loops:
+        lp.eager_after_shift, lp._eager_left = 2, 0
+    b = bm.PIC_batch(loops, lanes=1)
+    assert all(lp.eager_after_shift == 0 for lp in loops)
+    for lp in loops:
+        lp.it = 3
+    assert b._eligible()
+    loops[1]._eager_left = 1
+    assert not b._eligible()

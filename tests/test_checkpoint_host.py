@@ -89,7 +89,9 @@ def test_restore_and_recompute_reproduce_the_run():
     first = snapshot(loop)
     for _ in range(2):  # restorable more than once
         E, graphs = loop.solvers[0].DataDev["E"], loop._graphs
+        loop._eager_left = 2  # as if a window shift had just been stepped
         restore_checkpoint(loop, ck)
+        assert loop._eager_left == 0  # no eager steps pending after a restore
         # same-shape buffers restored in place: captured launches stay valid
         assert loop.it == 4 and loop.solvers[0].DataDev["E"] is E and loop._graphs is graphs
         for _ in range(6):
