@@ -193,7 +193,7 @@ static __global__ void __launch_bounds__(LB_THREADS)
       __syncthreads();
       if (flag == LB_INCL) atomicMin(&s_stop, (u32)threadIdx.x);  // nearest inclusive prefix
       __syncthreads();
-      const u32 stop = s_stop;  // LB_THREADS: none in this round
+      const u32 stop = s_stop;  // LB_THREADS: none in this window
       const bool missing = __syncthreads_or(flag == 0u && threadIdx.x <= stop);
       if (missing && !gave_up) {
         if (++spins < spin_limit) continue;
